@@ -1,0 +1,254 @@
+/*
+ * sylver_gb300: GB300-native numeric factorize + solve for sparse symmetric
+ * systems (multifrontal Cholesky and threshold-pivoted LDL^T), exported with
+ * the reference SyLVER C-ABI so that existing callers relink unchanged.
+ *
+ * Indexing, ownership and error conventions are the reference's:
+ *   - ptr/row are 1-based lower-triangle CSC (ptr is long, row is int);
+ *   - akeep/fkeep are opaque handles allocated by the library and released by
+ *     spldlt_free_akeep/spldlt_free_fkeep;
+ *   - errors come back in inform->flag (<0 error, >0 warning, 0 success);
+ *   - factorize and solve are synchronous.
+ * Factors live in GPU memory owned by fkeep.  There is no CPU fallback: when
+ * no CUDA device is usable, factorize returns SYLVER_ERROR_CUDA_UNKNOWN (-51).
+ */
+#ifndef SYLVER_GB300_H
+#define SYLVER_GB300_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Reference: include/sylver/sylver.h:19-37 (same layout). */
+typedef struct {
+  int flag;
+  int matrix_dup;
+  int matrix_missing_diag;
+  int matrix_outrange;
+  int matrix_rank;
+  int maxdepth;
+  int maxfront;
+  int num_delay;
+  long num_factor;
+  long num_flops;
+  int num_neg;
+  int num_sup;
+  int num_two;
+  int stat;
+  int cuda_error;
+  int cublas_error;
+  char unused[80];
+} sylver_inform_t;
+
+/* Reference: include/sylver/sylver.h:39-71 (same layout). */
+typedef struct {
+  int array_base;
+  int print_level;
+  int unit_diagnostics;
+  int unit_error;
+  int unit_warning;
+  int ordering;
+  int nemin;
+  bool prune_tree;
+  long min_gpu_work;
+  int scaling;
+  int pivot_method;
+  double small;
+  double u;
+  long small_subtree_threshold;
+  int nb;
+  int cpu_topology;
+  bool action;
+  bool use_gpu;
+  double gpu_perf_coeff;
+  int failed_pivot_method;
+  int scheduler;
+} sylver_options_t;
+
+/* Error / warning flags: src/sylver_datatypes_mod.F90:14-45. */
+enum {
+  SYLVER_SUCCESS = 0,
+  SYLVER_ERROR_CALL_SEQUENCE = -1,
+  SYLVER_ERROR_A_N_OOR = -2,
+  SYLVER_ERROR_A_PTR = -3,
+  SYLVER_ERROR_A_ALL_OOR = -4,
+  SYLVER_ERROR_SINGULAR = -5,
+  SYLVER_ERROR_NOT_POS_DEF = -6,
+  SYLVER_ERROR_PTR_ROW = -7,
+  SYLVER_ERROR_ORDER = -8,
+  SYLVER_ERROR_VAL = -9,
+  SYLVER_ERROR_X_SIZE = -10,
+  SYLVER_ERROR_JOB_OOR = -11,
+  SYLVER_ERROR_ALLOCATION = -50,
+  SYLVER_ERROR_CUDA_UNKNOWN = -51,
+  SYLVER_ERROR_UNIMPLEMENTED = -98,
+  SYLVER_ERROR_UNKNOWN = -99,
+  SYLVER_WARNING_IDX_OOR = 1,
+  SYLVER_WARNING_DUP_IDX = 2,
+  SYLVER_WARNING_DUP_AND_OOR = 3,
+  SYLVER_WARNING_MISSING_DIAGONAL = 4,
+  SYLVER_WARNING_MISS_DIAG_OORDUP = 5,
+  SYLVER_WARNING_FACT_SINGULAR = 7
+};
+
+/* Solve job values: src/sylver_datatypes_mod.F90:46-51. */
+enum {
+  SYLVER_SOLVE_JOB_ALL = 0,
+  SYLVER_SOLVE_JOB_FWD = 1,
+  SYLVER_SOLVE_JOB_DIAG = 2,
+  SYLVER_SOLVE_JOB_BWD = 3,
+  SYLVER_SOLVE_JOB_DIAG_BWD = 4
+};
+
+/* ---- public C-ABI (replaces src/interfaces/C/sylver_ciface.F90) ---------- */
+
+/* Replaces sylver_c_init (sylver_ciface.F90:354-364): selects device 0 and
+ * creates the library's stream.  ncpu/ngpu are accepted and recorded. */
+void sylver_init(int ncpu, int ngpu);
+/* Replaces sylver_c_finalize (sylver_ciface.F90:367-375). */
+void sylver_finalize(void);
+/* Replaces sylver_c_default_options (sylver_ciface.F90:304-351). */
+void sylver_default_options(sylver_options_t* options);
+/* Replaces spldlt_c_analyse (sylver_ciface.F90:374-467).  options->ordering
+ * 0 takes `order` (order[i] = 1-based pivot position of variable i); any
+ * other value runs the library's nested dissection. */
+void spldlt_analyse(int n, int* order, long const* ptr, int const* row, double const* val,
+                    void** akeep, bool check, sylver_options_t const* options,
+                    sylver_inform_t* inform);
+/* Replaces spldlt_c_factorize (sylver_ciface.F90:530-631), FP64 factors. */
+void spldlt_factorize(bool posdef, long const* ptr, int const* row, double const* val,
+                      double* scale, void* akeep, void** fkeep,
+                      sylver_options_t const* options, sylver_inform_t* inform);
+/* Replaces spldlt_c_solve (sylver_ciface.F90:634-711).  x is ldx x nrhs,
+ * column-major, overwritten by the solution.  When fkeep holds FP32 factors
+ * (spldlt_factorize_mixed) job 0 runs FP64 iterative refinement. */
+void spldlt_solve(int job, int nrhs, double* x, int ldx, void* akeep, void* fkeep,
+                  sylver_options_t const* options, sylver_inform_t* inform);
+/* Replace spldlt_c_free_akeep / spldlt_c_free_fkeep (sylver_ciface.F90:714-826). */
+void spldlt_free_akeep(void** akeep);
+void spldlt_free_fkeep(void** fkeep);
+
+/* ---- internal C-ABI #2 (replaces src/SymbolicTree.cxx, src/NumericTree*.cxx) */
+
+/* Interoperable options/inform: src/sylver_ciface.hxx:39-87. */
+typedef struct {
+  int print_level;
+  bool action;
+  double small;
+  double u;
+  double multiplier;
+  long small_subtree_threshold;
+  int nb;
+  int pivot_method;
+  int failed_pivot_method;
+  int cpu_topology;
+} sylver_options_c;
+
+typedef struct {
+  int flag;
+  int num_delay;
+  int num_neg;
+  int num_two;
+  int num_zero;
+  int maxfront;
+  int not_first_pass;
+  int not_second_pass;
+} sylver_inform_c;
+
+/* Replaces spldlt_create_symbolic_tree (src/SymbolicTree.cxx:110-137).  The
+ * arrays are copied; nsubtrees/subtrees/small/contrib_dest/exec_loc are
+ * accepted for signature compatibility (no CPU subtrees exist here). */
+void* spldlt_create_symbolic_tree(void* akeep, int n, int nnodes, int const* sptr,
+                                  int const* sparent, long const* rptr, int const* rlist,
+                                  long const* nptr, long const* nlist, int nsubtrees,
+                                  int const* subtrees, int const* small,
+                                  int const* contrib_dest, int const* exec_loc);
+void spldlt_destroy_symbolic_tree(void* symbolic_tree);
+
+/* Replace spldlt_create_numeric_tree_dbl (src/NumericTree.cxx:27-45) and
+ * spldlt_create_numeric_tree_posdef_dbl (src/NumericTreePosdef.cxx:19-35).
+ * aval is host memory (values in the order nlist refers to). */
+void* spldlt_create_numeric_tree_dbl(bool posdef, void* fkeep, void* symbolic_tree,
+                                     double* aval, const double* scaling,
+                                     void** child_contrib, sylver_options_c* options,
+                                     sylver_inform_c* inform);
+void* spldlt_create_numeric_tree_posdef_dbl(void* fkeep, void* symbolic_tree, double* aval,
+                                            void** child_contrib, sylver_options_c* options,
+                                            sylver_inform_c* inform);
+void spldlt_destroy_numeric_tree_dbl(bool posdef, void* tree);
+void spldlt_destroy_numeric_tree_posdef_dbl(void* tree);
+
+/* Replace spldlt_tree_solve_{fwd,bwd,diag,diag_bwd}_dbl
+ * (src/NumericTree.cxx:56-136) and the _posdef_ fwd/bwd
+ * (src/NumericTreePosdef.cxx:46-83).  x is host memory, indexed in pivot
+ * order as the reference's tree solves expect; returns a reference flag. */
+int spldlt_tree_solve_fwd_dbl(bool posdef, void const* tree, int nrhs, double* x, int ldx);
+int spldlt_tree_solve_bwd_dbl(bool posdef, void const* tree, int nrhs, double* x, int ldx);
+int spldlt_tree_solve_diag_dbl(bool posdef, void const* tree, int nrhs, double* x, int ldx);
+int spldlt_tree_solve_diag_bwd_dbl(bool posdef, void const* tree, int nrhs, double* x, int ldx);
+int spldlt_tree_solve_fwd_posdef_dbl(void const* tree, int nrhs, double* x, int ldx);
+int spldlt_tree_solve_bwd_posdef_dbl(void const* tree, int nrhs, double* x, int ldx);
+
+/* ---- GB300 extensions (no reference counterpart) ------------------------- */
+
+/* Factor precision selector for spldlt_factorize_mixed. */
+enum { SYLVER_GB300_FP64 = 0, SYLVER_GB300_FP32 = 1 };
+
+/* Same contract as spldlt_factorize; `precision` chooses FP64 factors or FP32
+ * factors (FP32 arithmetic, FP64 pivot tests).  FP32 factors make
+ * spldlt_solve refine in FP64 until the scaled backward error is <= ir_tol
+ * (or ir_max_iter iterations). */
+void spldlt_factorize_mixed(bool posdef, long const* ptr, int const* row, double const* val,
+                            double* scale, void* akeep, void** fkeep,
+                            sylver_options_t const* options, sylver_inform_t* inform,
+                            int precision, double ir_tol, int ir_max_iter);
+
+/* Device-resident variants: val_dev / x_dev are CUDA device pointers (same
+ * layouts as the host calls).  Used when inputs already live in HBM. */
+void spldlt_factorize_device(bool posdef, double const* val_dev, void* akeep, void** fkeep,
+                             sylver_options_t const* options, sylver_inform_t* inform,
+                             int precision, double ir_tol, int ir_max_iter);
+void spldlt_solve_device(int job, int nrhs, double* x_dev, int ldx, void* akeep, void* fkeep,
+                         sylver_options_t const* options, sylver_inform_t* inform);
+
+/* Refinement statistics of the last solve on fkeep: iterations taken and the
+ * final max-over-RHS scaled backward error.  Returns 0, or -1 for a null fkeep. */
+int sylver_gb300_solve_stats(void const* fkeep, int* ir_iters, double* bwd_err);
+
+/* Symbolic arrays of an analysis (1-based, reference layout).  Pass null for
+ * any array not wanted; sizes: sptr/rptr/nptr nnodes+1, sparent nnodes,
+ * rlist rptr[nnodes]-1, nlist 2*(nptr[nnodes]-1), perm n (1-based position). */
+int sylver_gb300_akeep_sizes(void const* akeep, int* n, int* nnodes, long* rlist_len,
+                             long* nlist_len);
+int sylver_gb300_akeep_arrays(void const* akeep, int* sptr, int* sparent, long* rptr,
+                              int* rlist, long* nptr, long* nlist, int* perm);
+
+/* Pivot-order D^-1 of an LDL^T factorization (2 entries per pivot, the
+ * reference's storage: 1x1 [d, 0], 2x2 [a, b, Inf, c]) and the pivot-order
+ * permutation applied by delays; for tests.  Returns number of pivots. */
+int sylver_gb300_fkeep_diag(void const* fkeep, double* d, int* piv_order);
+
+/* The CUDA stream (cudaStream_t) all library work is issued on; callers that
+ * time with CUDA events record them on this stream. */
+void* sylver_gb300_stream(void);
+
+/* Re-run the factorization held by fkeep with one CUDA event pair around
+ * every launch (no graph) and accumulate per kernel kind:
+ * 0 memset, 1 init-A, 2 extend-add, 3 small fronts, 4 panel, 5 update, 6 LDL^T
+ * diagonal/apply kernels.  ms[k] = total milliseconds, launches[k] = count,
+ * flops[k] = algorithmic flops (update kernels: lower-triangle tile work).
+ * Arrays hold 8 entries.  Returns 0 or a reference flag. */
+int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, long* launches,
+                                double* flops);
+
+/* Counters of the last factorization on fkeep (kernel launches, levels). */
+int sylver_gb300_fkeep_counters(void const* fkeep, long* kernel_launches, int* nlevels,
+                                double* factor_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SYLVER_GB300_H */

@@ -1,0 +1,145 @@
+// Shared device-side definitions: task descriptors of the level schedule,
+// status bits written by kernels, and the launcher entry points of each
+// kernel translation unit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+
+namespace sylver_gb300 {
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+
+#define SG_CUDA(call)                                                              \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      throw ::sylver_gb300::CudaError(std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// Status bits accumulated (atomicOr) by kernels into one device word.
+enum : unsigned {
+  ST_NOT_POSDEF = 1u,     // non-positive / NaN pivot in a Cholesky front
+  ST_ZERO_PIVOT = 2u,     // LDL^T eliminated a zero pivot (action = true)
+  ST_SINGULAR = 4u,       // LDL^T zero pivot with action = false
+  ST_OVERFLOW = 8u,       // a front outgrew its planned storage
+  ST_BAD_INDEX = 16u,     // an index map pointed outside its front
+};
+
+// ---------------------------------------------------------------------------
+// Task descriptors (one per CTA unless stated).
+
+// Dense front stored column-major, full m x m square at arena[off], leading
+// dimension ld; only the lower triangle is meaningful.
+struct FrontDesc {
+  int64_t off;
+  int ld, m, n;   // rows, fully-summed columns
+  int rl;         // offset of the front's pivot-order row list (0-based ints)
+  int pad;
+};
+
+// Whole small front factorized by one CTA in shared memory.
+struct SmallTask {
+  int64_t off;
+  int ld, m, n, pad;
+};
+
+// Panel step: Cholesky of the w x w diagonal block at (k0,k0) and the
+// triangular solve of rows [r0, r1) of columns [k0, k0+w).
+struct PanelTask {
+  int64_t off;
+  int ld, k0, w, r0, r1, pad;
+};
+
+// Tile update C -= A_rows * A_cols^T inside one front:
+// rows [row0, min(row0+TM,rowEnd)), cols [col0, min(col0+TN,colEnd)),
+// inner index k in [k0, k1).
+struct UpdTask {
+  int64_t off;
+  int ld, row0, col0, rowEnd, colEnd, k0, k1, pad;
+};
+
+// Extend-add of one child contribution column into its parent.
+struct ChildDesc {
+  int64_t cb_off;   // child CB (0,0) in the arena
+  int64_t p_off;    // parent front (0,0)
+  int ld_c, ld_p, mc, map_off;
+};
+struct EaItem {
+  int child;  // index into ChildDesc array
+  int col;    // CB column
+};
+
+// ---------------------------------------------------------------------------
+// Launchers (kernels_factor.cu)
+
+template <typename T>
+void prepare_factor_kernels();
+template <typename T>
+void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
+                   int64_t count, bool atomic, cudaStream_t s);
+template <typename T>
+void launch_extend_add(T* arena, const ChildDesc* cd, const EaItem* items, const int* maps,
+                       int nitems, cudaStream_t s);
+template <typename T>
+void launch_small_chol(T* arena, const SmallTask* t, int ntask, int maxm, unsigned* status,
+                       cudaStream_t s);
+template <typename T>
+void launch_panel_chol(T* arena, const PanelTask* t, int ntask, unsigned* status,
+                       cudaStream_t s);
+template <typename T>
+void launch_update(T* arena, const UpdTask* t, int ntask, cudaStream_t s);
+
+template <typename T> struct Tiles;
+template <> struct Tiles<double> {
+  static constexpr int TM = 64, TN = 64, NB = 32, RT = 128, SMALL_M = 96;
+};
+template <> struct Tiles<float> {
+  static constexpr int TM = 128, TN = 128, NB = 64, RT = 128, SMALL_M = 128;
+};
+
+// ---------------------------------------------------------------------------
+// Launchers (kernels_solve.cu).  ACC is the solve's accumulation type.
+// scr_off[f] is the first scratch row of front f; its slab is m x nrhs.
+
+template <typename T, typename ACC>
+void launch_solve_fwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
+                      ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
+                      bool unit_diag, cudaStream_t s);
+template <typename T, typename ACC>
+void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
+                      ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
+                      bool unit_diag, cudaStream_t s);
+
+template <typename ACC>
+void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, int n, int nrhs,
+                       cudaStream_t s);
+template <typename ACC>
+void launch_permute_out_add(const ACC* xp, const int* perm, double* x, int ldx, int n,
+                            int nrhs, bool add, cudaStream_t s);
+
+// r = b - A x for a full CSR matrix (user order), FP64.
+void launch_residual(const int64_t* rowptr, const int* col, const double* aval, int n,
+                     const double* x, int ldx, const double* b, int ldb, double* r, int nrhs,
+                     cudaStream_t s);
+// norms[3*r+0] = max|res|, [3r+1] = max|x|, [3r+2] = max|b|  (atomic max).
+void launch_maxnorms(const double* res, const double* x, int ldx, const double* b, int ldb,
+                     int n, int nrhs, double* norms, cudaStream_t s);
+// out = max_i sum_j |a_ij| (atomic max into *out).
+void launch_rownorm_inf(const int64_t* rowptr, const double* aval, int n, double* out,
+                        cudaStream_t s);
+// clean values: cval[k] = sum val[src[srcptr[k]..srcptr[k+1])]; then full
+// CSR values aval[e] = cval[eidx[e]].
+void launch_gather_clean(const double* val, const int64_t* srcptr, const int64_t* src,
+                         int64_t nclean, double* cval, cudaStream_t s);
+void launch_gather(const double* cval, const int64_t* idx, int64_t count, double* out,
+                   cudaStream_t s);
+void launch_axpy_inplace(double* x, int ldx, const double* d, int n, int nrhs, cudaStream_t s);
+
+// LDL^T launchers (kernels_ldlt.cu) are declared in ldlt.hpp.
+
+}  // namespace sylver_gb300

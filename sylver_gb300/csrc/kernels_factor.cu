@@ -1,0 +1,337 @@
+// Cholesky-side kernels of the level schedule: A->front initialisation,
+// extend-add of contribution blocks, small fronts factorised whole in shared
+// memory, panel Cholesky + triangular solve, and the tile update
+// C -= A_rows A_cols^T used for both the trailing fully-summed update and the
+// contribution-block (Schur complement) update.
+//
+// Reference behaviour replaced:
+//   init_a_block / init_node         src/kernels/assemble.hxx:162-214
+//   assemble_block / _contrib_block  src/kernels/assemble.hxx:231-286, :344-425
+//   factorize_diag_block + solve_block + update_block + update_diag_block
+//                                     src/kernels/factor.hxx:56-260,
+//                                     src/factor.hxx:19-148
+#include "device.hpp"
+
+namespace sylver_gb300 {
+
+namespace {
+
+template <typename T> __device__ __forceinline__ void atomic_add(T* p, T v) { atomicAdd(p, v); }
+
+// ---------------------------------------------------------------------------
+// arena[dst[k]] (+)= val[src[k]]  -- assembly of original entries.
+template <typename T>
+__global__ void k_init_a(T* __restrict__ arena, const double* __restrict__ val,
+                         const int64_t* __restrict__ src, const int64_t* __restrict__ dst,
+                         int64_t count, bool atomic) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (; k < count; k += stride) {
+    T v = (T)val[src[k]];
+    if (atomic) atomic_add(arena + dst[k], v);
+    else arena[dst[k]] = v;
+  }
+}
+
+// One warp per (child, CB column): parent(map[i], map[j]) += cb(i, j), i >= j.
+// Two children of one parent may hit the same parent entry, hence atomics.
+template <typename T>
+__global__ void k_extend_add(T* __restrict__ arena, const ChildDesc* __restrict__ cd,
+                             const EaItem* __restrict__ items, const int* __restrict__ maps,
+                             int nitems) {
+  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (warp >= nitems) return;
+  EaItem it = items[warp];
+  ChildDesc c = cd[it.child];
+  const int* map = maps + c.map_off;
+  int j = it.col;
+  int pj = map[j];
+  const T* src = arena + c.cb_off + (int64_t)j * c.ld_c;
+  T* dst = arena + c.p_off + (int64_t)pj * c.ld_p;
+  for (int i = j + lane; i < c.mc; i += 32) atomic_add(dst + map[i], src[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Whole-front partial Cholesky in shared memory (m <= SMALL_M): eliminate the
+// first n columns and update the contribution block in place.
+template <typename T>
+__global__ void __launch_bounds__(256) k_small_chol(T* __restrict__ arena,
+                                                    const SmallTask* __restrict__ tasks,
+                                                    unsigned* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s = reinterpret_cast<T*>(smem_raw);
+  SmallTask t = tasks[blockIdx.x];
+  const int m = t.m, n = t.n, lds = m + 1;
+  T* a = arena + t.off;
+  for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+    int i = idx % m, j = idx / m;
+    if (i >= j) s[j * lds + i] = a[(int64_t)j * t.ld + i];
+  }
+  __syncthreads();
+  __shared__ T dkk;
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      T d = s[k * lds + k];
+      if (!(d > T(0))) {
+        atomicOr(status, ST_NOT_POSDEF);
+        d = T(1);
+      }
+      d = sqrt(d);
+      s[k * lds + k] = d;
+      dkk = T(1) / d;
+    }
+    __syncthreads();
+    T inv = dkk;
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) s[k * lds + i] *= inv;
+    __syncthreads();
+    const int w = m - k - 1;
+    for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
+      int i = k + 1 + idx % w, j = k + 1 + idx / w;
+      if (i >= j) s[j * lds + i] -= s[k * lds + i] * s[k * lds + j];
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < m * m; idx += blockDim.x) {
+    int i = idx % m, j = idx / m;
+    if (i >= j) a[(int64_t)j * t.ld + i] = s[j * lds + i];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Panel step: each CTA recomputes the NB x NB diagonal Cholesky (cheap, and
+// it avoids a launch + grid-wide dependency), then solves its row tile
+// L_r = A_r L_kk^-T.  The CTA whose tile starts at k0 writes L_kk back.
+template <typename T, int NB, int RT>
+__global__ void __launch_bounds__(RT) k_panel_chol(T* __restrict__ arena,
+                                                   const PanelTask* __restrict__ tasks,
+                                                   unsigned* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);  // NB x (NB+1), column-major
+  T* R = D + NB * (NB + 1);               // NB x (RT+1): R[k*(RT+1) + row]
+  __shared__ T dinv[NB];
+  PanelTask t = tasks[blockIdx.x];
+  T* a = arena + t.off;
+  const int ld = t.ld, k0 = t.k0, w = t.w;
+  const int tid = threadIdx.x;
+  constexpr int LDD = NB + 1, LDR = RT + 1;
+  for (int idx = tid; idx < w * w; idx += RT) {
+    int i = idx % w, j = idx / w;
+    D[j * LDD + i] = (i >= j) ? a[(int64_t)(k0 + j) * ld + k0 + i] : T(0);
+  }
+  // row tile load overlaps with the diagonal factorisation
+  const int rstart = max(t.r0, k0 + w);
+  const int r = rstart + tid;
+  const bool has_row = r < t.r1;
+  if (has_row)
+    for (int k = 0; k < w; ++k) R[k * LDR + tid] = a[(int64_t)(k0 + k) * ld + r];
+  __syncthreads();
+  for (int k = 0; k < w; ++k) {
+    if (tid == 0) {
+      T d = D[k * LDD + k];
+      if (!(d > T(0))) {
+        atomicOr(status, ST_NOT_POSDEF);
+        d = T(1);
+      }
+      d = sqrt(d);
+      D[k * LDD + k] = d;
+      dinv[k] = T(1) / d;
+    }
+    __syncthreads();
+    T inv = dinv[k];
+    for (int i = k + 1 + tid; i < w; i += RT) D[k * LDD + i] *= inv;
+    __syncthreads();
+    const int ww = w - k - 1;
+    for (int idx = tid; idx < ww * ww; idx += RT) {
+      int i = k + 1 + idx % ww, j = k + 1 + idx / ww;
+      if (i >= j) D[j * LDD + i] -= D[k * LDD + i] * D[k * LDD + j];
+    }
+    __syncthreads();
+  }
+  if (t.r0 <= k0) {
+    for (int idx = tid; idx < w * w; idx += RT) {
+      int i = idx % w, j = idx / w;
+      if (i >= j) a[(int64_t)(k0 + j) * ld + k0 + i] = D[j * LDD + i];
+    }
+  }
+  if (has_row) {
+    // x L_kk^T = a_r  (forward substitution along the row)
+    for (int j = 0; j < w; ++j) {
+      T x = R[j * LDR + tid] * dinv[j];
+      R[j * LDR + tid] = x;
+      for (int k = j + 1; k < w; ++k) R[k * LDR + tid] -= x * D[j * LDD + k];
+    }
+    for (int k = 0; k < w; ++k) a[(int64_t)(k0 + k) * ld + r] = R[k * LDR + tid];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// SIMT tile update C[rows, cols] -= sum_k A[rows,k] A[cols,k] with a 16x16
+// thread grid, RMxRN register micro-tiles split in two halves (rows
+// ty*RM/2.. and TM/2+ty*RM/2..) and double-buffered KT-deep shared tiles.
+template <typename T, int TM, int TN, int KT>
+__global__ void __launch_bounds__(256) k_update(T* __restrict__ arena,
+                                                const UpdTask* __restrict__ tasks) {
+  constexpr int RM = TM / 16, RN = TN / 16;
+  constexpr int HM = RM / 2, HN = RN / 2;
+  constexpr int LA = (KT * TM) / 256, LB = (KT * TN) / 256;
+  __shared__ __align__(16) T As[2][KT][TM];
+  __shared__ __align__(16) T Bs[2][KT][TN];
+  const UpdTask t = tasks[blockIdx.x];
+  T* base = arena + t.off;
+  const int ld = t.ld;
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  T ra[LA], rb[LB];
+  auto gload = [&](int kc) {
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      int e = tid + q * 256;
+      int i = e % TM, kk = e / TM;
+      int row = t.row0 + i, k = kc + kk;
+      ra[q] = (row < t.rowEnd && k < t.k1) ? base[(int64_t)k * ld + row] : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      int e = tid + q * 256;
+      int i = e % TN, kk = e / TN;
+      int col = t.col0 + i, k = kc + kk;
+      rb[q] = (col < t.colEnd && k < t.k1) ? base[(int64_t)k * ld + col] : T(0);
+    }
+  };
+  auto sstore = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < LA; ++q) {
+      int e = tid + q * 256;
+      As[buf][e / TM][e % TM] = ra[q];
+    }
+#pragma unroll
+    for (int q = 0; q < LB; ++q) {
+      int e = tid + q * 256;
+      Bs[buf][e / TN][e % TN] = rb[q];
+    }
+  };
+  T acc[RM][RN];
+#pragma unroll
+  for (int i = 0; i < RM; ++i)
+#pragma unroll
+    for (int j = 0; j < RN; ++j) acc[i][j] = T(0);
+
+  int kc = t.k0;
+  gload(kc);
+  sstore(0);
+  __syncthreads();
+  int buf = 0;
+  for (; kc < t.k1; kc += KT) {
+    const bool more = kc + KT < t.k1;
+    if (more) gload(kc + KT);
+#pragma unroll
+    for (int kk = 0; kk < KT; ++kk) {
+      T av[RM], bv[RN];
+#pragma unroll
+      for (int i = 0; i < HM; ++i) {
+        av[i] = As[buf][kk][ty * HM + i];
+        av[HM + i] = As[buf][kk][TM / 2 + ty * HM + i];
+      }
+#pragma unroll
+      for (int j = 0; j < HN; ++j) {
+        bv[j] = Bs[buf][kk][tx * HN + j];
+        bv[HN + j] = Bs[buf][kk][TN / 2 + tx * HN + j];
+      }
+#pragma unroll
+      for (int i = 0; i < RM; ++i)
+#pragma unroll
+        for (int j = 0; j < RN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+    }
+    if (more) {
+      sstore(buf ^ 1);
+      __syncthreads();
+      buf ^= 1;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < RM; ++i) {
+    int row = t.row0 + ((i < HM) ? ty * HM + i : TM / 2 + ty * HM + (i - HM));
+    if (row >= t.rowEnd) continue;
+#pragma unroll
+    for (int j = 0; j < RN; ++j) {
+      int col = t.col0 + ((j < HN) ? tx * HN + j : TN / 2 + tx * HN + (j - HN));
+      if (col >= t.colEnd || col > row) continue;
+      base[(int64_t)col * ld + row] -= acc[i][j];
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+template <typename T>
+void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
+                   int64_t count, bool atomic, cudaStream_t s) {
+  if (count <= 0) return;
+  int64_t blocks = std::min<int64_t>((count + 255) / 256, 152 * 32);
+  k_init_a<T><<<(int)blocks, 256, 0, s>>>(arena, val, src, dst, count, atomic);
+}
+
+template <typename T>
+void launch_extend_add(T* arena, const ChildDesc* cd, const EaItem* items, const int* maps,
+                       int nitems, cudaStream_t s) {
+  if (nitems <= 0) return;
+  int blocks = (nitems + 7) / 8;
+  k_extend_add<T><<<blocks, 256, 0, s>>>(arena, cd, items, maps, nitems);
+}
+
+template <typename T>
+static size_t panel_smem() {
+  constexpr int NB = Tiles<T>::NB, RT = Tiles<T>::RT;
+  return sizeof(T) * ((size_t)NB * (NB + 1) + (size_t)NB * (RT + 1));
+}
+
+// Opt-in shared memory sizes; called once per device before any launch (and
+// before stream capture).
+template <typename T>
+void prepare_factor_kernels() {
+  constexpr int SM = Tiles<T>::SMALL_M;
+  SG_CUDA(cudaFuncSetAttribute(k_small_chol<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(T) * SM * (SM + 1))));
+  SG_CUDA(cudaFuncSetAttribute(k_panel_chol<T, Tiles<T>::NB, Tiles<T>::RT>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)panel_smem<T>()));
+}
+
+template <typename T>
+void launch_small_chol(T* arena, const SmallTask* t, int ntask, int maxm, unsigned* status,
+                       cudaStream_t s) {
+  if (ntask <= 0) return;
+  size_t smem = sizeof(T) * (size_t)maxm * (maxm + 1);
+  k_small_chol<T><<<ntask, 256, smem, s>>>(arena, t, status);
+}
+
+template <typename T>
+void launch_panel_chol(T* arena, const PanelTask* t, int ntask, unsigned* status,
+                       cudaStream_t s) {
+  if (ntask <= 0) return;
+  constexpr int NB = Tiles<T>::NB, RT = Tiles<T>::RT;
+  k_panel_chol<T, NB, RT><<<ntask, RT, panel_smem<T>(), s>>>(arena, t, status);
+}
+
+template <typename T>
+void launch_update(T* arena, const UpdTask* t, int ntask, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_update<T, Tiles<T>::TM, Tiles<T>::TN, 16><<<ntask, 256, 0, s>>>(arena, t);
+}
+
+#define SG_INST(T)                                                                          \
+  template void prepare_factor_kernels<T>();                                                 \
+  template void launch_init_a<T>(T*, const double*, const int64_t*, const int64_t*, int64_t, \
+                                 bool, cudaStream_t);                                       \
+  template void launch_extend_add<T>(T*, const ChildDesc*, const EaItem*, const int*, int,   \
+                                     cudaStream_t);                                         \
+  template void launch_small_chol<T>(T*, const SmallTask*, int, int, unsigned*, cudaStream_t); \
+  template void launch_panel_chol<T>(T*, const PanelTask*, int, unsigned*, cudaStream_t);    \
+  template void launch_update<T>(T*, const UpdTask*, int, cudaStream_t);
+SG_INST(float)
+SG_INST(double)
+#undef SG_INST
+
+}  // namespace sylver_gb300

@@ -1,0 +1,360 @@
+// Level-batched triangular solves, permutation, FP64 residual and norms for
+// iterative refinement.
+//
+// Reference behaviour replaced:
+//   NumericTreePosdef::solve_fwd / solve_bwd   src/NumericTreePosdef.hxx:357-450
+//   NumericTree::solve_fwd / solve_diag_bwd     src/NumericTree.hxx:408-520
+//   permute + scale wrapper                     src/spldlt_factorize_mod.F90:901-1060
+//   backward error (driver)                     drivers/spldlt_test.F90:216-267
+//
+// One CTA handles one front of a level.  The front's right-hand-side rows are
+// gathered into a per-front scratch slab (m x nrhs), processed in 32-column
+// blocks (warp 0 solves the diagonal block with shuffles, all warps apply the
+// off-diagonal block), and scattered back; rows below the pivots go to
+// ancestors with atomics because sibling fronts of a level share them.
+#include "device.hpp"
+
+namespace sylver_gb300 {
+
+namespace {
+
+constexpr int SB = 32;      // column block
+constexpr int MAXR = 32;    // right-hand sides per launch
+constexpr int RC = 8;       // right-hand sides per register chunk
+
+template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
+
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
+                                                   const FrontDesc* __restrict__ fr,
+                                                   const int* __restrict__ rlist,
+                                                   ACC* __restrict__ x, int n, int nrhs,
+                                                   ACC* __restrict__ scratch,
+                                                   const int64_t* __restrict__ scr_off,
+                                                   bool unit) {
+  __shared__ ACC y[SB][MAXR];
+  const FrontDesc f = fr[blockIdx.x];
+  const T* L = arena + f.off;
+  const int ld = f.ld, m = f.m, nc = f.n;
+  const int* rl = rlist + f.rl;
+  ACC* xs = scratch + scr_off[blockIdx.x] * nrhs;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
+    int i = idx % m, r = idx / m;
+    xs[idx] = (i < nc) ? x[(int64_t)r * n + rl[i]] : ACC(0);
+  }
+  __syncthreads();
+  for (int c0 = 0; c0 < nc; c0 += SB) {
+    const int bw = min(SB, nc - c0);
+    if (warp == 0) {
+      for (int r = 0; r < nrhs; ++r) {
+        ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] : ACC(0);
+        for (int kk = 0; kk < bw; ++kk) {
+          ACC vk = __shfl_sync(0xffffffffu, v, kk);
+          if (!unit) vk = vk / (ACC)L[(int64_t)(c0 + kk) * ld + c0 + kk];
+          if (lane == kk) v = vk;
+          if (lane > kk && lane < bw) v -= (ACC)L[(int64_t)(c0 + kk) * ld + c0 + lane] * vk;
+        }
+        if (lane < bw) {
+          xs[(int64_t)r * m + c0 + lane] = v;
+          y[lane][r] = v;
+        }
+      }
+    }
+    __syncthreads();
+    const int c1 = c0 + bw;
+    for (int i = c1 + tid; i < m; i += blockDim.x) {
+      for (int r0 = 0; r0 < nrhs; r0 += RC) {
+        ACC acc[RC];
+#pragma unroll
+        for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
+        for (int kk = 0; kk < bw; ++kk) {
+          ACC l = (ACC)L[(int64_t)(c0 + kk) * ld + i];
+#pragma unroll
+          for (int q = 0; q < RC; ++q) acc[q] += l * y[kk][min(r0 + q, MAXR - 1)];
+        }
+#pragma unroll
+        for (int q = 0; q < RC; ++q)
+          if (r0 + q < nrhs) xs[(int64_t)(r0 + q) * m + i] -= acc[q];
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
+    int i = idx % m, r = idx / m;
+    ACC* dst = x + (int64_t)r * n + rl[i];
+    if (i < nc) *dst = xs[idx];
+    else aadd(dst, xs[idx]);
+  }
+}
+
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
+                                                   const FrontDesc* __restrict__ fr,
+                                                   const int* __restrict__ rlist,
+                                                   ACC* __restrict__ x, int n, int nrhs,
+                                                   ACC* __restrict__ scratch,
+                                                   const int64_t* __restrict__ scr_off,
+                                                   bool unit) {
+  __shared__ ACC tt[SB][MAXR];
+  const FrontDesc f = fr[blockIdx.x];
+  const T* L = arena + f.off;
+  const int ld = f.ld, m = f.m, nc = f.n;
+  const int* rl = rlist + f.rl;
+  ACC* xs = scratch + scr_off[blockIdx.x] * nrhs;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nwarps = blockDim.x >> 5;
+  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
+    int i = idx % m, r = idx / m;
+    xs[idx] = x[(int64_t)r * n + rl[i]];
+  }
+  __syncthreads();
+  const int nblk = (nc + SB - 1) / SB;
+  for (int b = nblk - 1; b >= 0; --b) {
+    const int c0 = b * SB, bw = min(SB, nc - c0), c1 = c0 + bw;
+    for (int kk = warp; kk < bw; kk += nwarps) {
+      const T* col = L + (int64_t)(c0 + kk) * ld;
+      for (int r0 = 0; r0 < nrhs; r0 += RC) {
+        ACC acc[RC];
+#pragma unroll
+        for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
+        for (int i = c1 + lane; i < m; i += 32) {
+          ACC l = (ACC)col[i];
+#pragma unroll
+          for (int q = 0; q < RC; ++q)
+            if (r0 + q < nrhs) acc[q] += l * xs[(int64_t)(r0 + q) * m + i];
+        }
+#pragma unroll
+        for (int q = 0; q < RC; ++q) {
+          ACC s = acc[q];
+          for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+          if (lane == 0 && r0 + q < nrhs) tt[kk][r0 + q] = s;
+        }
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      for (int r = 0; r < nrhs; ++r) {
+        ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] - tt[lane][r] : ACC(0);
+        for (int kk = bw - 1; kk >= 0; --kk) {
+          if (lane == kk && !unit) v = v / (ACC)L[(int64_t)(c0 + kk) * ld + c0 + kk];
+          ACC zk = __shfl_sync(0xffffffffu, v, kk);
+          if (lane < kk) v -= (ACC)L[(int64_t)(c0 + lane) * ld + c0 + kk] * zk;
+        }
+        if (lane < bw) xs[(int64_t)r * m + c0 + lane] = v;
+      }
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
+    int i = idx % m, r = idx / m;
+    if (i < nc) x[(int64_t)r * n + rl[i]] = xs[idx];
+  }
+}
+
+template <typename ACC>
+__global__ void k_permute_in(const double* __restrict__ x, int ldx, ACC* __restrict__ xp,
+                             const int* __restrict__ perm, int n, int nrhs) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * nrhs) return;
+  int i = (int)(idx % n), r = (int)(idx / n);
+  xp[(int64_t)r * n + perm[i]] = (ACC)x[(int64_t)r * ldx + i];
+}
+
+template <typename ACC>
+__global__ void k_permute_out(const ACC* __restrict__ xp, const int* __restrict__ perm,
+                              double* __restrict__ x, int ldx, int n, int nrhs, bool add) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * nrhs) return;
+  int i = (int)(idx % n), r = (int)(idx / n);
+  double v = (double)xp[(int64_t)r * n + perm[i]];
+  double* d = x + (int64_t)r * ldx + i;
+  *d = add ? *d + v : v;
+}
+
+__global__ void k_residual(const int64_t* __restrict__ rowptr, const int* __restrict__ col,
+                           const double* __restrict__ a, int n, const double* __restrict__ x,
+                           int ldx, const double* __restrict__ b, int ldb,
+                           double* __restrict__ res, int nrhs) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t p0 = rowptr[i], p1 = rowptr[i + 1];
+  for (int r0 = 0; r0 < nrhs; r0 += RC) {
+    double acc[RC];
+#pragma unroll
+    for (int q = 0; q < RC; ++q) acc[q] = 0.0;
+    for (int64_t p = p0; p < p1; ++p) {
+      double v = a[p];
+      int j = col[p];
+#pragma unroll
+      for (int q = 0; q < RC; ++q)
+        if (r0 + q < nrhs) acc[q] = fma(v, x[(int64_t)(r0 + q) * ldx + j], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < RC; ++q)
+      if (r0 + q < nrhs)
+        res[(int64_t)(r0 + q) * n + i] = b[(int64_t)(r0 + q) * ldb + i] - acc[q];
+  }
+}
+
+__device__ __forceinline__ void atomic_max_nonneg(double* p, double v) {
+  // non-negative doubles order like their bit patterns
+  atomicMax(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__double_as_longlong(v));
+}
+
+__global__ void k_maxnorms(const double* __restrict__ res, const double* __restrict__ x,
+                           int ldx, const double* __restrict__ b, int ldb, int n, int nrhs,
+                           double* norms) {
+  const int r = blockIdx.y;
+  double mr = 0.0, mx = 0.0, mb = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    mr = fmax(mr, fabs(res[(int64_t)r * n + i]));
+    mx = fmax(mx, fabs(x[(int64_t)r * ldx + i]));
+    mb = fmax(mb, fabs(b[(int64_t)r * ldb + i]));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_nonneg(&norms[3 * r + 0], mr);
+    atomic_max_nonneg(&norms[3 * r + 1], mx);
+    atomic_max_nonneg(&norms[3 * r + 2], mb);
+  }
+}
+
+__global__ void k_rownorm(const int64_t* __restrict__ rowptr, const double* __restrict__ a,
+                          int n, double* out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double s = 0.0;
+  if (i < n)
+    for (int64_t p = rowptr[i]; p < rowptr[i + 1]; ++p) s += fabs(a[p]);
+  for (int o = 16; o > 0; o >>= 1) s = fmax(s, __shfl_xor_sync(0xffffffffu, s, o));
+  if ((threadIdx.x & 31) == 0) atomic_max_nonneg(out, s);
+}
+
+__global__ void k_gather_clean(const double* __restrict__ val, const int64_t* __restrict__ srcptr,
+                               const int64_t* __restrict__ src, int64_t nclean,
+                               double* __restrict__ cval) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nclean) return;
+  double s = 0.0;
+  for (int64_t q = srcptr[k]; q < srcptr[k + 1]; ++q) s += val[src[q]];
+  cval[k] = s;
+}
+
+__global__ void k_gather(const double* __restrict__ c, const int64_t* __restrict__ idx,
+                         int64_t count, double* __restrict__ out) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < count) out[k] = c[idx[k]];
+}
+
+__global__ void k_axpy(double* __restrict__ x, int ldx, const double* __restrict__ d, int n,
+                       int nrhs) {
+  int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (int64_t)n * nrhs) return;
+  int i = (int)(idx % n), r = (int)(idx / n);
+  x[(int64_t)r * ldx + i] += d[(int64_t)r * n + i];
+}
+
+inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
+
+}  // namespace
+
+template <typename T, typename ACC>
+void launch_solve_fwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
+                      ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
+                      bool unit_diag, cudaStream_t s) {
+  if (nfronts <= 0) return;
+  if (nrhs > MAXR) throw CudaError("solve: more than 32 right-hand sides per launch");
+  k_solve_fwd<T, ACC><<<nfronts, 256, 0, s>>>(arena, fr, rlist, x, n, nrhs, scratch, scr_off,
+                                              unit_diag);
+}
+
+template <typename T, typename ACC>
+void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
+                      ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
+                      bool unit_diag, cudaStream_t s) {
+  if (nfronts <= 0) return;
+  if (nrhs > MAXR) throw CudaError("solve: more than 32 right-hand sides per launch");
+  k_solve_bwd<T, ACC><<<nfronts, 256, 0, s>>>(arena, fr, rlist, x, n, nrhs, scratch, scr_off,
+                                              unit_diag);
+}
+
+template <typename ACC>
+void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, int n, int nrhs,
+                       cudaStream_t s) {
+  int64_t c = (int64_t)n * nrhs;
+  if (c == 0) return;
+  k_permute_in<ACC><<<nblocks(c, 256), 256, 0, s>>>(x, ldx, xp, perm, n, nrhs);
+}
+
+template <typename ACC>
+void launch_permute_out_add(const ACC* xp, const int* perm, double* x, int ldx, int n,
+                            int nrhs, bool add, cudaStream_t s) {
+  int64_t c = (int64_t)n * nrhs;
+  if (c == 0) return;
+  k_permute_out<ACC><<<nblocks(c, 256), 256, 0, s>>>(xp, perm, x, ldx, n, nrhs, add);
+}
+
+void launch_residual(const int64_t* rowptr, const int* col, const double* aval, int n,
+                     const double* x, int ldx, const double* b, int ldb, double* r, int nrhs,
+                     cudaStream_t s) {
+  if (n == 0) return;
+  k_residual<<<nblocks(n, 128), 128, 0, s>>>(rowptr, col, aval, n, x, ldx, b, ldb, r, nrhs);
+}
+
+void launch_maxnorms(const double* res, const double* x, int ldx, const double* b, int ldb,
+                     int n, int nrhs, double* norms, cudaStream_t s) {
+  if (n == 0) return;
+  dim3 grid(std::min(nblocks(n, 256), 152 * 4), nrhs);
+  k_maxnorms<<<grid, 256, 0, s>>>(res, x, ldx, b, ldb, n, nrhs, norms);
+}
+
+void launch_rownorm_inf(const int64_t* rowptr, const double* aval, int n, double* out,
+                        cudaStream_t s) {
+  if (n == 0) return;
+  k_rownorm<<<nblocks(n, 256), 256, 0, s>>>(rowptr, aval, n, out);
+}
+
+void launch_gather_clean(const double* val, const int64_t* srcptr, const int64_t* src,
+                         int64_t nclean, double* cval, cudaStream_t s) {
+  if (nclean == 0) return;
+  k_gather_clean<<<nblocks(nclean, 256), 256, 0, s>>>(val, srcptr, src, nclean, cval);
+}
+
+void launch_gather(const double* cval, const int64_t* idx, int64_t count, double* out,
+                   cudaStream_t s) {
+  if (count == 0) return;
+  k_gather<<<nblocks(count, 256), 256, 0, s>>>(cval, idx, count, out);
+}
+
+void launch_axpy_inplace(double* x, int ldx, const double* d, int n, int nrhs, cudaStream_t s) {
+  int64_t c = (int64_t)n * nrhs;
+  if (c == 0) return;
+  k_axpy<<<nblocks(c, 256), 256, 0, s>>>(x, ldx, d, n, nrhs);
+}
+
+template void launch_solve_fwd<float, float>(const float*, const FrontDesc*, int, const int*,
+                                             float*, int, int, float*, const int64_t*, bool,
+                                             cudaStream_t);
+template void launch_solve_bwd<float, float>(const float*, const FrontDesc*, int, const int*,
+                                             float*, int, int, float*, const int64_t*, bool,
+                                             cudaStream_t);
+template void launch_solve_fwd<double, double>(const double*, const FrontDesc*, int,
+                                               const int*, double*, int, int, double*,
+                                               const int64_t*, bool, cudaStream_t);
+template void launch_solve_bwd<double, double>(const double*, const FrontDesc*, int,
+                                               const int*, double*, int, int, double*,
+                                               const int64_t*, bool, cudaStream_t);
+template void launch_permute_in<float>(const double*, int, float*, const int*, int, int,
+                                       cudaStream_t);
+template void launch_permute_in<double>(const double*, int, double*, const int*, int, int,
+                                        cudaStream_t);
+template void launch_permute_out_add<float>(const float*, const int*, double*, int, int, int,
+                                            bool, cudaStream_t);
+template void launch_permute_out_add<double>(const double*, const int*, double*, int, int, int,
+                                             bool, cudaStream_t);
+
+}  // namespace sylver_gb300

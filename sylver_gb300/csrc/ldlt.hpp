@@ -1,0 +1,15 @@
+// Threshold-pivoted LDL^T on the GPU: planning, factorization driver,
+// solves with D and delayed pivots.
+#pragma once
+
+#include "numeric.hpp"
+
+namespace sylver_gb300 {
+
+void plan_ldlt(FKeep& fk);
+int factorize_ldlt(FKeep& fk, const double* val_dev, cudaStream_t s);
+void ldlt_solve_pivot_order(FKeep& fk, int job, float* xp, int nrhs, cudaStream_t s);
+void ldlt_solve_pivot_order(FKeep& fk, int job, double* xp, int nrhs, cudaStream_t s);
+int ldlt_export_diag(const FKeep& fk, double* d, int* piv_order);
+
+}  // namespace sylver_gb300

@@ -1,0 +1,531 @@
+// Host runtime: level schedule planning, device memory, CUDA-graph replay of
+// the factorization and the solve / iterative-refinement driver.
+//
+// The reference walks fronts in postorder and inserts StarPU tasks per tile
+// (src/NumericTreePosdef.hxx:133-353, src/NumericTree.hxx:186-406).  Here the
+// fronts are grouped by height in the assembly tree ("levels"); every launch
+// covers all fronts of a level, so independent subtrees share kernels and the
+// whole posdef factorization is one captured CUDA graph.
+#include "numeric.hpp"
+#include "ldlt.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+namespace sylver_gb300 {
+
+Runtime& Runtime::get() {
+  static Runtime rt;
+  return rt;
+}
+
+bool Runtime::init() {
+  if (ok) return true;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    err = std::string("no CUDA device: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    return false;
+  }
+  e = cudaSetDevice(0);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    err = cudaGetErrorString(e);
+    return false;
+  }
+  device = 0;
+  try {
+    prepare_factor_kernels<float>();
+    prepare_factor_kernels<double>();
+  } catch (const std::exception& ex) {
+    err = ex.what();
+    return false;
+  }
+  ok = true;
+  return true;
+}
+
+void AKeep::build_full_csr() {
+  const int nn = n;
+  std::vector<int64_t> cnt(nn + 1, 0);
+  for (int c = 0; c < nn; ++c)
+    for (int64_t k = clean.cptr[c]; k < clean.cptr[c + 1]; ++k) {
+      int r = clean.crow[k];
+      cnt[r + 1]++;
+      if (r != c) cnt[c + 1]++;
+    }
+  frow.assign(nn + 1, 0);
+  for (int i = 0; i < nn; ++i) frow[i + 1] = frow[i] + cnt[i + 1];
+  fcol.assign(frow[nn], 0);
+  fidx.assign(frow[nn], 0);
+  std::vector<int64_t> pos(frow.begin(), frow.end() - 1);
+  for (int c = 0; c < nn; ++c)
+    for (int64_t k = clean.cptr[c]; k < clean.cptr[c + 1]; ++k) {
+      int r = clean.crow[k];
+      fcol[pos[r]] = c;
+      fidx[pos[r]++] = k;
+      if (r != c) {
+        fcol[pos[c]] = r;
+        fidx[pos[c]++] = k;
+      }
+    }
+}
+
+FKeep::~FKeep() {
+  if (graph) cudaGraphExecDestroy(graph);
+}
+
+int64_t FKeep::nnz_orig() const {
+  int64_t mx = 0;
+  for (int64_t s : ak->clean.src) mx = std::max(mx, s + 1);
+  const auto& nl = ak->st.nlist;
+  for (size_t k = 0; k < nl.size(); k += 2) mx = std::max<int64_t>(mx, nl[k]);
+  return mx;
+}
+
+namespace {
+inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
+inline int64_t round_up64(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Static plan for Cholesky: every front size is known after analysis, so the
+// arena, every task list and the launch sequence are fixed here.
+
+void FKeep::plan_cholesky() {
+  const SymbolicTree& st = ak->st;
+  const int ns = st.nnodes;
+  const bool f32 = precision == 1;
+  const int TM = f32 ? Tiles<float>::TM : Tiles<double>::TM;
+  const int NB = f32 ? Tiles<float>::NB : Tiles<double>::NB;
+  const int RT = f32 ? Tiles<float>::RT : Tiles<double>::RT;
+  const int SMALL_M = f32 ? Tiles<float>::SMALL_M : Tiles<double>::SMALL_M;
+
+  order.resize(ns);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return st.level[a] < st.level[b]; });
+  levels.assign(st.nlevels, Level());
+  {
+    std::vector<int> cnt(st.nlevels + 1, 0);
+    for (int s = 0; s < ns; ++s) cnt[st.level[s] + 1]++;
+    for (int l = 0; l < st.nlevels; ++l) {
+      cnt[l + 1] += cnt[l];
+      levels[l].f0 = cnt[l];
+      levels[l].f1 = cnt[l + 1];
+    }
+  }
+  off.assign(ns, 0);
+  ld.assign(ns, 0);
+  int64_t cur = 0;
+  for (int k = 0; k < ns; ++k) {
+    int s = order[k];
+    int m = st.nrow[s];
+    ld[s] = round_up(std::max(m, 1), 4);
+    off[s] = cur;
+    cur += round_up64((int64_t)ld[s] * m, 64);
+  }
+  arena_elems = std::max<int64_t>(cur, 1);
+
+  // A -> arena map
+  std::vector<int64_t> asrc, adst;
+  asrc.reserve(st.nlist.size() / 2);
+  adst.reserve(st.nlist.size() / 2);
+  init_atomic = false;
+  for (int s = 0; s < ns; ++s) {
+    int nrow = st.nrow[s];
+    int64_t prev = -1;
+    for (int64_t k = st.nptr[s] - 1; k < st.nptr[s + 1] - 1; ++k) {
+      int64_t src = st.nlist[2 * k] - 1, dest = st.nlist[2 * k + 1] - 1;
+      int64_t c = dest / nrow, r = dest % nrow;
+      asrc.push_back(src);
+      adst.push_back(off[s] + c * ld[s] + r);
+      if (dest == prev) init_atomic = true;
+      prev = dest;
+    }
+  }
+  ninit = (int64_t)asrc.size();
+
+  // rlist (0-based) and solve descriptors in level order
+  std::vector<int> rl0(st.rlist.size());
+  for (size_t k = 0; k < st.rlist.size(); ++k) rl0[k] = st.rlist[k] - 1;
+  hfr.resize(ns);
+  hscr.resize(ns);
+  scratch_rows = 0;
+  for (auto& L : levels) {
+    int64_t acc = 0;
+    for (int k = L.f0; k < L.f1; ++k) {
+      int s = order[k];
+      hfr[k] = FrontDesc{off[s], ld[s], st.nrow[s], st.ncol[s], (int)(st.rptr[s] - 1), 0};
+      hscr[k] = acc;
+      acc += st.nrow[s];
+    }
+    scratch_rows = std::max(scratch_rows, acc);
+  }
+
+  // per-level launches
+  std::vector<ChildDesc> cds;
+  std::vector<EaItem> items;
+  std::vector<int> maps;
+  std::vector<SmallTask> smalls;
+  std::vector<PanelTask> panels;
+  std::vector<UpdTask> upds;
+  std::vector<int> pos(st.n, -1);
+  ops.clear();
+  ops.push_back({Op::MEMSET, 0, 0, 0});
+  ops.push_back({Op::INIT, 0, ninit, 0});
+  for (auto& L : levels) {
+    // extend-add of children into this level's fronts
+    int64_t i0 = (int64_t)items.size();
+    for (int k = L.f0; k < L.f1; ++k) {
+      int p = order[k];
+      for (int64_t q = st.rptr[p] - 1; q < st.rptr[p + 1] - 1; ++q)
+        pos[st.rlist[q] - 1] = (int)(q - (st.rptr[p] - 1));
+      for (int c : st.children[p]) {
+        int mc = st.nrow[c] - st.ncol[c];
+        if (mc <= 0) continue;
+        ChildDesc cd;
+        cd.cb_off = off[c] + (int64_t)st.ncol[c] * ld[c] + st.ncol[c];
+        cd.p_off = off[p];
+        cd.ld_c = ld[c];
+        cd.ld_p = ld[p];
+        cd.mc = mc;
+        cd.map_off = (int)maps.size();
+        for (int i = 0; i < mc; ++i) maps.push_back(pos[st.rlist[st.rptr[c] - 1 + st.ncol[c] + i] - 1]);
+        int ci = (int)cds.size();
+        cds.push_back(cd);
+        for (int j = 0; j < mc; ++j) items.push_back({ci, j});
+      }
+    }
+    if ((int64_t)items.size() > i0) ops.push_back({Op::EA, i0, (int64_t)items.size(), 0});
+    // small fronts: one CTA each
+    int64_t s0 = (int64_t)smalls.size();
+    int maxm = 0;
+    std::vector<int> large;
+    for (int k = L.f0; k < L.f1; ++k) {
+      int s = order[k];
+      if (st.nrow[s] <= SMALL_M) {
+        smalls.push_back({off[s], ld[s], st.nrow[s], st.ncol[s], 0});
+        maxm = std::max(maxm, st.nrow[s]);
+      } else {
+        large.push_back(s);
+      }
+    }
+    if ((int64_t)smalls.size() > s0) ops.push_back({Op::SMALL, s0, (int64_t)smalls.size(), maxm});
+    // large fronts: panel steps over the fully-summed columns, batched
+    int maxsteps = 0;
+    for (int s : large) maxsteps = std::max(maxsteps, (st.ncol[s] + NB - 1) / NB);
+    for (int step = 0; step < maxsteps; ++step) {
+      int64_t p0 = (int64_t)panels.size(), u0 = (int64_t)upds.size();
+      for (int s : large) {
+        int m = st.nrow[s], n = st.ncol[s];
+        int k0 = step * NB;
+        if (k0 >= n) continue;
+        int w = std::min(NB, n - k0);
+        for (int r0 = k0; r0 < m; r0 += RT)
+          panels.push_back({off[s], ld[s], k0, w, r0, std::min(r0 + RT, m), 0});
+        int o = k0 + w;
+        if (o < n) {
+          for (int cj = 0; o + cj * TM < n; ++cj)
+            for (int ri = cj; o + ri * TM < m; ++ri)
+              upds.push_back({off[s], ld[s], o + ri * TM, o + cj * TM, m, n, k0, k0 + w, 0});
+        }
+      }
+      if ((int64_t)panels.size() > p0) ops.push_back({Op::PANEL, p0, (int64_t)panels.size(), 0});
+      if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
+    }
+    // contribution blocks: one Schur-complement update with K = n
+    int64_t u0 = (int64_t)upds.size();
+    for (int s : large) {
+      int m = st.nrow[s], n = st.ncol[s];
+      if (m <= n) continue;
+      for (int cj = 0; n + cj * TM < m; ++cj)
+        for (int ri = cj; n + ri * TM < m; ++ri)
+          upds.push_back({off[s], ld[s], n + ri * TM, n + cj * TM, m, m, 0, n, 0});
+    }
+    if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
+  }
+
+  // algorithmic flops of update launches: lower-triangle entries x 2K
+  op_flops.assign(ops.size(), 0.0);
+  for (size_t q = 0; q < ops.size(); ++q) {
+    if (ops[q].kind != Op::UPD) continue;
+    double f = 0.0;
+    for (int64_t k = ops[q].a; k < ops[q].b; ++k) {
+      const UpdTask& t = upds[k];
+      int r1 = std::min(t.row0 + TM, t.rowEnd), c1 = std::min(t.col0 + TM, t.colEnd);
+      double pairs = 0.0;
+      for (int c = t.col0; c < c1; ++c) pairs += std::max(0, r1 - std::max(c, t.row0));
+      f += 2.0 * pairs * (t.k1 - t.k0);
+    }
+    op_flops[q] = f;
+  }
+  cudaStream_t s = Runtime::get().stream;
+  amap_src.upload(asrc, s);
+  amap_dst.upload(adst, s);
+  cdesc.upload(cds, s);
+  eaitems.upload(items, s);
+  eamaps.upload(maps, s);
+  small.upload(smalls, s);
+  panel.upload(panels, s);
+  upd.upload(upds, s);
+  dfr.upload(hfr, s);
+  dscr.upload(hscr, s);
+  rlist0.upload(rl0, s);
+  std::vector<int> p0(st.n);
+  for (int i = 0; i < st.n; ++i) p0[i] = st.perm[i];
+  perm0.upload(p0, s);
+  maxfront = st.maxfront;
+  num_factor = st.num_factor;
+  num_flops = st.num_flops;
+}
+
+void FKeep::upload_static(cudaStream_t s) {
+  AKeep& a = *ak;
+  frow.upload(a.frow, s);
+  fcol.upload(a.fcol, s);
+  fidx.upload(a.fidx, s);
+  srcptr.upload(a.clean.srcptr, s);
+  src.upload(a.clean.src, s);
+  cval.ensure(std::max<size_t>(1, a.clean.crow.size()) * sizeof(double));
+  faval.ensure(std::max<size_t>(1, a.fcol.size()) * sizeof(double));
+  status.ensure(sizeof(unsigned));
+  anorm.ensure(sizeof(double));
+  arena.ensure((size_t)arena_elems * (precision == 1 ? sizeof(float) : sizeof(double)));
+}
+
+template <typename T>
+void FKeep::run_ops(cudaStream_t s) {
+  T* A = arena.as<T>();
+  unsigned* stp = status.as<unsigned>();
+  for (const Op& op : ops) {
+    int64_t cnt = op.b - op.a;
+    switch (op.kind) {
+      case Op::MEMSET:
+        SG_CUDA(cudaMemsetAsync(A, 0, (size_t)arena_elems * sizeof(T), s));
+        break;
+      case Op::INIT:
+        launch_init_a<T>(A, val.as<double>(), amap_src.as<int64_t>(), amap_dst.as<int64_t>(),
+                         ninit, init_atomic, s);
+        break;
+      case Op::EA:
+        launch_extend_add<T>(A, cdesc.as<ChildDesc>(), eaitems.as<EaItem>() + op.a,
+                             eamaps.as<int>(), (int)cnt, s);
+        break;
+      case Op::SMALL:
+        launch_small_chol<T>(A, small.as<SmallTask>() + op.a, (int)cnt, op.aux, stp, s);
+        break;
+      case Op::PANEL:
+        launch_panel_chol<T>(A, panel.as<PanelTask>() + op.a, (int)cnt, stp, s);
+        break;
+      case Op::UPD:
+        launch_update<T>(A, upd.as<UpdTask>() + op.a, (int)cnt, s);
+        break;
+    }
+  }
+}
+
+int FKeep::factorize(const double* val_dev, cudaStream_t s) {
+  AKeep& a = *ak;
+  const int64_t nclean = (int64_t)a.clean.crow.size();
+  // values: clean (duplicates summed) then full CSR for residuals
+  launch_gather_clean(val_dev, srcptr.as<int64_t>(), src.as<int64_t>(), nclean,
+                      cval.as<double>(), s);
+  launch_gather(cval.as<double>(), fidx.as<int64_t>(), (int64_t)a.fcol.size(),
+                faval.as<double>(), s);
+  SG_CUDA(cudaMemsetAsync(anorm.p, 0, sizeof(double), s));
+  launch_rownorm_inf(frow.as<int64_t>(), faval.as<double>(), a.n, anorm.as<double>(), s);
+  SG_CUDA(cudaMemsetAsync(status.p, 0, sizeof(unsigned), s));
+  // the factor schedule reads val through the fkeep-owned buffer so that the
+  // captured graph stays valid across calls
+  if (val_dev != val.as<double>()) {
+    int64_t nz = nnz_orig();
+    val.ensure(std::max<int64_t>(nz, 1) * sizeof(double));
+    if (nz) SG_CUDA(cudaMemcpyAsync(val.p, val_dev, nz * sizeof(double),
+                                    cudaMemcpyDeviceToDevice, s));
+  }
+  cudaEvent_t e0, e1;
+  SG_CUDA(cudaEventCreate(&e0));
+  SG_CUDA(cudaEventCreate(&e1));
+  SG_CUDA(cudaEventRecord(e0, s));
+  if (use_graph) {
+    if (!graph) {
+      cudaGraph_t g;
+      SG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      if (precision == 1) run_ops<float>(s);
+      else run_ops<double>(s);
+      SG_CUDA(cudaStreamEndCapture(s, &g));
+      SG_CUDA(cudaGraphInstantiate(&graph, g, 0));
+      cudaGraphDestroy(g);
+    }
+    SG_CUDA(cudaGraphLaunch(graph, s));
+  } else {
+    if (precision == 1) run_ops<float>(s);
+    else run_ops<double>(s);
+  }
+  SG_CUDA(cudaEventRecord(e1, s));
+  launches = (long)ops.size() - 1;  // the memset is not a kernel
+  unsigned st = 0;
+  SG_CUDA(cudaMemcpyAsync(&st, status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  SG_CUDA(cudaMemcpyAsync(&anorm_h, anorm.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  SG_CUDA(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  factor_ms = ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  flag = 0;
+  if (posdef) {
+    rank = (st & ST_NOT_POSDEF) ? 0 : ak->n;
+    if (st & ST_NOT_POSDEF) flag = -6;
+  }
+  return flag;
+}
+
+int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, cudaStream_t s) {
+  for (int k = 0; k < 8; ++k) {
+    ms[k] = 0.0;
+    nl[k] = 0;
+    flops[k] = 0.0;
+  }
+  if (!posdef) return -98;
+  if (val_dev && val_dev != val.as<double>()) {
+    int64_t nz = nnz_orig();
+    SG_CUDA(cudaMemcpyAsync(val.p, val_dev, nz * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  }
+  SG_CUDA(cudaMemsetAsync(status.p, 0, sizeof(unsigned), s));
+  std::vector<cudaEvent_t> ev(ops.size() + 1);
+  for (auto& e : ev) SG_CUDA(cudaEventCreate(&e));
+  SG_CUDA(cudaEventRecord(ev[0], s));
+  std::vector<Op> all = ops;
+  for (size_t q = 0; q < all.size(); ++q) {
+    ops = {all[q]};
+    if (precision == 1) run_ops<float>(s);
+    else run_ops<double>(s);
+    SG_CUDA(cudaEventRecord(ev[q + 1], s));
+  }
+  ops = all;
+  SG_CUDA(cudaStreamSynchronize(s));
+  for (size_t q = 0; q < all.size(); ++q) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
+    int k = (int)all[q].kind;
+    ms[k] += t;
+    nl[k] += 1;
+    flops[k] += op_flops.empty() ? 0.0 : op_flops[q];
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+
+template <typename T>
+void FKeep::solve_pivot_order(int job, void* xpv, int nrhs, cudaStream_t s) {
+  using ACC = T;
+  ACC* xpd = static_cast<ACC*>(xpv);
+  const int n = ak->n;
+  const T* A = arena.as<T>();
+  scratch.ensure(std::max<int64_t>(scratch_rows * nrhs, 1) * sizeof(ACC));
+  bool fwd = job == 0 || job == 1;
+  bool bwd = job == 0 || job == 3 || job == 4;
+  const FrontDesc* fr = dfr.as<FrontDesc>();
+  const int64_t* sc = dscr.as<int64_t>();
+  for (int r0 = 0; r0 < nrhs; r0 += 32) {
+    int nr = std::min(32, nrhs - r0);
+    ACC* xr = xpd + (int64_t)r0 * n;
+    if (fwd)
+      for (auto& L : levels)
+        launch_solve_fwd<T, ACC>(A, fr + L.f0, L.f1 - L.f0, rlist0.as<int>(), xr, n, nr,
+                                 scratch.as<ACC>(), sc + L.f0, !posdef, s);
+    if (bwd)
+      for (int l = (int)levels.size() - 1; l >= 0; --l) {
+        auto& L = levels[l];
+        launch_solve_bwd<T, ACC>(A, fr + L.f0, L.f1 - L.f0, rlist0.as<int>(), xr, n, nr,
+                                 scratch.as<ACC>(), sc + L.f0, !posdef, s);
+      }
+  }
+}
+
+int FKeep::solve_raw(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
+  if (precision != 0) return -98;
+  const int n = ak->n;
+  xp.ensure((size_t)n * nrhs * sizeof(double));
+  for (int r = 0; r < nrhs; ++r)
+    SG_CUDA(cudaMemcpyAsync(xp.as<double>() + (size_t)r * n, x + (size_t)r * ldx,
+                            n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  if (ldlt) ldlt_solve_pivot_order(*this, job, xp.as<double>(), nrhs, s);
+  else solve_pivot_order<double>(job, xp.p, nrhs, s);
+  for (int r = 0; r < nrhs; ++r)
+    SG_CUDA(cudaMemcpyAsync(x + (size_t)r * ldx, xp.as<double>() + (size_t)r * n,
+                            n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  return 0;
+}
+
+int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
+  const int n = ak->n;
+  if (n == 0) return 0;
+  const bool f32 = precision == 1;
+  const size_t acc_sz = f32 ? sizeof(float) : sizeof(double);
+  xp.ensure((size_t)n * nrhs * acc_sz);
+  const int* perm = perm0.as<int>();
+  last_ir_iters = 0;
+  last_bwd_err = -1.0;
+  auto one_solve = [&](const double* rhs, int ldr, double* out, int ldo, bool add, int jb) {
+    if (f32) {
+      launch_permute_in<float>(rhs, ldr, xp.as<float>(), perm, n, nrhs, s);
+      if (ldlt) ldlt_solve_pivot_order(*this, jb, xp.as<float>(), nrhs, s);
+      else solve_pivot_order<float>(jb, xp.p, nrhs, s);
+      launch_permute_out_add<float>(xp.as<float>(), perm, out, ldo, n, nrhs, add, s);
+    } else {
+      launch_permute_in<double>(rhs, ldr, xp.as<double>(), perm, n, nrhs, s);
+      if (ldlt) ldlt_solve_pivot_order(*this, jb, xp.as<double>(), nrhs, s);
+      else solve_pivot_order<double>(jb, xp.p, nrhs, s);
+      launch_permute_out_add<double>(xp.as<double>(), perm, out, ldo, n, nrhs, add, s);
+    }
+  };
+  const bool refine = job == 0 && (f32 || ir_max_iter > 0);
+  if (!refine) {
+    one_solve(x, ldx, x, ldx, false, job);
+    SG_CUDA(cudaStreamSynchronize(s));
+    return 0;
+  }
+  // iterative refinement: x0 = solve(b); repeat r = b - A x (FP64), check
+  // the scaled backward error, x += solve(r)
+  bcopy.ensure((size_t)n * nrhs * sizeof(double));
+  resid.ensure((size_t)n * nrhs * sizeof(double));
+  norms.ensure((size_t)3 * nrhs * sizeof(double));
+  for (int r = 0; r < nrhs; ++r)
+    SG_CUDA(cudaMemcpyAsync(bcopy.as<double>() + (size_t)r * n, x + (size_t)r * ldx,
+                            n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  one_solve(bcopy.as<double>(), n, x, ldx, false, 0);
+  const int maxit = std::max(ir_max_iter, 1);
+  std::vector<double> hn(3 * nrhs);
+  for (int it = 0;; ++it) {
+    launch_residual(frow.as<int64_t>(), fcol.as<int>(), faval.as<double>(), n, x, ldx,
+                    bcopy.as<double>(), n, resid.as<double>(), nrhs, s);
+    SG_CUDA(cudaMemsetAsync(norms.p, 0, 3 * nrhs * sizeof(double), s));
+    launch_maxnorms(resid.as<double>(), x, ldx, bcopy.as<double>(), n, n, nrhs,
+                    norms.as<double>(), s);
+    SG_CUDA(cudaMemcpyAsync(hn.data(), norms.p, 3 * nrhs * sizeof(double),
+                            cudaMemcpyDeviceToHost, s));
+    SG_CUDA(cudaStreamSynchronize(s));
+    double worst = 0.0;
+    for (int r = 0; r < nrhs; ++r) {
+      double den = anorm_h * hn[3 * r + 1] + hn[3 * r + 2];
+      double be = den > 0 ? hn[3 * r] / den : 0.0;
+      if (!(be == be)) be = INFINITY;
+      worst = std::max(worst, be);
+    }
+    last_bwd_err = worst;
+    last_ir_iters = it;
+    if (worst <= ir_tol || it >= maxit) break;
+    one_solve(resid.as<double>(), n, x, ldx, true, 0);
+  }
+  return 0;
+}
+
+}  // namespace sylver_gb300

@@ -1,0 +1,152 @@
+// Host runtime of the GPU numeric phase: analysis handle (akeep), factor
+// handle (fkeep), device memory, the level schedule and the solve driver.
+//
+// Replaces the reference's NumericTree / NumericTreePosdef objects
+// (src/NumericTree.hxx:54-181, src/NumericTreePosdef.hxx:42-128) and the
+// Fortran orchestration of factorize/solve (src/spldlt_factorize_mod.F90).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "analyse.hpp"
+#include "device.hpp"
+
+namespace sylver_gb300 {
+
+// Owned device allocation.
+struct DevMem {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevMem() = default;
+  DevMem(const DevMem&) = delete;
+  DevMem& operator=(const DevMem&) = delete;
+  ~DevMem() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void ensure(size_t nbytes) {
+    if (nbytes <= bytes && p) return;
+    release();
+    if (nbytes == 0) return;
+    SG_CUDA(cudaMalloc(&p, nbytes));
+    bytes = nbytes;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+  template <typename T> void upload(const std::vector<T>& v, cudaStream_t s) {
+    ensure(std::max<size_t>(1, v.size()) * sizeof(T));
+    if (!v.empty()) SG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T),
+                                            cudaMemcpyHostToDevice, s));
+  }
+};
+
+// Process-wide device context: device 0, one non-blocking stream.
+struct Runtime {
+  int device = -1;
+  cudaStream_t stream = nullptr;
+  bool ok = false;
+  std::string err;
+  static Runtime& get();
+  bool init();  // returns false (and sets err) when no CUDA device is usable
+};
+
+struct AKeep {
+  int n = 0;
+  bool check = false;
+  int flag = 0;
+  int matrix_outrange = 0, matrix_dup = 0, matrix_missing_diag = 0;
+  AnalyseResult clean;
+  SymbolicTree st;
+  // full symmetric CSR (user order) used by residual computations:
+  // value of entry e = clean value fidx[e]
+  std::vector<int64_t> frow;
+  std::vector<int> fcol;
+  std::vector<int64_t> fidx;
+  void build_full_csr();
+};
+
+// One kernel launch of the factor schedule.
+struct Op {
+  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD } kind;
+  int64_t a = 0, b = 0;  // task range [a, b)
+  int aux = 0;           // SMALL: max front rows in the launch
+};
+
+struct Level {
+  int f0 = 0, f1 = 0;  // fronts [f0, f1) of the level-ordered front table
+};
+
+struct FKeep {
+  AKeep* ak = nullptr;
+  bool posdef = true;
+  int precision = 0;  // 0 FP64, 1 FP32
+  double ir_tol = 1e-14;
+  int ir_max_iter = 0;
+  bool use_graph = true;
+  // pivoting options (src/sylver_datatypes_mod.F90:57-72)
+  double u = 0.01;
+  double small_piv = 1e-20;
+  bool action = true;
+  std::vector<double> scale;  // user scaling S (empty: none)
+
+  // host plan
+  std::vector<int> order;            // level-ordered front indices
+  std::vector<Level> levels;
+  std::vector<int64_t> off;          // per front (original index)
+  std::vector<int> ld;
+  int64_t arena_elems = 0;
+  std::vector<FrontDesc> hfr;        // level-ordered solve descriptors
+  std::vector<int64_t> hscr;         // level-ordered scratch row offsets
+  int64_t scratch_rows = 0;
+  std::vector<Op> ops;
+  std::vector<double> op_flops;      // algorithmic flops per op (update launches)
+  bool init_atomic = false;
+  int64_t ninit = 0;
+
+  // device data
+  DevMem arena, val, cval, faval, frow, fcol, fidx, srcptr, src, status, anorm;
+  DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, small, panel, upd;
+  DevMem dfr, dscr, rlist0, perm0;
+  DevMem xp, scratch, bcopy, resid, norms;
+  cudaGraphExec_t graph = nullptr;
+  double anorm_h = 0.0;
+
+  // statistics
+  long launches = 0;
+  double factor_ms = 0.0;
+  int last_ir_iters = 0;
+  double last_bwd_err = 0.0;
+  int flag = 0;
+  int num_neg = 0, num_two = 0, num_delay = 0, num_zero = 0, rank = 0;
+  int maxfront = 0;
+  int64_t num_factor = 0, num_flops = 0;
+  int not_first_pass = 0, not_second_pass = 0;
+
+  // LDL^T state (ldlt.cpp)
+  std::shared_ptr<struct LdltState> ldlt;
+
+  ~FKeep();
+  void plan_cholesky();
+  void upload_static(cudaStream_t s);
+  // Factorize from device values (val_dev: original val layout, nnz entries).
+  int factorize(const double* val_dev, cudaStream_t s);
+  // Solve in place on device; x is ldx x nrhs in user order.
+  int solve(int job, int nrhs, double* x_dev, int ldx, cudaStream_t s);
+  // Solve with x already in pivot order (the tree-level seam), FP64 only.
+  int solve_raw(int job, int nrhs, double* x_dev, int ldx, cudaStream_t s);
+  // Per-kind timing of the factor schedule (see sylver_gb300_profile_factor).
+  int profile(const double* val_dev, double* ms, long* launches, double* flops, cudaStream_t s);
+
+ public:
+  template <typename T> void run_ops(cudaStream_t s);
+  template <typename T> void solve_pivot_order(int job, void* xp, int nrhs, cudaStream_t s);
+  int64_t nnz_orig() const;
+};
+
+}  // namespace sylver_gb300

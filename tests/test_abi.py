@@ -1,0 +1,61 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+
+from conftest import ROOT
+
+
+def header_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        txt = open(h).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        for m in re.finditer(r"^\s*(?:void\*?|int|long|double)\s*\**\s*(\w+)\s*\(", txt, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_exports_match_header(sylver):
+    lib = sylver.load()
+    names = header_functions()
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(sylver.EXPORTS) <= names
+
+
+def test_struct_layouts(sylver):
+    # sylver_inform_t / sylver_options_t sizes as compiled by the C compiler
+    assert ctypes.sizeof(sylver.Inform) == 4 * 8 + 8 * 2 + 4 * 6 + 80
+    o = sylver.default_options()
+    assert o.nemin == 32 and o.nb == 256 and abs(o.u - 0.01) < 1e-15 and o.action
+    assert o.ordering == 1 and abs(o.small - 1e-20) < 1e-35
+
+
+def test_no_gpu_means_error_not_fallback(sylver):
+    import torch
+    if torch.cuda.is_available():
+        return
+    from sylver_gb300 import workloads as w
+    p = w.laplace2d(6)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    f = sylver.Factor(an, True, p.a.val)
+    assert f.flag == -51
+
+
+def test_call_sequence_errors(sylver):
+    lib = sylver.load()
+    inf = sylver.Inform()
+    o = sylver.default_options()
+    x = np.zeros(4)
+    lib.spldlt_solve(0, 1, x.ctypes.data_as(ctypes.c_void_p), 4, None, None, ctypes.byref(o),
+                     ctypes.byref(inf))
+    assert inf.flag == -1
+    fk = ctypes.c_void_p()
+    lib.spldlt_factorize(True, None, None, x.ctypes.data_as(ctypes.c_void_p), None, None,
+                         ctypes.byref(fk), ctypes.byref(o), ctypes.byref(inf))
+    assert inf.flag == -1

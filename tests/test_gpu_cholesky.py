@@ -1,0 +1,145 @@
+"""GPU Cholesky path through the C-ABI against the CPU oracle.
+
+Bars (the benchmark spec): FP64 path -- backward error <= 1e-14 and the solution
+agrees with the oracle's to 1e-10 relative; FP32 factors + FP64 iterative
+refinement -- the same backward error after refinement."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+from sylver_gb300 import workloads as w
+
+pytestmark = pytest.mark.gpu
+
+SPD = [n for n in golden_names() if load_golden(n)["posdef"] and load_golden(n)["flag"] == 0]
+
+
+def run(sylver, g, precision, ir=0):
+    an = sylver.Analysis(g["n"], g["ptr"], g["row"], order=g["order"])
+    f = sylver.Factor(an, True, g["val"], precision=precision, ir_max_iter=ir)
+    return an, f
+
+
+@pytest.mark.parametrize("name", SPD)
+@pytest.mark.parametrize("precision", [0, 1])
+def test_spd_golden(sylver, orc, gpu, name, precision):
+    g = load_golden(name)
+    an, f = run(sylver, g, precision, ir=10)
+    assert f.flag == 0, f.inform.as_dict()
+    full = w.SymMatrix(g["n"], g["ptr"], g["row"], g["val"]).to_scipy_full()
+    x = f.solve(g["rhs"])
+    be = w.backward_error(full, x, g["rhs"]).max()
+    assert be <= 1e-14, (be, f.solve_stats())
+    o = orc.OracleFactor(True, an.symbolic(), g["val"])
+    xo = o.solve(g["rhs"])
+    xo = xo + o.solve(g["rhs"] - full @ xo)
+    assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
+    if "x_true" in g:
+        assert np.abs(x - g["x_true"]).max() <= 1e-10
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_spd_plain_solve_matches_oracle(sylver, orc, gpu, precision):
+    """Without refinement the GPU factor solves like the FP64 oracle factor
+    (FP64) or to FP32 accuracy (FP32)."""
+    g = load_golden("lognormal27_7")
+    an, f = run(sylver, g, precision, ir=0)
+    o = orc.OracleFactor(True, an.symbolic(), g["val"])
+    xo = o.solve(g["rhs"])
+    if precision == 0:
+        x = f.solve(g["rhs"])
+        assert np.abs(x - xo).max() <= 1e-11 * np.abs(xo).max()
+    # partial jobs: fwd then bwd equals the full solve of the same factor
+    y = f.solve(g["rhs"], job=1)
+    y = f.solve(y, job=3)
+    yo = o.solve(o.solve(g["rhs"], job=1), job=3)
+    tol = 1e-11 if precision == 0 else 2e-4
+    assert np.abs(y - yo).max() <= tol * np.abs(yo).max()
+
+
+def test_not_posdef_flag(sylver, gpu):
+    g = load_golden("not_posdef_5")
+    an, f = run(sylver, g, 0)
+    assert f.flag == -6
+    with pytest.raises(RuntimeError):
+        f.solve(g["rhs"])  # call sequence error after a failed factorization
+
+
+def test_solve_arg_errors(sylver, gpu):
+    g = load_golden("laplace2d_12")
+    an, f = run(sylver, g, 0)
+    import ctypes
+    lib = sylver.load()
+    x = np.zeros((g["n"], 1), order="F")
+    inf = sylver.Inform()
+    o = sylver.default_options()
+    P = ctypes.c_void_p
+    lib.spldlt_solve(0, 1, x.ctypes.data_as(P), g["n"] - 1, an.akeep, f.fkeep, ctypes.byref(o),
+                     ctypes.byref(inf))
+    assert inf.flag == -10
+    lib.spldlt_solve(0, 0, x.ctypes.data_as(P), g["n"], an.akeep, f.fkeep, ctypes.byref(o),
+                     ctypes.byref(inf))
+    assert inf.flag == -10
+    lib.spldlt_solve(2, 1, x.ctypes.data_as(P), g["n"], an.akeep, f.fkeep, ctypes.byref(o),
+                     ctypes.byref(inf))
+    assert inf.flag == -11
+    lib.spldlt_solve(7, 1, x.ctypes.data_as(P), g["n"], an.akeep, f.fkeep, ctypes.byref(o),
+                     ctypes.byref(inf))
+    assert inf.flag == -11
+
+
+@pytest.mark.parametrize("k,precision", [(20, 0), (24, 1), (40, 1)])
+def test_spd_medium_grids(sylver, orc, gpu, k, precision):
+    """Fronts large enough for the panel / tile-update kernels."""
+    p = w.lognormal27(k, nrhs=3)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    assert an.inform.maxfront > 256
+    f = sylver.Factor(an, True, p.a.val, precision=precision, ir_max_iter=10)
+    assert f.flag == 0
+    full = p.a.to_scipy_full()
+    x = f.solve(p.rhs)
+    be = w.backward_error(full, x, p.rhs).max()
+    assert be <= 1e-14, (be, f.solve_stats())
+    if k <= 24:
+        o = orc.OracleFactor(True, an.symbolic(), p.a.val)
+        xo = o.solve(p.rhs)
+        xo = xo + o.solve(p.rhs - full @ xo)
+        assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
+
+
+def test_many_rhs_and_ldx(sylver, gpu):
+    """More right-hand sides than one solve launch takes (32), ldx > n."""
+    p = w.laplace2d(30, nrhs=1)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    f = sylver.Factor(an, True, p.a.val)
+    rng = np.random.default_rng(9)
+    n = p.a.n
+    b = np.asfortranarray(rng.standard_normal((n + 5, 37)))
+    x = f.solve(b[:, :])  # ldx = n + 5
+    full = p.a.to_scipy_full()
+    be = w.backward_error(full, x[:n], b[:n]).max()
+    assert be <= 1e-14
+
+
+def test_refactorize_reuses_fkeep(sylver, gpu):
+    p = w.laplace2d(25, nrhs=1)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    f = sylver.Factor(an, True, p.a.val)
+    x1 = f.solve(p.rhs)
+    assert f.refactor(2.0 * p.a.val) == 0
+    x2 = f.solve(p.rhs)
+    np.testing.assert_allclose(x2, 0.5 * x1, rtol=1e-12, atol=1e-14)
+
+
+def test_trivial_sizes(sylver, gpu):
+    # n = 1
+    an = sylver.Analysis(1, np.array([1, 2]), np.array([1]))
+    f = sylver.Factor(an, True, np.array([4.0]))
+    assert f.flag == 0
+    np.testing.assert_allclose(f.solve(np.array([[2.0]])), [[0.5]])
+    # diagonal matrix
+    n = 50
+    an = sylver.Analysis(n, np.arange(1, n + 2), np.arange(1, n + 1))
+    d = np.arange(1.0, n + 1)
+    f = sylver.Factor(an, True, d)
+    np.testing.assert_allclose(f.solve(np.ones((n, 1)))[:, 0], 1.0 / d, rtol=1e-15)
