@@ -248,7 +248,8 @@ def run_ours(args, rank, ws):
     ms = np.zeros(8); cnt = np.zeros(8, dtype=np.int64); fl = np.zeros(8)
     lib.sylver_gb300_profile_factor(fkeep, None, ms.ctypes.data_as(P), cnt.ctypes.data_as(P),
                                     fl.ctypes.data_as(P))
-    kinds = ("memset", "init_a", "extend_add", "small_fronts", "panel", "update", "ldlt", "other")
+    kinds = ("memset", "init_a", "extend_add", "small_fronts", "panel_trsm", "update",
+             "diag_chol", "other")
     prof = {k: {"ms": round(float(ms[i]), 3), "launches": int(cnt[i])} for i, k in enumerate(kinds)
             if cnt[i]}
     hbm, bf16, src = peaks()

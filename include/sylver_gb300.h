@@ -237,8 +237,8 @@ void* sylver_gb300_stream(void);
 
 /* Re-run the factorization held by fkeep with one CUDA event pair around
  * every launch (no graph) and accumulate per kernel kind:
- * 0 memset, 1 init-A, 2 extend-add, 3 small fronts, 4 panel, 5 update, 6 LDL^T
- * diagonal/apply kernels.  ms[k] = total milliseconds, launches[k] = count,
+ * 0 memset, 1 init-A, 2 extend-add, 3 small fronts, 4 panel triangular solve,
+ * 5 tile update, 6 diagonal-block Cholesky (Cholesky factorizations only).  ms[k] = total milliseconds, launches[k] = count,
  * flops[k] = algorithmic flops (update kernels: lower-triangle tile work).
  * Arrays hold 8 entries.  Returns 0 or a reference flag. */
 int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, long* launches,

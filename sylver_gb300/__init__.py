@@ -242,7 +242,8 @@ class Factor:
                                            ctypes.byref(ms))
         return dict(kernel_launches=nl.value, nlevels=lv.value, factor_ms=ms.value)
 
-    KINDS = ("memset", "init_a", "extend_add", "small_fronts", "panel", "update", "ldlt", "other")
+    KINDS = ("memset", "init_a", "extend_add", "small_fronts", "panel_trsm", "update",
+             "diag_chol", "other")
 
     def profile(self, val_dev_ptr=None):
         """Per-kernel-kind timing of one extra factorization (no graph)."""

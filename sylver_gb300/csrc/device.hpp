@@ -48,22 +48,27 @@ struct SmallTask {
   int ld, m, n, pad;
 };
 
-// Panel step: Cholesky of the w x w diagonal block at (k0,k0) and the
-// triangular solve of rows [r0, r1) of columns [k0, k0+w).
+// Panel step: Cholesky of the w x w diagonal block at (k0,k0) (one task per
+// front) or the triangular solve of rows [r0, r1) of columns [k0, k0+w).
 struct PanelTask {
   int64_t off;
   int ld, k0, w, r0, r1, pad;
 };
 
-// Tile update C -= A_rows * A_cols^T inside one front:
-// rows [row0, min(row0+TM,rowEnd)), cols [col0, min(col0+TN,colEnd)),
-// inner index k in [k0, k1).
+// Tile update C(i,j) -= sum_k A(i,k) B(j,k) with
+//   C(i,j) = arena[c_off + j*ldc + i], B(j,k) = arena[b_off + k*ldb + j],
+//   A(i,k) = abuf[a_off + k*lda + i]  (abuf is the arena itself for Cholesky,
+//   an L*D panel for LDL^T),
+// rows [row0, min(row0+TM,rowEnd)), cols [col0, min(col0+TN,colEnd)), only
+// i >= j written, inner index k in [k0, k1).
 struct UpdTask {
-  int64_t off;
-  int ld, row0, col0, rowEnd, colEnd, k0, k1, pad;
+  int64_t c_off, a_off, b_off;
+  int ldc, lda, ldb, row0, col0, rowEnd, colEnd, k0, k1, pad;
 };
 
-// Extend-add of one child contribution column into its parent.
+// Extend-add of one child contribution column into its parent; the entry
+// (i, j), i >= j, of the child block lands at (max, min) of the mapped rows
+// (maps are monotone for Cholesky, not once delayed columns move up).
 struct ChildDesc {
   int64_t cb_off;   // child CB (0,0) in the arena
   int64_t p_off;    // parent front (0,0)
@@ -89,10 +94,12 @@ template <typename T>
 void launch_small_chol(T* arena, const SmallTask* t, int ntask, int maxm, unsigned* status,
                        cudaStream_t s);
 template <typename T>
-void launch_panel_chol(T* arena, const PanelTask* t, int ntask, unsigned* status,
-                       cudaStream_t s);
+void launch_diag_chol(T* arena, const PanelTask* t, int ntask, unsigned* status,
+                      cudaStream_t s);
 template <typename T>
-void launch_update(T* arena, const UpdTask* t, int ntask, cudaStream_t s);
+void launch_panel_trsm(T* arena, const PanelTask* t, int ntask, cudaStream_t s);
+template <typename T>
+void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStream_t s);
 
 template <typename T> struct Tiles;
 template <> struct Tiles<double> {
@@ -114,6 +121,22 @@ template <typename T, typename ACC>
 void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
                       ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
                       bool unit_diag, cudaStream_t s);
+
+// Large-front blocked sweeps (block width 64).  Task f indexes the level's
+// FrontDesc array; c0/bw give the diagonal block, r0 the first row of a tile.
+struct LTask {
+  int f, c0, bw, r0;
+};
+enum LsKind {
+  LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD,
+  LS_FWD_DIAG, LS_FWD_UPD, LS_BWD_RED, LS_BWD_DIAG
+};
+constexpr int LSOLVE_BW = 64;
+// tt: per front of the level, 64 x 32 accumulators (zero on entry, left zero).
+template <typename T, typename ACC>
+void launch_lsolve(int kind, const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+                   const int* rlist, ACC* x, int n, int nrhs, ACC* scratch,
+                   const int64_t* scr_off, ACC* tt, bool unit, cudaStream_t s);
 
 template <typename ACC>
 void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, int n, int nrhs,

@@ -46,10 +46,14 @@ __global__ void k_extend_add(T* __restrict__ arena, const ChildDesc* __restrict_
   ChildDesc c = cd[it.child];
   const int* map = maps + c.map_off;
   int j = it.col;
-  int pj = map[j];
+  const int pj = map[j];
   const T* src = arena + c.cb_off + (int64_t)j * c.ld_c;
-  T* dst = arena + c.p_off + (int64_t)pj * c.ld_p;
-  for (int i = j + lane; i < c.mc; i += 32) atomic_add(dst + map[i], src[i]);
+  T* dst = arena + c.p_off;
+  for (int i = j + lane; i < c.mc; i += 32) {
+    const int pi = map[i];
+    const int r = max(pi, pj), cc = min(pi, pj);
+    atomic_add(dst + (int64_t)cc * c.ld_p + r, src[i]);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -99,18 +103,60 @@ __global__ void __launch_bounds__(256) k_small_chol(T* __restrict__ arena,
 }
 
 // ---------------------------------------------------------------------------
-// Panel step: each CTA recomputes the NB x NB diagonal Cholesky (cheap, and
-// it avoids a launch + grid-wide dependency), then solves its row tile
-// L_r = A_r L_kk^-T.  The CTA whose tile starts at k0 writes L_kk back.
-template <typename T, int NB, int RT>
-__global__ void __launch_bounds__(RT) k_panel_chol(T* __restrict__ arena,
+// Panel step, part 1: Cholesky of the w x w diagonal block at (k0, k0), one
+// CTA per front, in place.
+template <typename T, int NB>
+__global__ void __launch_bounds__(128) k_diag_chol(T* __restrict__ arena,
                                                    const PanelTask* __restrict__ tasks,
                                                    unsigned* status) {
+  __shared__ T D[NB][NB + 1];  // D[j][i] = A(i, j)
+  __shared__ T dinv;
+  const PanelTask t = tasks[blockIdx.x];
+  T* a = arena + t.off;
+  const int ld = t.ld, k0 = t.k0, w = t.w, tid = threadIdx.x;
+  for (int idx = tid; idx < w * w; idx += blockDim.x) {
+    int i = idx % w, j = idx / w;
+    if (i >= j) D[j][i] = a[(int64_t)(k0 + j) * ld + k0 + i];
+  }
+  __syncthreads();
+  for (int k = 0; k < w; ++k) {
+    if (tid == 0) {
+      T d = D[k][k];
+      if (!(d > T(0))) {
+        atomicOr(status, ST_NOT_POSDEF);
+        d = T(1);
+      }
+      d = sqrt(d);
+      D[k][k] = d;
+      dinv = T(1) / d;
+    }
+    __syncthreads();
+    const T inv = dinv;
+    for (int i = k + 1 + tid; i < w; i += blockDim.x) D[k][i] *= inv;
+    __syncthreads();
+    const int ww = w - k - 1;
+    for (int idx = tid; idx < ww * ww; idx += blockDim.x) {
+      int i = k + 1 + idx % ww, j = k + 1 + idx / ww;
+      if (i >= j) D[j][i] -= D[k][i] * D[k][j];
+    }
+    __syncthreads();
+  }
+  for (int idx = tid; idx < w * w; idx += blockDim.x) {
+    int i = idx % w, j = idx / w;
+    if (i >= j) a[(int64_t)(k0 + j) * ld + k0 + i] = D[j][i];
+  }
+}
+
+// Panel step, part 2: rows [r0, r1) below the diagonal block solve
+// L_r = A_r L_kk^-T against the factor written by k_diag_chol.
+template <typename T, int NB, int RT>
+__global__ void __launch_bounds__(RT) k_panel_trsm(T* __restrict__ arena,
+                                                   const PanelTask* __restrict__ tasks) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* D = reinterpret_cast<T*>(smem_raw);  // NB x (NB+1), column-major
   T* R = D + NB * (NB + 1);               // NB x (RT+1): R[k*(RT+1) + row]
   __shared__ T dinv[NB];
-  PanelTask t = tasks[blockIdx.x];
+  const PanelTask t = tasks[blockIdx.x];
   T* a = arena + t.off;
   const int ld = t.ld, k0 = t.k0, w = t.w;
   const int tid = threadIdx.x;
@@ -119,41 +165,13 @@ __global__ void __launch_bounds__(RT) k_panel_chol(T* __restrict__ arena,
     int i = idx % w, j = idx / w;
     D[j * LDD + i] = (i >= j) ? a[(int64_t)(k0 + j) * ld + k0 + i] : T(0);
   }
-  // row tile load overlaps with the diagonal factorisation
-  const int rstart = max(t.r0, k0 + w);
-  const int r = rstart + tid;
+  const int r = t.r0 + tid;
   const bool has_row = r < t.r1;
   if (has_row)
     for (int k = 0; k < w; ++k) R[k * LDR + tid] = a[(int64_t)(k0 + k) * ld + r];
   __syncthreads();
-  for (int k = 0; k < w; ++k) {
-    if (tid == 0) {
-      T d = D[k * LDD + k];
-      if (!(d > T(0))) {
-        atomicOr(status, ST_NOT_POSDEF);
-        d = T(1);
-      }
-      d = sqrt(d);
-      D[k * LDD + k] = d;
-      dinv[k] = T(1) / d;
-    }
-    __syncthreads();
-    T inv = dinv[k];
-    for (int i = k + 1 + tid; i < w; i += RT) D[k * LDD + i] *= inv;
-    __syncthreads();
-    const int ww = w - k - 1;
-    for (int idx = tid; idx < ww * ww; idx += RT) {
-      int i = k + 1 + idx % ww, j = k + 1 + idx / ww;
-      if (i >= j) D[j * LDD + i] -= D[k * LDD + i] * D[k * LDD + j];
-    }
-    __syncthreads();
-  }
-  if (t.r0 <= k0) {
-    for (int idx = tid; idx < w * w; idx += RT) {
-      int i = idx % w, j = idx / w;
-      if (i >= j) a[(int64_t)(k0 + j) * ld + k0 + i] = D[j * LDD + i];
-    }
-  }
+  if (tid < w) dinv[tid] = T(1) / D[tid * LDD + tid];
+  __syncthreads();
   if (has_row) {
     // x L_kk^T = a_r  (forward substitution along the row)
     for (int j = 0; j < w; ++j) {
@@ -171,6 +189,7 @@ __global__ void __launch_bounds__(RT) k_panel_chol(T* __restrict__ arena,
 // ty*RM/2.. and TM/2+ty*RM/2..) and double-buffered KT-deep shared tiles.
 template <typename T, int TM, int TN, int KT>
 __global__ void __launch_bounds__(256) k_update(T* __restrict__ arena,
+                                                const T* __restrict__ abuf,
                                                 const UpdTask* __restrict__ tasks) {
   constexpr int RM = TM / 16, RN = TN / 16;
   constexpr int HM = RM / 2, HN = RN / 2;
@@ -178,8 +197,9 @@ __global__ void __launch_bounds__(256) k_update(T* __restrict__ arena,
   __shared__ __align__(16) T As[2][KT][TM];
   __shared__ __align__(16) T Bs[2][KT][TN];
   const UpdTask t = tasks[blockIdx.x];
-  T* base = arena + t.off;
-  const int ld = t.ld;
+  const T* A = abuf + t.a_off;
+  const T* B = arena + t.b_off;
+  T* C = arena + t.c_off;
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   T ra[LA], rb[LB];
   auto gload = [&](int kc) {
@@ -188,14 +208,14 @@ __global__ void __launch_bounds__(256) k_update(T* __restrict__ arena,
       int e = tid + q * 256;
       int i = e % TM, kk = e / TM;
       int row = t.row0 + i, k = kc + kk;
-      ra[q] = (row < t.rowEnd && k < t.k1) ? base[(int64_t)k * ld + row] : T(0);
+      ra[q] = (row < t.rowEnd && k < t.k1) ? A[(int64_t)k * t.lda + row] : T(0);
     }
 #pragma unroll
     for (int q = 0; q < LB; ++q) {
       int e = tid + q * 256;
       int i = e % TN, kk = e / TN;
       int col = t.col0 + i, k = kc + kk;
-      rb[q] = (col < t.colEnd && k < t.k1) ? base[(int64_t)k * ld + col] : T(0);
+      rb[q] = (col < t.colEnd && k < t.k1) ? B[(int64_t)k * t.ldb + col] : T(0);
     }
   };
   auto sstore = [&](int buf) {
@@ -256,7 +276,7 @@ __global__ void __launch_bounds__(256) k_update(T* __restrict__ arena,
     for (int j = 0; j < RN; ++j) {
       int col = t.col0 + ((j < HN) ? tx * HN + j : TN / 2 + tx * HN + (j - HN));
       if (col >= t.colEnd || col > row) continue;
-      base[(int64_t)col * ld + row] -= acc[i][j];
+      C[(int64_t)col * t.ldc + row] -= acc[i][j];
     }
   }
 }
@@ -294,7 +314,7 @@ void prepare_factor_kernels() {
   constexpr int SM = Tiles<T>::SMALL_M;
   SG_CUDA(cudaFuncSetAttribute(k_small_chol<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(sizeof(T) * SM * (SM + 1))));
-  SG_CUDA(cudaFuncSetAttribute(k_panel_chol<T, Tiles<T>::NB, Tiles<T>::RT>,
+  SG_CUDA(cudaFuncSetAttribute(k_panel_trsm<T, Tiles<T>::NB, Tiles<T>::RT>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)panel_smem<T>()));
 }
@@ -308,17 +328,23 @@ void launch_small_chol(T* arena, const SmallTask* t, int ntask, int maxm, unsign
 }
 
 template <typename T>
-void launch_panel_chol(T* arena, const PanelTask* t, int ntask, unsigned* status,
-                       cudaStream_t s) {
+void launch_diag_chol(T* arena, const PanelTask* t, int ntask, unsigned* status,
+                      cudaStream_t s) {
   if (ntask <= 0) return;
-  constexpr int NB = Tiles<T>::NB, RT = Tiles<T>::RT;
-  k_panel_chol<T, NB, RT><<<ntask, RT, panel_smem<T>(), s>>>(arena, t, status);
+  k_diag_chol<T, Tiles<T>::NB><<<ntask, 128, 0, s>>>(arena, t, status);
 }
 
 template <typename T>
-void launch_update(T* arena, const UpdTask* t, int ntask, cudaStream_t s) {
+void launch_panel_trsm(T* arena, const PanelTask* t, int ntask, cudaStream_t s) {
   if (ntask <= 0) return;
-  k_update<T, Tiles<T>::TM, Tiles<T>::TN, 16><<<ntask, 256, 0, s>>>(arena, t);
+  constexpr int NB = Tiles<T>::NB, RT = Tiles<T>::RT;
+  k_panel_trsm<T, NB, RT><<<ntask, RT, panel_smem<T>(), s>>>(arena, t);
+}
+
+template <typename T>
+void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_update<T, Tiles<T>::TM, Tiles<T>::TN, 16><<<ntask, 256, 0, s>>>(arena, abuf, t);
 }
 
 #define SG_INST(T)                                                                          \
@@ -328,8 +354,9 @@ void launch_update(T* arena, const UpdTask* t, int ntask, cudaStream_t s) {
   template void launch_extend_add<T>(T*, const ChildDesc*, const EaItem*, const int*, int,   \
                                      cudaStream_t);                                         \
   template void launch_small_chol<T>(T*, const SmallTask*, int, int, unsigned*, cudaStream_t); \
-  template void launch_panel_chol<T>(T*, const PanelTask*, int, unsigned*, cudaStream_t);    \
-  template void launch_update<T>(T*, const UpdTask*, int, cudaStream_t);
+  template void launch_diag_chol<T>(T*, const PanelTask*, int, unsigned*, cudaStream_t);     \
+  template void launch_panel_trsm<T>(T*, const PanelTask*, int, cudaStream_t);               \
+  template void launch_update<T>(T*, const T*, const UpdTask*, int, cudaStream_t);
 SG_INST(float)
 SG_INST(double)
 #undef SG_INST

@@ -258,6 +258,218 @@ __global__ void k_axpy(double* __restrict__ x, int ldx, const double* __restrict
   x[(int64_t)r * ldx + i] += d[(int64_t)r * n + i];
 }
 
+// ---------------------------------------------------------------------------
+// Large fronts: blocked multi-CTA sweeps.  One CTA solves each LB-wide
+// diagonal block (warp per right-hand side, lanes over rows); the rows below
+// are updated (forward) or reduced into the block (backward) by one CTA per
+// row tile, so a 6400-column front keeps the whole GPU busy.
+
+constexpr int LB = 64;
+
+template <typename ACC>
+__global__ void k_lgather(const FrontDesc* __restrict__ fr, const LTask* __restrict__ tasks,
+                          const int* __restrict__ rlist, const ACC* __restrict__ x, int n,
+                          int nrhs, ACC* __restrict__ scratch, const int64_t* __restrict__ scr_off,
+                          bool fwd) {
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const int i = t.r0 + threadIdx.x;
+  if (i >= f.m) return;
+  ACC* xs = scratch + scr_off[t.f] * nrhs;
+  const int v = rlist[f.rl + i];
+  for (int r = 0; r < nrhs; ++r)
+    xs[(int64_t)r * f.m + i] = (fwd && i >= f.n) ? ACC(0) : x[(int64_t)r * n + v];
+}
+
+template <typename ACC>
+__global__ void k_lscatter(const FrontDesc* __restrict__ fr, const LTask* __restrict__ tasks,
+                           const int* __restrict__ rlist, ACC* __restrict__ x, int n, int nrhs,
+                           const ACC* __restrict__ scratch, const int64_t* __restrict__ scr_off,
+                           bool fwd) {
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const int i = t.r0 + threadIdx.x;
+  if (i >= f.m) return;
+  if (!fwd && i >= f.n) return;
+  const ACC* xs = scratch + scr_off[t.f] * nrhs;
+  const int v = rlist[f.rl + i];
+  for (int r = 0; r < nrhs; ++r) {
+    ACC val = xs[(int64_t)r * f.m + i];
+    if (i < f.n) x[(int64_t)r * n + v] = val;
+    else aadd(x + (int64_t)r * n + v, val);
+  }
+}
+
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_lfwd_diag(const T* __restrict__ arena,
+                                                   const FrontDesc* __restrict__ fr,
+                                                   const LTask* __restrict__ tasks, int nrhs,
+                                                   ACC* __restrict__ scratch,
+                                                   const int64_t* __restrict__ scr_off,
+                                                   bool unit) {
+  __shared__ ACC Ls[LB][LB + 1];  // Ls[j][i] = L(c0+i, c0+j)
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const T* L = arena + f.off;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int idx = tid; idx < bw * bw; idx += blockDim.x) {
+    int i = idx % bw, j = idx / bw;
+    Ls[j][i] = (i >= j) ? (ACC)L[(int64_t)(c0 + j) * f.ld + c0 + i] : ACC(0);
+  }
+  __syncthreads();
+  ACC* xs = scratch + scr_off[t.f] * nrhs;
+  for (int r = warp; r < nrhs; r += blockDim.x / 32) {
+    ACC* xr = xs + (int64_t)r * f.m + c0;
+    ACC v0 = (lane < bw) ? xr[lane] : ACC(0);
+    ACC v1 = (32 + lane < bw) ? xr[32 + lane] : ACC(0);
+    for (int kk = 0; kk < bw; ++kk) {
+      ACC vk = __shfl_sync(0xffffffffu, kk < 32 ? v0 : v1, kk & 31);
+      if (!unit) vk = vk / Ls[kk][kk];
+      if (kk < 32) {
+        if (lane == kk) v0 = vk;
+      } else if (lane == kk - 32) {
+        v1 = vk;
+      }
+      if (lane > kk && lane < bw) v0 -= Ls[kk][lane] * vk;
+      if (32 + lane > kk && 32 + lane < bw) v1 -= Ls[kk][32 + lane] * vk;
+    }
+    if (lane < bw) xr[lane] = v0;
+    if (32 + lane < bw) xr[32 + lane] = v1;
+  }
+}
+
+// rows [r0, r0+128) of the block column: xs_i -= L_i,blk * y_blk
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(128) k_lfwd_upd(const T* __restrict__ arena,
+                                                  const FrontDesc* __restrict__ fr,
+                                                  const LTask* __restrict__ tasks, int nrhs,
+                                                  ACC* __restrict__ scratch,
+                                                  const int64_t* __restrict__ scr_off) {
+  __shared__ ACC ys[LB][MAXR];
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const T* L = arena + f.off;
+  ACC* xs = scratch + scr_off[t.f] * nrhs;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  for (int e = tid; e < bw * nrhs; e += blockDim.x) {
+    int k = e % bw, r = e / bw;
+    ys[k][r] = xs[(int64_t)r * f.m + c0 + k];
+  }
+  __syncthreads();
+  const int i = t.r0 + tid;
+  if (i >= f.m) return;
+  for (int r0 = 0; r0 < nrhs; r0 += 16) {
+    ACC acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = ACC(0);
+    for (int k = 0; k < bw; ++k) {
+      ACC l = (ACC)L[(int64_t)(c0 + k) * f.ld + i];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) acc[q] += l * ys[k][min(r0 + q, MAXR - 1)];
+    }
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      if (r0 + q < nrhs) xs[(int64_t)(r0 + q) * f.m + i] -= acc[q];
+  }
+}
+
+// rows [r0, r0+128) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r)
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_lbwd_red(const T* __restrict__ arena,
+                                                  const FrontDesc* __restrict__ fr,
+                                                  const LTask* __restrict__ tasks, int nrhs,
+                                                  const ACC* __restrict__ scratch,
+                                                  const int64_t* __restrict__ scr_off,
+                                                  ACC* __restrict__ tt) {
+  constexpr int SR = 32;  // rows per sub-tile
+  __shared__ ACC Lt[SR][LB + 1];
+  __shared__ ACC xt[SR][MAXR + 1];
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const T* L = arena + f.off;
+  const ACC* xs = scratch + scr_off[t.f] * nrhs;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  const int k = tid % LB, g = tid / LB;  // 4 groups share the right-hand sides
+  ACC acc[MAXR / 4];
+#pragma unroll
+  for (int q = 0; q < MAXR / 4; ++q) acc[q] = ACC(0);
+  const int rend = min(t.r0 + 128, f.m);
+  for (int s0 = t.r0; s0 < rend; s0 += SR) {
+    const int nr = min(SR, rend - s0);
+    for (int e = tid; e < SR * LB; e += blockDim.x) {
+      int i = e % SR, kk = e / SR;
+      Lt[i][kk] = (i < nr && kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * f.ld + s0 + i] : ACC(0);
+    }
+    for (int e = tid; e < SR * nrhs; e += blockDim.x) {
+      int i = e % SR, r = e / SR;
+      xt[i][r] = (i < nr) ? xs[(int64_t)r * f.m + s0 + i] : ACC(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < MAXR / 4; ++q) {
+      int r = g + 4 * q;
+      if (r < nrhs) {
+        ACC a = acc[q];
+        for (int i = 0; i < SR; ++i) a += Lt[i][k] * xt[i][r];
+        acc[q] = a;
+      }
+    }
+    __syncthreads();
+  }
+  if (k < bw)
+#pragma unroll
+    for (int q = 0; q < MAXR / 4; ++q) {
+      int r = g + 4 * q;
+      if (r < nrhs) aadd(&tt[((int64_t)t.f * LB + k) * MAXR + r], acc[q]);
+    }
+}
+
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_lbwd_diag(const T* __restrict__ arena,
+                                                   const FrontDesc* __restrict__ fr,
+                                                   const LTask* __restrict__ tasks, int nrhs,
+                                                   ACC* __restrict__ scratch,
+                                                   const int64_t* __restrict__ scr_off,
+                                                   ACC* __restrict__ tt, bool unit) {
+  __shared__ ACC Ls[LB][LB + 1];  // Ls[j][i] = L(c0+i, c0+j)
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const T* L = arena + f.off;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int idx = tid; idx < bw * bw; idx += blockDim.x) {
+    int i = idx % bw, j = idx / bw;
+    Ls[j][i] = (i >= j) ? (ACC)L[(int64_t)(c0 + j) * f.ld + c0 + i] : ACC(0);
+  }
+  __syncthreads();
+  ACC* xs = scratch + scr_off[t.f] * nrhs;
+  ACC* tf = tt + (int64_t)t.f * LB * MAXR;
+  for (int r = warp; r < nrhs; r += blockDim.x / 32) {
+    ACC* xr = xs + (int64_t)r * f.m + c0;
+    ACC v0 = (lane < bw) ? xr[lane] - tf[lane * MAXR + r] : ACC(0);
+    ACC v1 = (32 + lane < bw) ? xr[32 + lane] - tf[(32 + lane) * MAXR + r] : ACC(0);
+    for (int kk = bw - 1; kk >= 0; --kk) {
+      if (!unit) {
+        if (kk < 32) {
+          if (lane == kk) v0 = v0 / Ls[kk][kk];
+        } else if (lane == kk - 32) {
+          v1 = v1 / Ls[kk][kk];
+        }
+      }
+      ACC zk = __shfl_sync(0xffffffffu, kk < 32 ? v0 : v1, kk & 31);
+      if (lane < kk) v0 -= Ls[lane][kk] * zk;
+      if (32 + lane < kk) v1 -= Ls[32 + lane][kk] * zk;
+    }
+    if (lane < bw) {
+      xr[lane] = v0;
+      tf[lane * MAXR + r] = ACC(0);
+    }
+    if (32 + lane < bw) {
+      xr[32 + lane] = v1;
+      tf[(32 + lane) * MAXR + r] = ACC(0);
+    }
+  }
+}
+
 inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
 
 }  // namespace
@@ -336,6 +548,45 @@ void launch_axpy_inplace(double* x, int ldx, const double* d, int n, int nrhs, c
   k_axpy<<<nblocks(c, 256), 256, 0, s>>>(x, ldx, d, n, nrhs);
 }
 
+template <typename T, typename ACC>
+void launch_lsolve(int kind, const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+                   const int* rlist, ACC* x, int n, int nrhs, ACC* scratch,
+                   const int64_t* scr_off, ACC* tt, bool unit, cudaStream_t s) {
+  if (ntask <= 0) return;
+  if (nrhs > MAXR) throw CudaError("solve: more than 32 right-hand sides per launch");
+  switch (kind) {
+    case LS_GATHER_FWD:
+    case LS_GATHER_BWD:
+      k_lgather<ACC><<<ntask, 256, 0, s>>>(fr, tasks, rlist, x, n, nrhs, scratch, scr_off,
+                                           kind == LS_GATHER_FWD);
+      break;
+    case LS_SCATTER_FWD:
+    case LS_SCATTER_BWD:
+      k_lscatter<ACC><<<ntask, 256, 0, s>>>(fr, tasks, rlist, x, n, nrhs, scratch, scr_off,
+                                            kind == LS_SCATTER_FWD);
+      break;
+    case LS_FWD_DIAG:
+      k_lfwd_diag<T, ACC><<<ntask, 256, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off, unit);
+      break;
+    case LS_FWD_UPD:
+      k_lfwd_upd<T, ACC><<<ntask, 128, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off);
+      break;
+    case LS_BWD_RED:
+      k_lbwd_red<T, ACC><<<ntask, 256, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off, tt);
+      break;
+    case LS_BWD_DIAG:
+      k_lbwd_diag<T, ACC><<<ntask, 256, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off, tt,
+                                                unit);
+      break;
+  }
+}
+
+template void launch_lsolve<float, float>(int, const float*, const FrontDesc*, const LTask*, int,
+                                          const int*, float*, int, int, float*, const int64_t*,
+                                          float*, bool, cudaStream_t);
+template void launch_lsolve<double, double>(int, const double*, const FrontDesc*, const LTask*,
+                                            int, const int*, double*, int, int, double*,
+                                            const int64_t*, double*, bool, cudaStream_t);
 template void launch_solve_fwd<float, float>(const float*, const FrontDesc*, int, const int*,
                                              float*, int, int, float*, const int64_t*, bool,
                                              cudaStream_t);

@@ -87,6 +87,8 @@ int64_t FKeep::nnz_orig() const {
 }
 
 namespace {
+// fronts that get the blocked multi-CTA solve
+inline bool is_large(const FrontDesc& d) { return d.n >= 192 || (int64_t)d.m * d.n >= (1 << 18); }
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
 inline int64_t round_up64(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 }  // namespace
@@ -149,19 +151,27 @@ void FKeep::plan_cholesky() {
   }
   ninit = (int64_t)asrc.size();
 
-  // rlist (0-based) and solve descriptors in level order
+  // rlist (0-based) and solve descriptors in level order, small fronts first
   std::vector<int> rl0(st.rlist.size());
   for (size_t k = 0; k < st.rlist.size(); ++k) rl0[k] = st.rlist[k] - 1;
   hfr.resize(ns);
   hscr.resize(ns);
+  for (int k = 0; k < ns; ++k) {
+    int s = order[k];
+    hfr[k] = FrontDesc{off[s], ld[s], st.nrow[s], st.ncol[s], (int)(st.rptr[s] - 1), 0};
+  }
+  {
+    std::vector<int> pm = SolvePlan::small_first(hfr, levels);
+    std::vector<FrontDesc> t(ns);
+    for (int k = 0; k < ns; ++k) t[k] = hfr[pm[k]];
+    hfr.swap(t);
+  }
   scratch_rows = 0;
   for (auto& L : levels) {
     int64_t acc = 0;
     for (int k = L.f0; k < L.f1; ++k) {
-      int s = order[k];
-      hfr[k] = FrontDesc{off[s], ld[s], st.nrow[s], st.ncol[s], (int)(st.rptr[s] - 1), 0};
       hscr[k] = acc;
-      acc += st.nrow[s];
+      acc += hfr[k].m;
     }
     scratch_rows = std::max(scratch_rows, acc);
   }
@@ -171,7 +181,7 @@ void FKeep::plan_cholesky() {
   std::vector<EaItem> items;
   std::vector<int> maps;
   std::vector<SmallTask> smalls;
-  std::vector<PanelTask> panels;
+  std::vector<PanelTask> panels, diags;
   std::vector<UpdTask> upds;
   std::vector<int> pos(st.n, -1);
   ops.clear();
@@ -220,20 +230,24 @@ void FKeep::plan_cholesky() {
     for (int s : large) maxsteps = std::max(maxsteps, (st.ncol[s] + NB - 1) / NB);
     for (int step = 0; step < maxsteps; ++step) {
       int64_t p0 = (int64_t)panels.size(), u0 = (int64_t)upds.size();
+      int64_t d0 = (int64_t)diags.size();
       for (int s : large) {
         int m = st.nrow[s], n = st.ncol[s];
         int k0 = step * NB;
         if (k0 >= n) continue;
         int w = std::min(NB, n - k0);
-        for (int r0 = k0; r0 < m; r0 += RT)
+        diags.push_back({off[s], ld[s], k0, w, k0, k0 + w, 0});
+        for (int r0 = k0 + w; r0 < m; r0 += RT)
           panels.push_back({off[s], ld[s], k0, w, r0, std::min(r0 + RT, m), 0});
         int o = k0 + w;
         if (o < n) {
           for (int cj = 0; o + cj * TM < n; ++cj)
             for (int ri = cj; o + ri * TM < m; ++ri)
-              upds.push_back({off[s], ld[s], o + ri * TM, o + cj * TM, m, n, k0, k0 + w, 0});
+              upds.push_back({off[s], off[s], off[s], ld[s], ld[s], ld[s], o + ri * TM,
+                              o + cj * TM, m, n, k0, k0 + w, 0});
         }
       }
+      if ((int64_t)diags.size() > d0) ops.push_back({Op::DIAG, d0, (int64_t)diags.size(), 0});
       if ((int64_t)panels.size() > p0) ops.push_back({Op::PANEL, p0, (int64_t)panels.size(), 0});
       if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
     }
@@ -244,7 +258,8 @@ void FKeep::plan_cholesky() {
       if (m <= n) continue;
       for (int cj = 0; n + cj * TM < m; ++cj)
         for (int ri = cj; n + ri * TM < m; ++ri)
-          upds.push_back({off[s], ld[s], n + ri * TM, n + cj * TM, m, m, 0, n, 0});
+          upds.push_back({off[s], off[s], off[s], ld[s], ld[s], ld[s], n + ri * TM,
+                          n + cj * TM, m, m, 0, n, 0});
     }
     if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
   }
@@ -271,9 +286,11 @@ void FKeep::plan_cholesky() {
   eamaps.upload(maps, s);
   small.upload(smalls, s);
   panel.upload(panels, s);
+  diagt.upload(diags, s);
   upd.upload(upds, s);
   dfr.upload(hfr, s);
   dscr.upload(hscr, s);
+  splan.build_tasks(hfr, levels, s);
   rlist0.upload(rl0, s);
   std::vector<int> p0(st.n);
   for (int i = 0; i < st.n; ++i) p0[i] = st.perm[i];
@@ -318,11 +335,14 @@ void FKeep::run_ops(cudaStream_t s) {
       case Op::SMALL:
         launch_small_chol<T>(A, small.as<SmallTask>() + op.a, (int)cnt, op.aux, stp, s);
         break;
+      case Op::DIAG:
+        launch_diag_chol<T>(A, diagt.as<PanelTask>() + op.a, (int)cnt, stp, s);
+        break;
       case Op::PANEL:
-        launch_panel_chol<T>(A, panel.as<PanelTask>() + op.a, (int)cnt, stp, s);
+        launch_panel_trsm<T>(A, panel.as<PanelTask>() + op.a, (int)cnt, s);
         break;
       case Op::UPD:
-        launch_update<T>(A, upd.as<UpdTask>() + op.a, (int)cnt, s);
+        launch_update<T>(A, A, upd.as<UpdTask>() + op.a, (int)cnt, s);
         break;
     }
   }
@@ -423,30 +443,123 @@ int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, c
 
 // ---------------------------------------------------------------------------
 
+std::vector<int> SolvePlan::small_first(const std::vector<FrontDesc>& hfr,
+                                        const std::vector<Level>& levels) {
+  std::vector<int> pm(hfr.size());
+  std::iota(pm.begin(), pm.end(), 0);
+  for (const Level& L : levels)
+    std::stable_sort(pm.begin() + L.f0, pm.begin() + L.f1, [&](int a, int b) {
+      return is_large(hfr[a]) < is_large(hfr[b]);
+    });
+  return pm;
+}
+
+void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector<Level>& levels,
+                            cudaStream_t s) {
+  const int LB = LSOLVE_BW;
+  lv.clear();
+  htasks.clear();
+  max_large = 0;
+  for (const Level& L : levels) {
+    Lv v;
+    v.f0 = L.f0;
+    v.nfront = L.f1 - L.f0;
+    v.nsmall = 0;
+    while (v.nsmall < v.nfront && !is_large(hfr[L.f0 + v.nsmall])) v.nsmall++;
+    max_large = std::max(max_large, v.nfront);
+    auto add_rows_tasks = [&](std::vector<SOp>& ops, int kind, int step, bool gather) {
+      int64_t a = (int64_t)htasks.size();
+      for (int f = v.nsmall; f < v.nfront; ++f) {
+        const FrontDesc& d = hfr[L.f0 + f];
+        if (gather) {
+          for (int r0 = 0; r0 < d.m; r0 += 256) htasks.push_back({f, 0, 0, r0});
+        } else {
+          int c0 = step * LB;
+          if (c0 >= d.n) continue;
+          int bw = std::min(LB, d.n - c0);
+          if (kind == LS_FWD_DIAG || kind == LS_BWD_DIAG) {
+            htasks.push_back({f, c0, bw, 0});
+          } else {
+            for (int r0 = c0 + bw; r0 < d.m; r0 += 128) htasks.push_back({f, c0, bw, r0});
+          }
+        }
+      }
+      int64_t b = (int64_t)htasks.size();
+      if (b > a) ops.push_back({kind, a, b});
+    };
+    if (v.nsmall < v.nfront) {
+      int maxb = 0;
+      for (int f = v.nsmall; f < v.nfront; ++f)
+        maxb = std::max(maxb, (hfr[L.f0 + f].n + LB - 1) / LB);
+      add_rows_tasks(v.fwd, LS_GATHER_FWD, 0, true);
+      for (int b = 0; b < maxb; ++b) {
+        add_rows_tasks(v.fwd, LS_FWD_DIAG, b, false);
+        add_rows_tasks(v.fwd, LS_FWD_UPD, b, false);
+      }
+      add_rows_tasks(v.fwd, LS_SCATTER_FWD, 0, true);
+      add_rows_tasks(v.bwd, LS_GATHER_BWD, 0, true);
+      for (int b = maxb - 1; b >= 0; --b) {
+        add_rows_tasks(v.bwd, LS_BWD_RED, b, false);
+        add_rows_tasks(v.bwd, LS_BWD_DIAG, b, false);
+      }
+      add_rows_tasks(v.bwd, LS_SCATTER_BWD, 0, true);
+    }
+    lv.push_back(std::move(v));
+  }
+  tasks.upload(htasks, s);
+}
+
+template <typename T, typename ACC>
+void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* rlist, ACC* x,
+                    int n, int nrhs, ACC* scratch, const int64_t* dscr, bool unit,
+                    cudaStream_t s) {
+  tt.ensure((size_t)std::max(max_large, 1) * LSOLVE_BW * 32 * sizeof(ACC));
+  auto level = [&](const Lv& v) {
+    const FrontDesc* fr = dfr + v.f0;
+    const int64_t* sc = dscr + v.f0;
+    if (v.nsmall > 0) {
+      if (fwd) launch_solve_fwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc,
+                                        unit, s);
+      else launch_solve_bwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc, unit,
+                                    s);
+    }
+    const std::vector<SOp>& ops = fwd ? v.fwd : v.bwd;
+    if (!ops.empty() && !fwd)
+      SG_CUDA(cudaMemsetAsync(tt.p, 0, (size_t)v.nfront * LSOLVE_BW * 32 * sizeof(ACC), s));
+    for (const SOp& op : ops)
+      launch_lsolve<T, ACC>(op.kind, arena, fr, tasks.as<LTask>() + op.a,
+                            (int)(op.b - op.a), rlist, x, n, nrhs, scratch, sc, tt.as<ACC>(),
+                            unit, s);
+  };
+  if (fwd)
+    for (const Lv& v : lv) level(v);
+  else
+    for (int l = (int)lv.size() - 1; l >= 0; --l) level(lv[l]);
+}
+
+template void SolvePlan::run<float, float>(bool, const float*, const FrontDesc*, const int*,
+                                           float*, int, int, float*, const int64_t*, bool,
+                                           cudaStream_t);
+template void SolvePlan::run<double, double>(bool, const double*, const FrontDesc*, const int*,
+                                             double*, int, int, double*, const int64_t*, bool,
+                                             cudaStream_t);
+
 template <typename T>
 void FKeep::solve_pivot_order(int job, void* xpv, int nrhs, cudaStream_t s) {
   using ACC = T;
   ACC* xpd = static_cast<ACC*>(xpv);
   const int n = ak->n;
   const T* A = arena.as<T>();
-  scratch.ensure(std::max<int64_t>(scratch_rows * nrhs, 1) * sizeof(ACC));
+  scratch.ensure(std::max<int64_t>(scratch_rows * std::min(nrhs, 32), 1) * sizeof(ACC));
   bool fwd = job == 0 || job == 1;
   bool bwd = job == 0 || job == 3 || job == 4;
-  const FrontDesc* fr = dfr.as<FrontDesc>();
-  const int64_t* sc = dscr.as<int64_t>();
   for (int r0 = 0; r0 < nrhs; r0 += 32) {
     int nr = std::min(32, nrhs - r0);
     ACC* xr = xpd + (int64_t)r0 * n;
-    if (fwd)
-      for (auto& L : levels)
-        launch_solve_fwd<T, ACC>(A, fr + L.f0, L.f1 - L.f0, rlist0.as<int>(), xr, n, nr,
-                                 scratch.as<ACC>(), sc + L.f0, !posdef, s);
-    if (bwd)
-      for (int l = (int)levels.size() - 1; l >= 0; --l) {
-        auto& L = levels[l];
-        launch_solve_bwd<T, ACC>(A, fr + L.f0, L.f1 - L.f0, rlist0.as<int>(), xr, n, nr,
-                                 scratch.as<ACC>(), sc + L.f0, !posdef, s);
-      }
+    if (fwd) splan.run<T, ACC>(true, A, dfr.as<FrontDesc>(), rlist0.as<int>(), xr, n, nr,
+                               scratch.as<ACC>(), dscr.as<int64_t>(), !posdef, s);
+    if (bwd) splan.run<T, ACC>(false, A, dfr.as<FrontDesc>(), rlist0.as<int>(), xr, n, nr,
+                               scratch.as<ACC>(), dscr.as<int64_t>(), !posdef, s);
   }
 }
 

@@ -73,13 +73,41 @@ struct AKeep {
 
 // One kernel launch of the factor schedule.
 struct Op {
-  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD } kind;
+  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG } kind;
   int64_t a = 0, b = 0;  // task range [a, b)
   int aux = 0;           // SMALL: max front rows in the launch
 };
 
 struct Level {
   int f0 = 0, f1 = 0;  // fronts [f0, f1) of the level-ordered front table
+};
+
+// Solve schedule over a level-ordered front table: per level the small
+// fronts (one CTA each) come first, then the large fronts, which run blocked
+// multi-CTA sweeps.
+struct SolvePlan {
+  struct SOp {
+    int kind;      // LsKind
+    int64_t a, b;  // task range
+  };
+  struct Lv {
+    int f0 = 0, nsmall = 0, nfront = 0;
+    std::vector<SOp> fwd, bwd;
+  };
+  std::vector<Lv> lv;
+  std::vector<LTask> htasks;
+  DevMem tasks, tt;
+  int max_large = 0;
+  // Reorder each level small-first (perm[k] = old position of new k) and
+  // build the task lists; hfr must already be in that order on entry to
+  // build_tasks.
+  static std::vector<int> small_first(const std::vector<FrontDesc>& hfr,
+                                      const std::vector<Level>& levels);
+  void build_tasks(const std::vector<FrontDesc>& hfr, const std::vector<Level>& levels,
+                   cudaStream_t s);
+  template <typename T, typename ACC>
+  void run(bool fwd, const T* arena, const FrontDesc* dfr, const int* rlist, ACC* x, int n,
+           int nrhs, ACC* scratch, const int64_t* dscr, bool unit, cudaStream_t s);
 };
 
 struct FKeep {
@@ -111,7 +139,7 @@ struct FKeep {
 
   // device data
   DevMem arena, val, cval, faval, frow, fcol, fidx, srcptr, src, status, anorm;
-  DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, small, panel, upd;
+  DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, small, panel, upd, diagt;
   DevMem dfr, dscr, rlist0, perm0;
   DevMem xp, scratch, bcopy, resid, norms;
   cudaGraphExec_t graph = nullptr;
@@ -130,6 +158,7 @@ struct FKeep {
 
   // LDL^T state (ldlt.cpp)
   std::shared_ptr<struct LdltState> ldlt;
+  SolvePlan splan;
 
   ~FKeep();
   void plan_cholesky();
