@@ -248,6 +248,23 @@ int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, 
 int sylver_gb300_fkeep_counters(void const* fkeep, long* kernel_launches, int* nlevels,
                                 double* factor_ms);
 
+/* No counterpart in the reference.  Allocation-free forward solve L y = b of
+ * an existing factorization `tree` (an fkeep, or a tree from
+ * spldlt_create_numeric_tree_dbl) with FP64 factors, for callers that cannot
+ * let a library allocate device memory: applications whose own pool
+ * allocator owns the device memory budget, or code that must not risk the
+ * device-wide synchronisation of cudaMalloc/cudaFree.  x_dev is device
+ * memory, ldx x nrhs, indexed in pivot order like spldlt_tree_solve_fwd_dbl;
+ * `stream` is a cudaStream_t (null: the library stream); the call returns
+ * after the solve completes.  Its only scratch is a fixed 16 MiB __device__
+ * array in the library image: a level needing more than 2,097,152 doubles
+ * (sum of the level's front rows x min(nrhs, 32)) returns
+ * SYLVER_ERROR_X_SIZE.  The first call on a device looks up that array's
+ * address; make it before any stream capture.  All calls share the array,
+ * so calls that overlap on the GPU race.  Returns a reference flag. */
+int spldlt_tree_solve_fwd_noalloc_dbl(bool posdef, void const* tree, int nrhs, double* x_dev,
+                                      int ldx, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

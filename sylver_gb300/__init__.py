@@ -76,7 +76,7 @@ EXPORTS = (
     "spldlt_tree_solve_bwd_posdef_dbl", "spldlt_factorize_mixed", "spldlt_factorize_device",
     "spldlt_solve_device", "sylver_gb300_solve_stats", "sylver_gb300_akeep_sizes",
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
-    "sylver_gb300_stream", "sylver_gb300_profile_factor",
+    "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
 )
 
 
@@ -126,6 +126,7 @@ def load(path: str | None = None):
         "spldlt_tree_solve_bwd_dbl": (I, [B, P, I, P, I]),
         "spldlt_tree_solve_diag_dbl": (I, [B, P, I, P, I]),
         "spldlt_tree_solve_diag_bwd_dbl": (I, [B, P, I, P, I]),
+        "spldlt_tree_solve_fwd_noalloc_dbl": (I, [B, P, I, P, I, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -549,6 +549,17 @@ void ldlt_solve_pivot_order(FKeep& fk, int job, double* xp, int nrhs, cudaStream
   ldlt_solve_t<double>(fk, job, xp, nrhs, s);
 }
 
+bool ldlt_solve_tables(const FKeep& fk, const FrontDesc** fr, const int64_t** scr,
+                       const int** rows, int64_t* scratch_rows) {
+  if (!fk.ldlt || fk.ldlt->hsfr.empty()) return false;
+  const LdltState& L = *fk.ldlt;
+  *fr = L.sfr.as<FrontDesc>();
+  *scr = L.sscr.as<int64_t>();
+  *rows = L.dvar.as<int>();
+  *scratch_rows = L.scratch_rows;
+  return true;
+}
+
 int ldlt_export_diag(const FKeep& fk, double* d, int* piv_order) {
   if (!fk.ldlt) return 0;
   const LdltState& L = *fk.ldlt;
