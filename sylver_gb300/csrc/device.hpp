@@ -126,17 +126,39 @@ void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const in
 // FrontDesc array; c0/bw give the diagonal block, r0 the first row of a tile.
 struct LTask {
   int f, c0, bw, r0;
+  int ntiles;  // backward step: row tiles of this front in the launch
+  int pad;
 };
 enum LsKind {
-  LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD,
-  LS_FWD_DIAG, LS_FWD_UPD, LS_BWD_RED, LS_BWD_DIAG
+  LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD, LS_FWD_STEP, LS_BWD_STEP
 };
 constexpr int LSOLVE_BW = 64;
-// tt: per front of the level, 64 x 32 accumulators (zero on entry, left zero).
+// Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
+// explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
+// index), tt: 64 x 32 accumulators per front, cnt: one ticket counter per
+// front (both zero on entry and left zero).
 template <typename T, typename ACC>
-void launch_lsolve(int kind, const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
-                   const int* rlist, ACC* x, int n, int nrhs, ACC* scratch,
-                   const int64_t* scr_off, ACC* tt, bool unit, cudaStream_t s);
+struct LsArgs {
+  const T* arena;
+  const FrontDesc* fr;
+  const int* rlist;
+  ACC* x;
+  int n, nrhs;
+  ACC* scratch;
+  ACC* ys;
+  const int64_t* scr_off;
+  const T* inv;
+  const int64_t* inv_off;
+  ACC* tt;
+  unsigned* cnt;
+};
+template <typename T, typename ACC>
+void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cudaStream_t s);
+// Explicit inverse of each diagonal block: task (front f, c0, bw), output at
+// inv + inv_off[f] + (c0/64)*64*64, column-major 64 x 64, identity padded.
+template <typename T>
+void launch_inv_diag(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+                     T* inv, const int64_t* inv_off, bool unit, cudaStream_t s);
 
 template <typename ACC>
 void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, int n, int nrhs,

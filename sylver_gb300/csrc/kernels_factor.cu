@@ -104,46 +104,43 @@ __global__ void __launch_bounds__(256) k_small_chol(T* __restrict__ arena,
 
 // ---------------------------------------------------------------------------
 // Panel step, part 1: Cholesky of the w x w diagonal block at (k0, k0), one
-// CTA per front, in place.
+// CTA of four warps per front, in shared memory: warp q updates the trailing
+// columns j = q (mod 4), lanes run down the rows.
 template <typename T, int NB>
 __global__ void __launch_bounds__(128) k_diag_chol(T* __restrict__ arena,
                                                    const PanelTask* __restrict__ tasks,
                                                    unsigned* status) {
   __shared__ T D[NB][NB + 1];  // D[j][i] = A(i, j)
-  __shared__ T dinv;
   const PanelTask t = tasks[blockIdx.x];
   T* a = arena + t.off;
-  const int ld = t.ld, k0 = t.k0, w = t.w, tid = threadIdx.x;
-  for (int idx = tid; idx < w * w; idx += blockDim.x) {
-    int i = idx % w, j = idx / w;
-    if (i >= j) D[j][i] = a[(int64_t)(k0 + j) * ld + k0 + i];
+  const int ld = t.ld, k0 = t.k0, w = t.w, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll 4
+  for (int e = tid; e < NB * NB; e += 128) {
+    int i = e % NB, j = e / NB;
+    if (i < w && j < w && i >= j) D[j][i] = a[(int64_t)(k0 + j) * ld + k0 + i];
   }
   __syncthreads();
   for (int k = 0; k < w; ++k) {
-    if (tid == 0) {
-      T d = D[k][k];
-      if (!(d > T(0))) {
-        atomicOr(status, ST_NOT_POSDEF);
-        d = T(1);
-      }
-      d = sqrt(d);
-      D[k][k] = d;
-      dinv = T(1) / d;
+    T d = D[k][k];
+    if (!(d > T(0))) {
+      if (tid == 0) atomicOr(status, ST_NOT_POSDEF);
+      d = T(1);
+    }
+    const T inv = T(1) / sqrt(d);
+    // column k below the diagonal, scaled into registers; row k+1.. by lanes
+    for (int j = k + 1 + warp; j < w; j += 4) {
+      const T ljk = D[k][j] * inv;
+      for (int i = j + lane; i < w; i += 32) D[j][i] -= D[k][i] * inv * ljk;
     }
     __syncthreads();
-    const T inv = dinv;
-    for (int i = k + 1 + tid; i < w; i += blockDim.x) D[k][i] *= inv;
-    __syncthreads();
-    const int ww = w - k - 1;
-    for (int idx = tid; idx < ww * ww; idx += blockDim.x) {
-      int i = k + 1 + idx % ww, j = k + 1 + idx / ww;
-      if (i >= j) D[j][i] -= D[k][i] * D[k][j];
-    }
+    if (tid == 0) D[k][k] = sqrt(d);
+    for (int i = k + 1 + tid; i < w; i += 128) D[k][i] *= inv;
     __syncthreads();
   }
-  for (int idx = tid; idx < w * w; idx += blockDim.x) {
-    int i = idx % w, j = idx / w;
-    if (i >= j) a[(int64_t)(k0 + j) * ld + k0 + i] = D[j][i];
+#pragma unroll 4
+  for (int e = tid; e < NB * NB; e += 128) {
+    int i = e % NB, j = e / NB;
+    if (i < w && j < w && i >= j) a[(int64_t)(k0 + j) * ld + k0 + i] = D[j][i];
   }
 }
 
@@ -167,8 +164,11 @@ __global__ void __launch_bounds__(RT) k_panel_trsm(T* __restrict__ arena,
   }
   const int r = t.r0 + tid;
   const bool has_row = r < t.r1;
-  if (has_row)
-    for (int k = 0; k < w; ++k) R[k * LDR + tid] = a[(int64_t)(k0 + k) * ld + r];
+  if (has_row) {
+#pragma unroll 16
+    for (int k = 0; k < NB; ++k)
+      if (k < w) R[k * LDR + tid] = a[(int64_t)(k0 + k) * ld + r];
+  }
   __syncthreads();
   if (tid < w) dinv[tid] = T(1) / D[tid * LDD + tid];
   __syncthreads();
@@ -179,7 +179,9 @@ __global__ void __launch_bounds__(RT) k_panel_trsm(T* __restrict__ arena,
       R[j * LDR + tid] = x;
       for (int k = j + 1; k < w; ++k) R[k * LDR + tid] -= x * D[j * LDD + k];
     }
-    for (int k = 0; k < w; ++k) a[(int64_t)(k0 + k) * ld + r] = R[k * LDR + tid];
+#pragma unroll 16
+    for (int k = 0; k < NB; ++k)
+      if (k < w) a[(int64_t)(k0 + k) * ld + r] = R[k * LDR + tid];
   }
 }
 

@@ -33,6 +33,7 @@ __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
                                                    const int64_t* __restrict__ scr_off,
                                                    bool unit) {
   __shared__ ACC y[SB][MAXR];
+  for (int e = threadIdx.x; e < SB * MAXR; e += blockDim.x) (&y[0][0])[e] = ACC(0);
   const FrontDesc f = fr[blockIdx.x];
   const T* L = arena + f.off;
   const int ld = f.ld, m = f.m, nc = f.n;
@@ -68,8 +69,9 @@ __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
         ACC acc[RC];
 #pragma unroll
         for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
-        for (int kk = 0; kk < bw; ++kk) {
-          ACC l = (ACC)L[(int64_t)(c0 + kk) * ld + i];
+#pragma unroll 8
+        for (int kk = 0; kk < SB; ++kk) {
+          const ACC l = (kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * ld + i] : ACC(0);
 #pragma unroll
           for (int q = 0; q < RC; ++q) acc[q] += l * y[kk][min(r0 + q, MAXR - 1)];
         }
@@ -118,6 +120,7 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
         ACC acc[RC];
 #pragma unroll
         for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
+#pragma unroll 4
         for (int i = c1 + lane; i < m; i += 32) {
           ACC l = (ACC)col[i];
 #pragma unroll
@@ -259,136 +262,146 @@ __global__ void k_axpy(double* __restrict__ x, int ldx, const double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Large fronts: blocked multi-CTA sweeps.  One CTA solves each LB-wide
-// diagonal block (warp per right-hand side, lanes over rows); the rows below
-// are updated (forward) or reduced into the block (backward) by one CTA per
-// row tile, so a 6400-column front keeps the whole GPU busy.
+// Large fronts: blocked multi-CTA sweeps with explicit inverses of the 64x64
+// diagonal blocks (computed once per factorization).  Forward step b: every
+// CTA forms y_b = L_bb^-1 x_b itself and updates its own rows below the
+// block; y_b goes to a separate slab so no CTA overwrites what others read.
+// Backward step b: CTAs reduce L_{i,b}^T x_i over their rows into tt, and
+// the last CTA to finish (atomic ticket, no waiting) solves the block.
 
-constexpr int LB = 64;
+constexpr int LB = LSOLVE_BW;
 
-template <typename ACC>
-__global__ void k_lgather(const FrontDesc* __restrict__ fr, const LTask* __restrict__ tasks,
-                          const int* __restrict__ rlist, const ACC* __restrict__ x, int n,
-                          int nrhs, ACC* __restrict__ scratch, const int64_t* __restrict__ scr_off,
-                          bool fwd) {
+template <typename T, typename ACC>
+__global__ void k_lgather(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
   const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = fr[t.f];
+  const FrontDesc f = a.fr[t.f];
   const int i = t.r0 + threadIdx.x;
   if (i >= f.m) return;
-  ACC* xs = scratch + scr_off[t.f] * nrhs;
-  const int v = rlist[f.rl + i];
-  for (int r = 0; r < nrhs; ++r)
-    xs[(int64_t)r * f.m + i] = (fwd && i >= f.n) ? ACC(0) : x[(int64_t)r * n + v];
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  const int v = a.rlist[f.rl + i];
+  for (int r = 0; r < a.nrhs; ++r)
+    xs[(int64_t)r * f.m + i] = (fwd && i >= f.n) ? ACC(0) : a.x[(int64_t)r * a.n + v];
 }
 
-template <typename ACC>
-__global__ void k_lscatter(const FrontDesc* __restrict__ fr, const LTask* __restrict__ tasks,
-                           const int* __restrict__ rlist, ACC* __restrict__ x, int n, int nrhs,
-                           const ACC* __restrict__ scratch, const int64_t* __restrict__ scr_off,
-                           bool fwd) {
+template <typename T, typename ACC>
+__global__ void k_lscatter(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
   const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = fr[t.f];
+  const FrontDesc f = a.fr[t.f];
   const int i = t.r0 + threadIdx.x;
   if (i >= f.m) return;
   if (!fwd && i >= f.n) return;
-  const ACC* xs = scratch + scr_off[t.f] * nrhs;
-  const int v = rlist[f.rl + i];
-  for (int r = 0; r < nrhs; ++r) {
-    ACC val = xs[(int64_t)r * f.m + i];
-    if (i < f.n) x[(int64_t)r * n + v] = val;
-    else aadd(x + (int64_t)r * n + v, val);
+  const int64_t so = a.scr_off[t.f] * a.nrhs;
+  const int v = a.rlist[f.rl + i];
+  for (int r = 0; r < a.nrhs; ++r) {
+    const int64_t e = so + (int64_t)r * f.m + i;
+    ACC* dst = a.x + (int64_t)r * a.n + v;
+    if (i >= f.n) aadd(dst, a.scratch[e]);
+    else *dst = fwd ? a.ys[e] : a.scratch[e];
   }
 }
 
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_lfwd_diag(const T* __restrict__ arena,
-                                                   const FrontDesc* __restrict__ fr,
-                                                   const LTask* __restrict__ tasks, int nrhs,
-                                                   ACC* __restrict__ scratch,
-                                                   const int64_t* __restrict__ scr_off,
-                                                   bool unit) {
-  __shared__ ACC Ls[LB][LB + 1];  // Ls[j][i] = L(c0+i, c0+j)
+// X = L^-1 for one diagonal block, thread j computes column j; L is read
+// straight from the front (all threads read the same element: broadcast).
+template <typename T>
+__global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
+                                                 const FrontDesc* __restrict__ fr,
+                                                 const LTask* __restrict__ tasks,
+                                                 T* __restrict__ inv,
+                                                 const int64_t* __restrict__ inv_off, bool unit) {
+  __shared__ T Xs[LB][LB + 1];  // Xs[j][i] = X(i, j)
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = fr[t.f];
   const T* L = arena + f.off;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int idx = tid; idx < bw * bw; idx += blockDim.x) {
-    int i = idx % bw, j = idx / bw;
-    Ls[j][i] = (i >= j) ? (ACC)L[(int64_t)(c0 + j) * f.ld + c0 + i] : ACC(0);
+  const int c0 = t.c0, bw = t.bw, j = threadIdx.x;
+  auto l = [&](int i, int k) -> T {  // padded block: identity outside bw
+    if (i >= bw || k >= bw) return (i == k) ? T(1) : T(0);
+    if (i == k && unit) return T(1);
+    return L[(int64_t)(c0 + k) * f.ld + c0 + i];
+  };
+  for (int i = 0; i < LB; ++i) {
+    T acc = (i == j) ? T(1) : T(0);
+    if (i > j)
+      for (int k = j; k < i; ++k) acc -= l(i, k) * Xs[j][k];
+    Xs[j][i] = (i >= j) ? acc / l(i, i) : T(0);
+  }
+  T* out = inv + inv_off[t.f] + (int64_t)(c0 / LB) * LB * LB;
+  __syncthreads();
+  for (int e = j; e < LB * LB; e += LB) out[e] = Xs[e / LB][e % LB];
+}
+
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(128) k_lfwd_step(const LTask* __restrict__ tasks,
+                                                   LsArgs<T, ACC> a) {
+  __shared__ ACC xb[LB][MAXR + 1];
+  __shared__ ACC ysh[LB][MAXR];
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  const T* L = a.arena + f.off;
+  const int nrhs = a.nrhs, c0 = t.c0, bw = t.bw, c1 = c0 + bw, tid = threadIdx.x;
+  ACC* xs = a.scratch + a.scr_off[t.f] * nrhs;
+  const T* Li = a.inv + a.inv_off[t.f] + (int64_t)(c0 / LB) * LB * LB;
+  for (int e = tid; e < LB * nrhs; e += blockDim.x) {
+    int k = e % LB, r = e / LB;
+    xb[k][r] = (k < bw) ? xs[(int64_t)r * f.m + c0 + k] : ACC(0);
   }
   __syncthreads();
-  ACC* xs = scratch + scr_off[t.f] * nrhs;
-  for (int r = warp; r < nrhs; r += blockDim.x / 32) {
-    ACC* xr = xs + (int64_t)r * f.m + c0;
-    ACC v0 = (lane < bw) ? xr[lane] : ACC(0);
-    ACC v1 = (32 + lane < bw) ? xr[32 + lane] : ACC(0);
-    for (int kk = 0; kk < bw; ++kk) {
-      ACC vk = __shfl_sync(0xffffffffu, kk < 32 ? v0 : v1, kk & 31);
-      if (!unit) vk = vk / Ls[kk][kk];
-      if (kk < 32) {
-        if (lane == kk) v0 = vk;
-      } else if (lane == kk - 32) {
-        v1 = vk;
-      }
-      if (lane > kk && lane < bw) v0 -= Ls[kk][lane] * vk;
-      if (32 + lane > kk && 32 + lane < bw) v1 -= Ls[kk][32 + lane] * vk;
+  // y = L_bb^-1 x_b: thread (row i = tid % 64, half h = tid / 64) does 16 rhs
+  {
+    const int i = tid % LB, h = tid / LB;
+    ACC acc[16];
+#pragma unroll
+    for (int q = 0; q < 16; ++q) acc[q] = ACC(0);
+#pragma unroll 16
+    for (int k = 0; k < LB; ++k) {
+      const ACC l = (ACC)Li[(int64_t)k * LB + i];  // zero above the diagonal
+#pragma unroll
+      for (int q = 0; q < 16; ++q) acc[q] += l * xb[k][min(16 * h + q, MAXR - 1)];
     }
-    if (lane < bw) xr[lane] = v0;
-    if (32 + lane < bw) xr[32 + lane] = v1;
-  }
-}
-
-// rows [r0, r0+128) of the block column: xs_i -= L_i,blk * y_blk
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(128) k_lfwd_upd(const T* __restrict__ arena,
-                                                  const FrontDesc* __restrict__ fr,
-                                                  const LTask* __restrict__ tasks, int nrhs,
-                                                  ACC* __restrict__ scratch,
-                                                  const int64_t* __restrict__ scr_off) {
-  __shared__ ACC ys[LB][MAXR];
-  const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = fr[t.f];
-  const T* L = arena + f.off;
-  ACC* xs = scratch + scr_off[t.f] * nrhs;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
-  for (int e = tid; e < bw * nrhs; e += blockDim.x) {
-    int k = e % bw, r = e / bw;
-    ys[k][r] = xs[(int64_t)r * f.m + c0 + k];
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+      if (16 * h + q < MAXR) ysh[i][16 * h + q] = acc[q];
   }
   __syncthreads();
   const int i = t.r0 + tid;
   if (i >= f.m) return;
+  if (i < c1) {
+    if (i >= c0) {
+      ACC* ysl = a.ys + a.scr_off[t.f] * nrhs;
+      for (int r = 0; r < nrhs; ++r) ysl[(int64_t)r * f.m + i] = ysh[i - c0][r];
+    }
+    return;
+  }
+  // this row's 64 entries of the block column, all loads in flight together
+  ACC lr[LB];
+#pragma unroll
+  for (int k = 0; k < LB; ++k) lr[k] = (k < bw) ? (ACC)L[(int64_t)(c0 + k) * f.ld + i] : ACC(0);
   for (int r0 = 0; r0 < nrhs; r0 += 16) {
     ACC acc[16];
 #pragma unroll
     for (int q = 0; q < 16; ++q) acc[q] = ACC(0);
-    for (int k = 0; k < bw; ++k) {
-      ACC l = (ACC)L[(int64_t)(c0 + k) * f.ld + i];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) acc[q] += l * ys[k][min(r0 + q, MAXR - 1)];
-    }
+    for (int k = 0; k < LB; ++k)
+#pragma unroll
+      for (int q = 0; q < 16; ++q) acc[q] += lr[k] * ysh[k][min(r0 + q, MAXR - 1)];
 #pragma unroll
     for (int q = 0; q < 16; ++q)
       if (r0 + q < nrhs) xs[(int64_t)(r0 + q) * f.m + i] -= acc[q];
   }
 }
 
-// rows [r0, r0+128) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r)
 template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_lbwd_red(const T* __restrict__ arena,
-                                                  const FrontDesc* __restrict__ fr,
-                                                  const LTask* __restrict__ tasks, int nrhs,
-                                                  const ACC* __restrict__ scratch,
-                                                  const int64_t* __restrict__ scr_off,
-                                                  ACC* __restrict__ tt) {
+__global__ void __launch_bounds__(256) k_lbwd_step(const LTask* __restrict__ tasks,
+                                                   LsArgs<T, ACC> a) {
   constexpr int SR = 32;  // rows per sub-tile
   __shared__ ACC Lt[SR][LB + 1];
   __shared__ ACC xt[SR][MAXR + 1];
+  __shared__ bool last;
   const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = fr[t.f];
-  const T* L = arena + f.off;
-  const ACC* xs = scratch + scr_off[t.f] * nrhs;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  const FrontDesc f = a.fr[t.f];
+  const T* L = a.arena + f.off;
+  const int nrhs = a.nrhs, c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  ACC* xs = a.scratch + a.scr_off[t.f] * nrhs;
+  ACC* tf = a.tt + (int64_t)t.f * LB * MAXR;
   const int k = tid % LB, g = tid / LB;  // 4 groups share the right-hand sides
   ACC acc[MAXR / 4];
 #pragma unroll
@@ -409,65 +422,48 @@ __global__ void __launch_bounds__(256) k_lbwd_red(const T* __restrict__ arena,
     for (int q = 0; q < MAXR / 4; ++q) {
       int r = g + 4 * q;
       if (r < nrhs) {
-        ACC a = acc[q];
-        for (int i = 0; i < SR; ++i) a += Lt[i][k] * xt[i][r];
-        acc[q] = a;
+        ACC s = acc[q];
+        for (int i = 0; i < SR; ++i) s += Lt[i][k] * xt[i][r];
+        acc[q] = s;
       }
     }
     __syncthreads();
   }
-  if (k < bw)
+  if (t.r0 < f.m && k < bw)
 #pragma unroll
     for (int q = 0; q < MAXR / 4; ++q) {
       int r = g + 4 * q;
-      if (r < nrhs) aadd(&tt[((int64_t)t.f * LB + k) * MAXR + r], acc[q]);
+      if (r < nrhs) aadd(&tf[k * MAXR + r], acc[q]);
     }
-}
-
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_lbwd_diag(const T* __restrict__ arena,
-                                                   const FrontDesc* __restrict__ fr,
-                                                   const LTask* __restrict__ tasks, int nrhs,
-                                                   ACC* __restrict__ scratch,
-                                                   const int64_t* __restrict__ scr_off,
-                                                   ACC* __restrict__ tt, bool unit) {
-  __shared__ ACC Ls[LB][LB + 1];  // Ls[j][i] = L(c0+i, c0+j)
-  const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = fr[t.f];
-  const T* L = arena + f.off;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int idx = tid; idx < bw * bw; idx += blockDim.x) {
-    int i = idx % bw, j = idx / bw;
-    Ls[j][i] = (i >= j) ? (ACC)L[(int64_t)(c0 + j) * f.ld + c0 + i] : ACC(0);
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) last = atomicAdd(&a.cnt[t.f], 1u) == (unsigned)(t.ntiles - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // z_b = L_bb^-T (x_b - tt): z(k) = sum_i Linv(i, k) v(i)
+  const T* Li = a.inv + a.inv_off[t.f] + (int64_t)(c0 / LB) * LB * LB;
+  __shared__ ACC vb[LB][MAXR + 1];
+  for (int e = tid; e < LB * nrhs; e += blockDim.x) {
+    int kk = e % LB, r = e / LB;
+    vb[kk][r] = (kk < bw) ? xs[(int64_t)r * f.m + c0 + kk] - __ldcg(&tf[kk * MAXR + r]) : ACC(0);
   }
   __syncthreads();
-  ACC* xs = scratch + scr_off[t.f] * nrhs;
-  ACC* tf = tt + (int64_t)t.f * LB * MAXR;
-  for (int r = warp; r < nrhs; r += blockDim.x / 32) {
-    ACC* xr = xs + (int64_t)r * f.m + c0;
-    ACC v0 = (lane < bw) ? xr[lane] - tf[lane * MAXR + r] : ACC(0);
-    ACC v1 = (32 + lane < bw) ? xr[32 + lane] - tf[(32 + lane) * MAXR + r] : ACC(0);
-    for (int kk = bw - 1; kk >= 0; --kk) {
-      if (!unit) {
-        if (kk < 32) {
-          if (lane == kk) v0 = v0 / Ls[kk][kk];
-        } else if (lane == kk - 32) {
-          v1 = v1 / Ls[kk][kk];
-        }
+  // warp per column kk of the inverse (coalesced), lanes over its 64 rows
+  {
+    const int lane = tid & 31, warp = tid >> 5;
+    for (int kk = warp; kk < bw; kk += blockDim.x / 32) {
+      const ACC l0 = (ACC)Li[(int64_t)kk * LB + lane];
+      const ACC l1 = (ACC)Li[(int64_t)kk * LB + 32 + lane];
+      for (int r = 0; r < nrhs; ++r) {
+        ACC z = l0 * vb[lane][r] + l1 * vb[32 + lane][r];
+        for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
+        if (lane == 0) xs[(int64_t)r * f.m + c0 + kk] = z;
       }
-      ACC zk = __shfl_sync(0xffffffffu, kk < 32 ? v0 : v1, kk & 31);
-      if (lane < kk) v0 -= Ls[lane][kk] * zk;
-      if (32 + lane < kk) v1 -= Ls[32 + lane][kk] * zk;
-    }
-    if (lane < bw) {
-      xr[lane] = v0;
-      tf[lane * MAXR + r] = ACC(0);
-    }
-    if (32 + lane < bw) {
-      xr[32 + lane] = v1;
-      tf[(32 + lane) * MAXR + r] = ACC(0);
     }
   }
+  for (int e = tid; e < LB * MAXR; e += blockDim.x) tf[e] = ACC(0);
+  if (tid == 0) a.cnt[t.f] = 0u;
 }
 
 inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
@@ -549,44 +545,42 @@ void launch_axpy_inplace(double* x, int ldx, const double* d, int n, int nrhs, c
 }
 
 template <typename T, typename ACC>
-void launch_lsolve(int kind, const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
-                   const int* rlist, ACC* x, int n, int nrhs, ACC* scratch,
-                   const int64_t* scr_off, ACC* tt, bool unit, cudaStream_t s) {
+void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cudaStream_t s) {
   if (ntask <= 0) return;
-  if (nrhs > MAXR) throw CudaError("solve: more than 32 right-hand sides per launch");
+  if (a.nrhs > MAXR) throw CudaError("solve: more than 32 right-hand sides per launch");
   switch (kind) {
     case LS_GATHER_FWD:
     case LS_GATHER_BWD:
-      k_lgather<ACC><<<ntask, 256, 0, s>>>(fr, tasks, rlist, x, n, nrhs, scratch, scr_off,
-                                           kind == LS_GATHER_FWD);
+      k_lgather<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_GATHER_FWD);
       break;
     case LS_SCATTER_FWD:
     case LS_SCATTER_BWD:
-      k_lscatter<ACC><<<ntask, 256, 0, s>>>(fr, tasks, rlist, x, n, nrhs, scratch, scr_off,
-                                            kind == LS_SCATTER_FWD);
+      k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
-    case LS_FWD_DIAG:
-      k_lfwd_diag<T, ACC><<<ntask, 256, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off, unit);
+    case LS_FWD_STEP:
+      k_lfwd_step<T, ACC><<<ntask, 128, 0, s>>>(tasks, a);
       break;
-    case LS_FWD_UPD:
-      k_lfwd_upd<T, ACC><<<ntask, 128, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off);
-      break;
-    case LS_BWD_RED:
-      k_lbwd_red<T, ACC><<<ntask, 256, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off, tt);
-      break;
-    case LS_BWD_DIAG:
-      k_lbwd_diag<T, ACC><<<ntask, 256, 0, s>>>(arena, fr, tasks, nrhs, scratch, scr_off, tt,
-                                                unit);
+    case LS_BWD_STEP:
+      k_lbwd_step<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
       break;
   }
 }
 
-template void launch_lsolve<float, float>(int, const float*, const FrontDesc*, const LTask*, int,
-                                          const int*, float*, int, int, float*, const int64_t*,
-                                          float*, bool, cudaStream_t);
-template void launch_lsolve<double, double>(int, const double*, const FrontDesc*, const LTask*,
-                                            int, const int*, double*, int, int, double*,
-                                            const int64_t*, double*, bool, cudaStream_t);
+template <typename T>
+void launch_inv_diag(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+                     T* inv, const int64_t* inv_off, bool unit, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_inv_diag<T><<<ntask, LB, 0, s>>>(arena, fr, tasks, inv, inv_off, unit);
+}
+
+template void launch_lsolve<float, float>(int, const LTask*, int, LsArgs<float, float>,
+                                          cudaStream_t);
+template void launch_lsolve<double, double>(int, const LTask*, int, LsArgs<double, double>,
+                                            cudaStream_t);
+template void launch_inv_diag<float>(const float*, const FrontDesc*, const LTask*, int, float*,
+                                     const int64_t*, bool, cudaStream_t);
+template void launch_inv_diag<double>(const double*, const FrontDesc*, const LTask*, int,
+                                      double*, const int64_t*, bool, cudaStream_t);
 template void launch_solve_fwd<float, float>(const float*, const FrontDesc*, int, const int*,
                                              float*, int, int, float*, const int64_t*, bool,
                                              cudaStream_t);

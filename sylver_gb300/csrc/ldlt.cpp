@@ -475,10 +475,12 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
     }
     L.scratch_rows = std::max(L.scratch_rows, acc);
   }
+  fk.clear_solve_graphs();
   put(L.sfr, L.hsfr, s);
   put(L.sscr, L.hsscr, s);
   put(L.sdoff, L.hsdoff, s);
   fk.splan.build_tasks(L.hsfr, fk.levels, s);
+  fk.splan.compute_inverses<T>(fk.arena.as<T>(), L.sfr.as<FrontDesc>(), true, s);
   SG_CUDA(cudaStreamSynchronize(s));
   return fk.flag;
 }
@@ -529,17 +531,20 @@ static void ldlt_solve_t(FKeep& fk, int job, ACC* xp, int nrhs, cudaStream_t s) 
   const int* var = L.dvar.as<int>();
   using T = ACC;  // factors and accumulation share the factor precision
   const T* A = fk.arena.as<T>();
-  for (int r0 = 0; r0 < nrhs; r0 += 32) {
-    int nr = std::min(32, nrhs - r0);
-    ACC* xr = xp + (int64_t)r0 * n;
-    if (fwd)
-      fk.splan.run<T, ACC>(true, A, fr, var, xr, n, nr, fk.scratch.as<ACC>(), sc, true, s);
-    if (diag)
-      launch_solve_diag<ACC>(fr, (int)L.hsfr.size(), var, L.dall.as<double>(), dof, xr, n, nr,
-                             s);
-    if (bwd)
-      fk.splan.run<T, ACC>(false, A, fr, var, xr, n, nr, fk.scratch.as<ACC>(), sc, true, s);
-  }
+  fk.splan.ensure_tt(sizeof(ACC), L.scratch_rows * std::min(nrhs, 32));
+  fk.replay(job, nrhs, xp, s, [&]() {
+    for (int r0 = 0; r0 < nrhs; r0 += 32) {
+      int nr = std::min(32, nrhs - r0);
+      ACC* xr = xp + (int64_t)r0 * n;
+      if (fwd)
+        fk.splan.run<T, ACC>(true, A, fr, var, xr, n, nr, fk.scratch.as<ACC>(), sc, true, s);
+      if (diag)
+        launch_solve_diag<ACC>(fr, (int)L.hsfr.size(), var, L.dall.as<double>(), dof, xr, n,
+                               nr, s);
+      if (bwd)
+        fk.splan.run<T, ACC>(false, A, fr, var, xr, n, nr, fk.scratch.as<ACC>(), sc, true, s);
+    }
+  });
 }
 
 void ldlt_solve_pivot_order(FKeep& fk, int job, float* xp, int nrhs, cudaStream_t s) {

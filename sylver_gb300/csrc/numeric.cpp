@@ -74,8 +74,14 @@ void AKeep::build_full_csr() {
     }
 }
 
+void FKeep::clear_solve_graphs() {
+  for (auto& g : sgraphs) cudaGraphExecDestroy(g.exec);
+  sgraphs.clear();
+}
+
 FKeep::~FKeep() {
   if (graph) cudaGraphExecDestroy(graph);
+  clear_solve_graphs();
 }
 
 int64_t FKeep::nnz_orig() const {
@@ -264,6 +270,7 @@ void FKeep::plan_cholesky() {
     if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
   }
 
+  ops.push_back({Op::INV, 0, 0, 0});
   // algorithmic flops of update launches: lower-triangle entries x 2K
   op_flops.assign(ops.size(), 0.0);
   for (size_t q = 0; q < ops.size(); ++q) {
@@ -312,6 +319,9 @@ void FKeep::upload_static(cudaStream_t s) {
   status.ensure(sizeof(unsigned));
   anorm.ensure(sizeof(double));
   arena.ensure((size_t)arena_elems * (precision == 1 ? sizeof(float) : sizeof(double)));
+  if (posdef)
+    splan.inv.ensure((size_t)std::max<int64_t>(splan.inv_elems, 1) *
+                     (precision == 1 ? sizeof(float) : sizeof(double)));
 }
 
 template <typename T>
@@ -343,6 +353,9 @@ void FKeep::run_ops(cudaStream_t s) {
         break;
       case Op::UPD:
         launch_update<T>(A, A, upd.as<UpdTask>() + op.a, (int)cnt, s);
+        break;
+      case Op::INV:
+        splan.compute_inverses<T>(A, dfr.as<FrontDesc>(), false, s);
         break;
     }
   }
@@ -459,6 +472,9 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
   const int LB = LSOLVE_BW;
   lv.clear();
   htasks.clear();
+  hinv.clear();
+  hinv_off.assign(hfr.size(), 0);
+  inv_elems = 0;
   max_large = 0;
   for (const Level& L : levels) {
     Lv v;
@@ -467,53 +483,84 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
     v.nsmall = 0;
     while (v.nsmall < v.nfront && !is_large(hfr[L.f0 + v.nsmall])) v.nsmall++;
     max_large = std::max(max_large, v.nfront);
-    auto add_rows_tasks = [&](std::vector<SOp>& ops, int kind, int step, bool gather) {
-      int64_t a = (int64_t)htasks.size();
-      for (int f = v.nsmall; f < v.nfront; ++f) {
-        const FrontDesc& d = hfr[L.f0 + f];
-        if (gather) {
-          for (int r0 = 0; r0 < d.m; r0 += 256) htasks.push_back({f, 0, 0, r0});
-        } else {
-          int c0 = step * LB;
-          if (c0 >= d.n) continue;
-          int bw = std::min(LB, d.n - c0);
-          if (kind == LS_FWD_DIAG || kind == LS_BWD_DIAG) {
-            htasks.push_back({f, c0, bw, 0});
-          } else {
-            for (int r0 = c0 + bw; r0 < d.m; r0 += 128) htasks.push_back({f, c0, bw, r0});
-          }
-        }
-      }
+    auto push = [&](std::vector<SOp>& ops, int kind, int64_t a) {
       int64_t b = (int64_t)htasks.size();
       if (b > a) ops.push_back({kind, a, b});
     };
     if (v.nsmall < v.nfront) {
       int maxb = 0;
-      for (int f = v.nsmall; f < v.nfront; ++f)
-        maxb = std::max(maxb, (hfr[L.f0 + f].n + LB - 1) / LB);
-      add_rows_tasks(v.fwd, LS_GATHER_FWD, 0, true);
+      for (int f = v.nsmall; f < v.nfront; ++f) {
+        const FrontDesc& d = hfr[L.f0 + f];
+        int nb = (d.n + LB - 1) / LB;
+        maxb = std::max(maxb, nb);
+        hinv_off[L.f0 + f] = inv_elems;
+        for (int b = 0; b < nb; ++b)
+          hinv.push_back({L.f0 + f, b * LB, std::min(LB, d.n - b * LB), 0, 0, 0});
+        inv_elems += (int64_t)nb * LB * LB;
+      }
+      auto rows = [&](std::vector<SOp>& ops, int kind) {
+        int64_t a = (int64_t)htasks.size();
+        for (int f = v.nsmall; f < v.nfront; ++f)
+          for (int r0 = 0; r0 < hfr[L.f0 + f].m; r0 += 256) htasks.push_back({f, 0, 0, r0, 0, 0});
+        push(ops, kind, a);
+      };
+      rows(v.fwd, LS_GATHER_FWD);
       for (int b = 0; b < maxb; ++b) {
-        add_rows_tasks(v.fwd, LS_FWD_DIAG, b, false);
-        add_rows_tasks(v.fwd, LS_FWD_UPD, b, false);
+        int64_t a = (int64_t)htasks.size();
+        for (int f = v.nsmall; f < v.nfront; ++f) {
+          const FrontDesc& d = hfr[L.f0 + f];
+          int c0 = b * LB;
+          if (c0 >= d.n) continue;
+          int bw = std::min(LB, d.n - c0);
+          for (int r0 = c0; r0 < d.m; r0 += 128) htasks.push_back({f, c0, bw, r0, 0, 0});
+        }
+        push(v.fwd, LS_FWD_STEP, a);
       }
-      add_rows_tasks(v.fwd, LS_SCATTER_FWD, 0, true);
-      add_rows_tasks(v.bwd, LS_GATHER_BWD, 0, true);
+      rows(v.fwd, LS_SCATTER_FWD);
+      rows(v.bwd, LS_GATHER_BWD);
       for (int b = maxb - 1; b >= 0; --b) {
-        add_rows_tasks(v.bwd, LS_BWD_RED, b, false);
-        add_rows_tasks(v.bwd, LS_BWD_DIAG, b, false);
+        int64_t a = (int64_t)htasks.size();
+        for (int f = v.nsmall; f < v.nfront; ++f) {
+          const FrontDesc& d = hfr[L.f0 + f];
+          int c0 = b * LB;
+          if (c0 >= d.n) continue;
+          int bw = std::min(LB, d.n - c0), c1 = c0 + bw;
+          int nt = std::max(1, (d.m - c1 + 127) / 128);
+          for (int q = 0; q < nt; ++q) htasks.push_back({f, c0, bw, c1 + q * 128, nt, 0});
+        }
+        push(v.bwd, LS_BWD_STEP, a);
       }
-      add_rows_tasks(v.bwd, LS_SCATTER_BWD, 0, true);
+      rows(v.bwd, LS_SCATTER_BWD);
     }
     lv.push_back(std::move(v));
   }
   tasks.upload(htasks, s);
+  invt.upload(hinv, s);
+  inv_off.upload(hinv_off, s);
+  cnt.ensure((size_t)std::max(max_large, 1) * sizeof(unsigned));
+  SG_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes, s));
+}
+
+template <typename T>
+void SolvePlan::compute_inverses(const T* arena, const FrontDesc* dfr, bool unit, cudaStream_t s) {
+  inv.ensure((size_t)std::max<int64_t>(inv_elems, 1) * sizeof(T));
+  launch_inv_diag<T>(arena, dfr, invt.as<LTask>(), (int)hinv.size(), inv.as<T>(),
+                     inv_off.as<int64_t>(), unit, s);
+}
+template void SolvePlan::compute_inverses<float>(const float*, const FrontDesc*, bool,
+                                                 cudaStream_t);
+template void SolvePlan::compute_inverses<double>(const double*, const FrontDesc*, bool,
+                                                  cudaStream_t);
+
+void SolvePlan::ensure_tt(size_t elem, int64_t scratch_elems) {
+  tt.ensure((size_t)std::max(max_large, 1) * LSOLVE_BW * 32 * elem);
+  ys.ensure((size_t)std::max<int64_t>(scratch_elems, 1) * elem);
 }
 
 template <typename T, typename ACC>
 void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* rlist, ACC* x,
                     int n, int nrhs, ACC* scratch, const int64_t* dscr, bool unit,
                     cudaStream_t s) {
-  tt.ensure((size_t)std::max(max_large, 1) * LSOLVE_BW * 32 * sizeof(ACC));
   auto level = [&](const Lv& v) {
     const FrontDesc* fr = dfr + v.f0;
     const int64_t* sc = dscr + v.f0;
@@ -523,13 +570,10 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
       else launch_solve_bwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc, unit,
                                     s);
     }
-    const std::vector<SOp>& ops = fwd ? v.fwd : v.bwd;
-    if (!ops.empty() && !fwd)
-      SG_CUDA(cudaMemsetAsync(tt.p, 0, (size_t)v.nfront * LSOLVE_BW * 32 * sizeof(ACC), s));
-    for (const SOp& op : ops)
-      launch_lsolve<T, ACC>(op.kind, arena, fr, tasks.as<LTask>() + op.a,
-                            (int)(op.b - op.a), rlist, x, n, nrhs, scratch, sc, tt.as<ACC>(),
-                            unit, s);
+    LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),
+                     inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), cnt.as<unsigned>()};
+    for (const SOp& op : fwd ? v.fwd : v.bwd)
+      launch_lsolve<T, ACC>(op.kind, tasks.as<LTask>() + op.a, (int)(op.b - op.a), a, s);
   };
   if (fwd)
     for (const Lv& v : lv) level(v);
@@ -553,14 +597,17 @@ void FKeep::solve_pivot_order(int job, void* xpv, int nrhs, cudaStream_t s) {
   scratch.ensure(std::max<int64_t>(scratch_rows * std::min(nrhs, 32), 1) * sizeof(ACC));
   bool fwd = job == 0 || job == 1;
   bool bwd = job == 0 || job == 3 || job == 4;
-  for (int r0 = 0; r0 < nrhs; r0 += 32) {
-    int nr = std::min(32, nrhs - r0);
-    ACC* xr = xpd + (int64_t)r0 * n;
-    if (fwd) splan.run<T, ACC>(true, A, dfr.as<FrontDesc>(), rlist0.as<int>(), xr, n, nr,
-                               scratch.as<ACC>(), dscr.as<int64_t>(), !posdef, s);
-    if (bwd) splan.run<T, ACC>(false, A, dfr.as<FrontDesc>(), rlist0.as<int>(), xr, n, nr,
-                               scratch.as<ACC>(), dscr.as<int64_t>(), !posdef, s);
-  }
+  splan.ensure_tt(sizeof(ACC), scratch_rows * std::min(nrhs, 32));
+  replay(job, nrhs, xpd, s, [&]() {
+    for (int r0 = 0; r0 < nrhs; r0 += 32) {
+      int nr = std::min(32, nrhs - r0);
+      ACC* xr = xpd + (int64_t)r0 * n;
+      if (fwd) splan.run<T, ACC>(true, A, dfr.as<FrontDesc>(), rlist0.as<int>(), xr, n, nr,
+                                 scratch.as<ACC>(), dscr.as<int64_t>(), !posdef, s);
+      if (bwd) splan.run<T, ACC>(false, A, dfr.as<FrontDesc>(), rlist0.as<int>(), xr, n, nr,
+                                 scratch.as<ACC>(), dscr.as<int64_t>(), !posdef, s);
+    }
+  });
 }
 
 int FKeep::solve_raw(int job, int nrhs, double* x, int ldx, cudaStream_t s) {

@@ -73,7 +73,7 @@ struct AKeep {
 
 // One kernel launch of the factor schedule.
 struct Op {
-  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG } kind;
+  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV } kind;
   int64_t a = 0, b = 0;  // task range [a, b)
   int aux = 0;           // SMALL: max front rows in the launch
 };
@@ -96,8 +96,14 @@ struct SolvePlan {
   };
   std::vector<Lv> lv;
   std::vector<LTask> htasks;
-  DevMem tasks, tt;
+  std::vector<LTask> hinv;       // diagonal blocks to invert (f = level-ordered index)
+  std::vector<int64_t> hinv_off; // per level-ordered front: offset of its inverses
+  int64_t inv_elems = 0;
+  DevMem tasks, tt, cnt, ys, inv, invt, inv_off;
   int max_large = 0;
+  // Invert every diagonal block of the large fronts (after a factorization).
+  template <typename T>
+  void compute_inverses(const T* arena, const FrontDesc* dfr, bool unit, cudaStream_t s);
   // Reorder each level small-first (perm[k] = old position of new k) and
   // build the task lists; hfr must already be in that order on entry to
   // build_tasks.
@@ -105,6 +111,7 @@ struct SolvePlan {
                                       const std::vector<Level>& levels);
   void build_tasks(const std::vector<FrontDesc>& hfr, const std::vector<Level>& levels,
                    cudaStream_t s);
+  void ensure_tt(size_t elem, int64_t scratch_elems);
   template <typename T, typename ACC>
   void run(bool fwd, const T* arena, const FrontDesc* dfr, const int* rlist, ACC* x, int n,
            int nrhs, ACC* scratch, const int64_t* dscr, bool unit, cudaStream_t s);
@@ -159,6 +166,34 @@ struct FKeep {
   // LDL^T state (ldlt.cpp)
   std::shared_ptr<struct LdltState> ldlt;
   SolvePlan splan;
+
+  // captured solve sweeps, keyed by job, right-hand sides and buffers
+  struct SolveGraph {
+    int job, nrhs;
+    const void *x, *scratch, *tt;
+    cudaGraphExec_t exec;
+  };
+  std::vector<SolveGraph> sgraphs;
+  void clear_solve_graphs();
+  // Run `body` (a launch sequence on stream s) through a cached graph.
+  template <typename F>
+  void replay(int job, int nrhs, const void* x, cudaStream_t s, F&& body) {
+    for (auto& g : sgraphs)
+      if (g.job == job && g.nrhs == nrhs && g.x == x && g.scratch == scratch.p &&
+          g.tt == splan.tt.p) {
+        SG_CUDA(cudaGraphLaunch(g.exec, s));
+        return;
+      }
+    cudaGraph_t gr;
+    SG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    body();
+    SG_CUDA(cudaStreamEndCapture(s, &gr));
+    cudaGraphExec_t ex;
+    SG_CUDA(cudaGraphInstantiate(&ex, gr, 0));
+    cudaGraphDestroy(gr);
+    sgraphs.push_back({job, nrhs, x, scratch.p, splan.tt.p, ex});
+    SG_CUDA(cudaGraphLaunch(ex, s));
+  }
 
   ~FKeep();
   void plan_cholesky();
