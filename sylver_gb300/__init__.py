@@ -77,6 +77,7 @@ EXPORTS = (
     "spldlt_solve_device", "sylver_gb300_solve_stats", "sylver_gb300_akeep_sizes",
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
+    "sylver_gb300_tc_selfcheck",
 )
 
 
@@ -118,6 +119,7 @@ def load(path: str | None = None):
                                             ctypes.POINTER(D)]),
         "sylver_gb300_stream": (P, []),
         "sylver_gb300_profile_factor": (I, [P, P, P, P, P]),
+        "sylver_gb300_tc_selfcheck": (I, [I, I, ctypes.POINTER(D)]),
         "spldlt_create_symbolic_tree": (P, [P, I, I, P, P, P, P, P, P, I, P, P, P, P]),
         "spldlt_destroy_symbolic_tree": (None, [P]),
         "spldlt_create_numeric_tree_dbl": (P, [B, P, P, P, P, P, P, P]),
@@ -244,11 +246,11 @@ class Factor:
         return dict(kernel_launches=nl.value, nlevels=lv.value, factor_ms=ms.value)
 
     KINDS = ("memset", "init_a", "extend_add", "small_fronts", "panel_trsm", "update",
-             "diag_chol", "other")
+             "diag_chol", "diag_inverse", "panel_split", "update_tc", "other10", "other11")
 
     def profile(self, val_dev_ptr=None):
         """Per-kernel-kind timing of one extra factorization (no graph)."""
-        ms = np.zeros(8); nl = np.zeros(8, dtype=np.int64); fl = np.zeros(8)
+        ms = np.zeros(12); nl = np.zeros(12, dtype=np.int64); fl = np.zeros(12)
         rc = load().sylver_gb300_profile_factor(self.fkeep, val_dev_ptr, _p(ms), _p(nl), _p(fl))
         if rc != 0:
             raise RuntimeError(f"profile failed: {rc}")

@@ -28,6 +28,7 @@ enum : unsigned {
   ST_SINGULAR = 4u,       // LDL^T zero pivot with action = false
   ST_OVERFLOW = 8u,       // a front outgrew its planned storage
   ST_BAD_INDEX = 16u,     // an index map pointed outside its front
+  ST_TIMEOUT = 32u,       // a bounded wait inside a kernel gave up
 };
 
 // ---------------------------------------------------------------------------

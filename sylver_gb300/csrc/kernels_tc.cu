@@ -1,0 +1,337 @@
+// Tensor-core Schur-complement update for FP32 fronts: C -= A B^T on the
+// 5th-generation tensor cores (tcgen05, kind::tf32) with the accumulator in
+// tensor memory and operands staged by TMA.
+//
+// Accuracy: 3xTF32.  Each operand is split into hi = rna_tf32(x) and
+// lo = x - hi (both FP32 containers), and C -= Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T
+// accumulates in FP32 -- close to an FP32 product, which keeps iterative
+// refinement convergence as for SIMT FP32 factors.
+//
+// Operand layout: TF32 MMAs read K-major shared-memory tiles, so A and B come
+// from a transposed copy of the contribution rows of L ("panel rows", one row
+// per front row, k contiguous, zero-padded to a multiple of 32) stacked for all
+// fronts of a level in one buffer with a fixed pitch; one 2D tensor map per
+// level covers it.  TMA boxes are 32 (k) x 128 (rows) FP32 with 128-byte
+// swizzle, matching the tcgen05 K-major SWIZZLE_128B canonical layout.
+//
+// One CTA computes one 128 x 128 tile (4 warps):
+//   warp 0 lane 0 : TMA producer over a 3-stage ring (full/empty mbarriers),
+//   warp 1 lane 0 : MMA issuer (12 MMAs per 32-wide k chunk), tcgen05.commit
+//                   releases a stage and finally signals the accumulator,
+//   all 4 warps   : epilogue, tcgen05.ld of their 32 TMEM lanes, C -= acc.
+// Every mbarrier wait is bounded: on timeout the CTA records an error bit,
+// skips the epilogue, waits (bounded) for its own copies and frees TMEM.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "device.hpp"
+#include "tc.hpp"
+
+namespace sylver_gb300 {
+
+namespace {
+
+constexpr int TC_M = 128, TC_N = 128, TC_KC = 32;  // tile rows, cols, k per stage
+constexpr int TC_STAGES = 3;
+constexpr int TILE_BYTES = TC_M * TC_KC * 4;        // 16 KiB per operand tile
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;         // Ahi, Alo, Bhi, Blo
+constexpr long WAIT_LIMIT = 1L << 24;               // try_wait polls before giving up
+
+__device__ __forceinline__ uint32_t su32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* b, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// bounded wait (poll count and one second of wall time); false, with the
+// error bit set, on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t* b, uint32_t parity, unsigned* err) {
+  const uint64_t t0 = global_ns();
+  for (long it = 0; it < WAIT_LIMIT; ++it) {
+    if (mbar_try(b, parity)) return true;
+    if ((it & 255) == 255 && global_ns() - t0 > 1000000000ull) break;
+  }
+  atomicOr(err, ST_TIMEOUT);
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(su32(dst)),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(su32(bar))
+      : "memory");
+}
+
+// K-major, 128-byte swizzle shared-memory matrix descriptor (tcgen05 format:
+// start >> 4 in bits 0-13, leading byte offset >> 4 in 16-29 (unused for a
+// swizzled K-major tile), stride byte offset >> 4 in 32-45 = 1024 B between
+// 8-row groups, version 1 in bits 46-47, swizzle mode 2 (128 B) in 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+// instruction descriptor: D f32, A/B tf32, both K-major, N = 128, M = 128
+__host__ __device__ constexpr uint32_t tf32_idesc() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+         ((uint32_t)(TC_M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t ad, uint64_t bd,
+                                         uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          su32(bar))
+      : "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[N]);
+
+template <>
+__device__ __forceinline__ void tmem_ld32<32>(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]),
+        "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]),
+        "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// ---------------------------------------------------------------------------
+
+__global__ void __launch_bounds__(128, 1)
+    k_update_tc(const __grid_constant__ CUtensorMap map_hi,
+                const __grid_constant__ CUtensorMap map_lo, float* __restrict__ arena,
+                const TcTask* __restrict__ tasks, unsigned* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // 1 KiB alignment for the swizzled tiles
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int failed;
+
+  const TcTask t = tasks[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nk = t.nk;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     su32(&tmem_slot)),
+                 "r"(TC_N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+
+  int issued = 0;  // TMA chunks issued (producer)
+  if (warp == 0 && lane == 0) {
+    for (int kc = 0; kc < nk; ++kc) {
+      const int s = kc % TC_STAGES;
+      if (kc >= TC_STAGES && !mbar_wait(&empty[s], ((kc / TC_STAGES) - 1) & 1, err)) {
+        failed = 1;
+        break;
+      }
+      unsigned char* st = smem + s * STAGE_BYTES;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      const int x = kc * TC_KC;
+      tma_load_2d(st + 0 * TILE_BYTES, &map_hi, x, t.a_row, &full[s]);
+      tma_load_2d(st + 1 * TILE_BYTES, &map_lo, x, t.a_row, &full[s]);
+      tma_load_2d(st + 2 * TILE_BYTES, &map_hi, x, t.b_row, &full[s]);
+      tma_load_2d(st + 3 * TILE_BYTES, &map_lo, x, t.b_row, &full[s]);
+      issued = kc + 1;
+    }
+  } else if (warp == 1 && lane == 0) {
+    const uint32_t idesc = tf32_idesc();
+    int kc = 0;
+    for (; kc < nk; ++kc) {
+      const int s = kc % TC_STAGES;
+      if (!mbar_wait(&full[s], (kc / TC_STAGES) & 1, err)) {
+        failed = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      unsigned char* st = smem + s * STAGE_BYTES;
+      const uint64_t ahi = sw128_desc(su32(st + 0 * TILE_BYTES));
+      const uint64_t alo = sw128_desc(su32(st + 1 * TILE_BYTES));
+      const uint64_t bhi = sw128_desc(su32(st + 2 * TILE_BYTES));
+      const uint64_t blo = sw128_desc(su32(st + 3 * TILE_BYTES));
+#pragma unroll
+      for (int kk = 0; kk < TC_KC / 8; ++kk) {
+        // 8 tf32 = 32 bytes further along k inside the swizzled row
+        const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+        const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
+        mma_tf32(tmem, ahi + adv, bhi + adv, idesc, acc0);
+        mma_tf32(tmem, ahi + adv, blo + adv, idesc, 1u);
+        mma_tf32(tmem, alo + adv, bhi + adv, idesc, 1u);
+      }
+      mma_commit(&empty[s]);
+    }
+    mma_commit(&done);
+  }
+  __syncthreads();
+  // the accumulator is complete (or the MMAs issued so far have drained)
+  // once `done` fires; wait for it even after a failure, before TMEM is freed
+  const bool drained = mbar_wait(&done, 0, err);
+  const bool ok = drained && !failed;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int row = t.row0 + warp * 32 + lane;
+    float* C = arena + t.c_off;
+#pragma unroll 1
+    for (int c = 0; c < TC_N / 32; ++c) {
+      float v[32];
+      tmem_ld32<32>(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
+      if (row < t.rowEnd) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) {
+          const int col = t.col0 + c * 32 + j;
+          if (col < t.colEnd && col <= row) C[(int64_t)col * t.ldc + row] -= v[j];
+        }
+      }
+    }
+  }
+  // copies still in flight after a timeout: wait for them (bounded) before
+  // the shared memory they target goes away
+  if (!ok && warp == 0 && lane == 0) {
+    for (int kc = 0; kc < issued; ++kc) mbar_wait(&full[kc % TC_STAGES], (kc / TC_STAGES) & 1, err);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N)
+                 : "memory");
+}
+
+// Transposed, hi/lo-split copy of rows [n, m) x cols [0, K) of one front into
+// the stacked panel buffer: out[(base + i - n) * pitch + k]; columns
+// [K, pitch) are zero.  One thread per (row, k) pair, k fastest in a warp for
+// coalesced writes; reads are strided (one column per k) but each front row
+// block is read once.
+__global__ void k_split_t(const float* __restrict__ arena, const TcSplit* __restrict__ sp,
+                          float* __restrict__ hi, float* __restrict__ lo, int pitch) {
+  const TcSplit t = sp[blockIdx.y];
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int rows = t.m - t.n;
+  if (e >= (int64_t)rows * pitch) return;
+  const int i = (int)(e / pitch), k = (int)(e % pitch);
+  float v = 0.f;
+  if (k < t.K) v = arena[t.off + (int64_t)k * t.ld + t.n + i];
+  uint32_t h;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+  const float fh = __uint_as_float(h);
+  const int64_t o = (int64_t)(t.base + i) * pitch + k;
+  hi[o] = fh;
+  lo[o] = v - fh;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    SG_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p) throw CudaError("cuTensorMapEncodeTiled missing");
+    fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+}  // namespace
+
+size_t tc_smem_bytes() { return (size_t)TC_STAGES * STAGE_BYTES + 1024; }
+
+void prepare_tc_kernels() {
+  SG_CUDA(cudaFuncSetAttribute(k_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)tc_smem_bytes()));
+}
+
+void make_panel_map(CUtensorMap* map, const float* base, int64_t rows, int pitch) {
+  // 2D: x = k (contiguous, pitch elements), y = stacked panel row
+  cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)std::max<int64_t>(rows, 1)};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)TC_KC, (cuuint32_t)TC_M};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides,
+                           box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw CudaError("cuTensorMapEncodeTiled failed");
+}
+
+void launch_split_t(const float* arena, const TcSplit* sp, int nsplit, int64_t max_elems,
+                    float* hi, float* lo, int pitch, cudaStream_t s) {
+  if (nsplit <= 0 || max_elems <= 0) return;
+  dim3 grid((unsigned)((max_elems + 255) / 256), (unsigned)nsplit);
+  k_split_t<<<grid, 256, 0, s>>>(arena, sp, hi, lo, pitch);
+}
+
+void launch_update_tc(const CUtensorMap& hi, const CUtensorMap& lo, float* arena,
+                      const TcTask* t, int ntask, unsigned* err, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_update_tc<<<ntask, 128, tc_smem_bytes(), s>>>(hi, lo, arena, t, err);
+}
+
+}  // namespace sylver_gb300

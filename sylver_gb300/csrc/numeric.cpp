@@ -13,6 +13,7 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 
 namespace sylver_gb300 {
 
@@ -40,6 +41,7 @@ bool Runtime::init() {
   try {
     prepare_factor_kernels<float>();
     prepare_factor_kernels<double>();
+    prepare_tc_kernels();
   } catch (const std::exception& ex) {
     err = ex.what();
     return false;
@@ -189,6 +191,10 @@ void FKeep::plan_cholesky() {
   std::vector<SmallTask> smalls;
   std::vector<PanelTask> panels, diags;
   std::vector<UpdTask> upds;
+  std::vector<TcSplit> tcs;
+  std::vector<TcTask> tct;
+  std::vector<double> tc_flops;
+  tclev.clear();
   std::vector<int> pos(st.n, -1);
   ops.clear();
   ops.push_back({Op::MEMSET, 0, 0, 0});
@@ -257,23 +263,59 @@ void FKeep::plan_cholesky() {
       if ((int64_t)panels.size() > p0) ops.push_back({Op::PANEL, p0, (int64_t)panels.size(), 0});
       if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
     }
-    // contribution blocks: one Schur-complement update with K = n
+    // contribution blocks: one Schur-complement update with K = n, on the
+    // tensor cores (FP32, 3xTF32) for blocks of at least 64 rows
     int64_t u0 = (int64_t)upds.size();
+    std::vector<int> tcf;
     for (int s : large) {
       int m = st.nrow[s], n = st.ncol[s];
       if (m <= n) continue;
+      if (f32 && use_tc && m - n >= 64) {
+        tcf.push_back(s);
+        continue;
+      }
       for (int cj = 0; n + cj * TM < m; ++cj)
         for (int ri = cj; n + ri * TM < m; ++ri)
           upds.push_back({off[s], off[s], off[s], ld[s], ld[s], ld[s], n + ri * TM,
                           n + cj * TM, m, m, 0, n, 0});
     }
     if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
+    if (!tcf.empty()) {
+      int pitch = 0;
+      int64_t rows = 0, mx = 0;
+      for (int s : tcf) pitch = std::max(pitch, (st.ncol[s] + 31) / 32 * 32);
+      int64_t sp0 = (int64_t)tcs.size(), tk0 = (int64_t)tct.size();
+      for (int s : tcf) {
+        int m = st.nrow[s], n = st.ncol[s];
+        tcs.push_back({off[s], ld[s], m, n, n, (int)rows, 0});
+        for (int cj = 0; cj * 128 < m - n; ++cj)
+          for (int ri = cj; ri * 128 < m - n; ++ri)
+            tct.push_back({off[s], ld[s], n + ri * 128, n + cj * 128, m, m,
+                           (int)rows + ri * 128, (int)rows + cj * 128, (n + 31) / 32});
+        mx = std::max(mx, (int64_t)(m - n) * pitch);
+        rows += m - n;
+      }
+      int lvl = (int)tclev.size();
+      tclev.push_back({pitch, rows, mx});
+      double fl = 0.0;  // lower triangle (diagonal included) x 2K
+      for (int s : tcf) {
+        double mc = st.nrow[s] - st.ncol[s];
+        fl += mc * (mc + 1.0) * st.ncol[s];
+      }
+      tc_flops.push_back(fl);
+      ops.push_back({Op::SPLIT, sp0, (int64_t)tcs.size(), lvl});
+      ops.push_back({Op::TCUPD, tk0, (int64_t)tct.size(), lvl});
+    }
   }
 
   ops.push_back({Op::INV, 0, 0, 0});
   // algorithmic flops of update launches: lower-triangle entries x 2K
   op_flops.assign(ops.size(), 0.0);
   for (size_t q = 0; q < ops.size(); ++q) {
+    if (ops[q].kind == Op::TCUPD) {
+      op_flops[q] = tc_flops[ops[q].aux];
+      continue;
+    }
     if (ops[q].kind != Op::UPD) continue;
     double f = 0.0;
     for (int64_t k = ops[q].a; k < ops[q].b; ++k) {
@@ -294,6 +336,8 @@ void FKeep::plan_cholesky() {
   small.upload(smalls, s);
   panel.upload(panels, s);
   diagt.upload(diags, s);
+  tcsplit.upload(tcs, s);
+  tctask.upload(tct, s);
   upd.upload(upds, s);
   dfr.upload(hfr, s);
   dscr.upload(hscr, s);
@@ -322,6 +366,19 @@ void FKeep::upload_static(cudaStream_t s) {
   if (posdef)
     splan.inv.ensure((size_t)std::max<int64_t>(splan.inv_elems, 1) *
                      (precision == 1 ? sizeof(float) : sizeof(double)));
+  tcerr.ensure(sizeof(unsigned));
+  if (!tclev.empty()) {
+    int64_t cap = 0;
+    for (auto& L : tclev) cap = std::max(cap, L.rows * L.pitch);
+    panel_hi.ensure((size_t)cap * sizeof(float));
+    panel_lo.ensure((size_t)cap * sizeof(float));
+    tmap_hi.resize(tclev.size());
+    tmap_lo.resize(tclev.size());
+    for (size_t l = 0; l < tclev.size(); ++l) {
+      make_panel_map(&tmap_hi[l], panel_hi.as<float>(), tclev[l].rows, tclev[l].pitch);
+      make_panel_map(&tmap_lo[l], panel_lo.as<float>(), tclev[l].rows, tclev[l].pitch);
+    }
+  }
 }
 
 template <typename T>
@@ -357,6 +414,16 @@ void FKeep::run_ops(cudaStream_t s) {
       case Op::INV:
         splan.compute_inverses<T>(A, dfr.as<FrontDesc>(), false, s);
         break;
+      case Op::SPLIT:
+        if constexpr (std::is_same<T, float>::value)
+          launch_split_t(A, tcsplit.as<TcSplit>() + op.a, (int)cnt, tclev[op.aux].max_elems,
+                         panel_hi.as<float>(), panel_lo.as<float>(), tclev[op.aux].pitch, s);
+        break;
+      case Op::TCUPD:
+        if constexpr (std::is_same<T, float>::value)
+          launch_update_tc(tmap_hi[op.aux], tmap_lo[op.aux], A, tctask.as<TcTask>() + op.a,
+                           (int)cnt, tcerr.as<unsigned>(), s);
+        break;
     }
   }
 }
@@ -372,6 +439,7 @@ int FKeep::factorize(const double* val_dev, cudaStream_t s) {
   SG_CUDA(cudaMemsetAsync(anorm.p, 0, sizeof(double), s));
   launch_rownorm_inf(frow.as<int64_t>(), faval.as<double>(), a.n, anorm.as<double>(), s);
   SG_CUDA(cudaMemsetAsync(status.p, 0, sizeof(unsigned), s));
+  SG_CUDA(cudaMemsetAsync(tcerr.p, 0, sizeof(unsigned), s));
   // the factor schedule reads val through the fkeep-owned buffer so that the
   // captured graph stays valid across calls
   if (val_dev != val.as<double>()) {
@@ -401,8 +469,9 @@ int FKeep::factorize(const double* val_dev, cudaStream_t s) {
   }
   SG_CUDA(cudaEventRecord(e1, s));
   launches = (long)ops.size() - 1;  // the memset is not a kernel
-  unsigned st = 0;
+  unsigned st = 0, tce = 0;
   SG_CUDA(cudaMemcpyAsync(&st, status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  SG_CUDA(cudaMemcpyAsync(&tce, tcerr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   SG_CUDA(cudaMemcpyAsync(&anorm_h, anorm.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   SG_CUDA(cudaStreamSynchronize(s));
   float ms = 0.f;
@@ -411,6 +480,7 @@ int FKeep::factorize(const double* val_dev, cudaStream_t s) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   flag = 0;
+  if (tce) throw CudaError("tensor-core update: a bounded wait timed out");
   if (posdef) {
     rank = (st & ST_NOT_POSDEF) ? 0 : ak->n;
     if (st & ST_NOT_POSDEF) flag = -6;
@@ -419,7 +489,7 @@ int FKeep::factorize(const double* val_dev, cudaStream_t s) {
 }
 
 int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, cudaStream_t s) {
-  for (int k = 0; k < 8; ++k) {
+  for (int k = 0; k < 12; ++k) {
     ms[k] = 0.0;
     nl[k] = 0;
     flops[k] = 0.0;

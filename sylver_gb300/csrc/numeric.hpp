@@ -15,6 +15,7 @@
 
 #include "analyse.hpp"
 #include "device.hpp"
+#include "tc.hpp"
 
 namespace sylver_gb300 {
 
@@ -73,9 +74,9 @@ struct AKeep {
 
 // One kernel launch of the factor schedule.
 struct Op {
-  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV } kind;
+  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV, SPLIT, TCUPD } kind;
   int64_t a = 0, b = 0;  // task range [a, b)
-  int aux = 0;           // SMALL: max front rows in the launch
+  int aux = 0;           // SMALL: max front rows; SPLIT/TCUPD: tensor-core level
 };
 
 struct Level {
@@ -129,6 +130,16 @@ struct FKeep {
   double small_piv = 1e-20;
   bool action = true;
   std::vector<double> scale;  // user scaling S (empty: none)
+
+  // tensor-core contribution-block updates (FP32 Cholesky)
+  bool use_tc = true;
+  struct TcLevel {
+    int pitch;
+    int64_t rows, max_elems;
+  };
+  std::vector<TcLevel> tclev;
+  std::vector<CUtensorMap> tmap_hi, tmap_lo;
+  DevMem tcsplit, tctask, panel_hi, panel_lo, tcerr;
 
   // host plan
   std::vector<int> order;            // level-ordered front indices
