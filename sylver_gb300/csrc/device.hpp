@@ -131,9 +131,11 @@ struct LTask {
   int pad;
 };
 enum LsKind {
-  LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD, LS_FWD_STEP, LS_BWD_STEP
+  LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD,
+  LS_FWD_DIAG2, LS_FWD_UPD2, LS_BWD_RED2, LS_BWD_DIAG2
 };
-constexpr int LSOLVE_BW = 64;
+constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
+constexpr int LSOLVE_BW2 = 256;  // columns per solve step
 // Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
 // explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
 // index), tt: 64 x 32 accumulators per front, cnt: one ticket counter per
@@ -152,7 +154,17 @@ struct LsArgs {
   const int64_t* inv_off;
   ACC* tt;
   unsigned* cnt;
+  const T* inv2;            // 256x256 inverses of the solve-step diagonal blocks
+  const int64_t* inv2_off;  // per front of the level
 };
+// Inverse of each 256-column diagonal block from its 64x64 inverses: task
+// (front f, c0, bw), output at inv2 + inv2_off[f] + (c0/256)*256*256.
+template <typename T>
+void prepare_solve_kernels();
+template <typename T>
+void launch_inv256(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+                   const T* inv64, const int64_t* inv_off, T* inv2, const int64_t* inv2_off,
+                   cudaStream_t s);
 template <typename T, typename ACC>
 void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cudaStream_t s);
 // Explicit inverse of each diagonal block: task (front f, c0, bw), output at

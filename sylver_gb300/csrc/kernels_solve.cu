@@ -329,141 +329,270 @@ __global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
   for (int e = j; e < LB * LB; e += LB) out[e] = Xs[e / LB][e % LB];
 }
 
+// Block steps of BW2 = 256 columns.  Each diagonal block has an explicit
+// inverse (built once per factorization from its four 64x64 inverses), so a
+// step is one parallel mat-vec on the diagonal block plus one update (forward)
+// or reduction (backward) of the rows below, spread over many small CTAs.
+constexpr int BW2 = LSOLVE_BW2;
+template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
+
+// X = inverse of the 256-column diagonal block (column-major, ld 256, lower):
+// X_jj = Inv64_j and X_ij = -Inv64_i * sum_{k=j}^{i-1} L_ik X_kj for i > j,
+// with 64x64 blocks; identity beyond bw.
+template <typename T>
+__global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
+                                                const FrontDesc* __restrict__ fr,
+                                                const LTask* __restrict__ tasks,
+                                                const T* __restrict__ inv64,
+                                                const int64_t* __restrict__ inv_off,
+                                                T* __restrict__ inv2,
+                                                const int64_t* __restrict__ inv2_off) {
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  T* As = reinterpret_cast<T*>(sm_raw);  // As[k*65 + r] = A(r, k)
+  T* Bs = As + 64 * 65;                  // Bs[c*65 + k] = B(k, c)
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const T* L = arena + f.off;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  T* X = inv2 + inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
+  const T* I64 = inv64 + inv_off[t.f] + (int64_t)(c0 / LB) * LB * LB;
+  const int nb = (bw + LB - 1) / LB;
+  for (int e = tid; e < BW2 * BW2; e += blockDim.x) X[e] = T(0);
+  __syncthreads();
+  for (int j = 0; j < 4; ++j)
+    for (int e = tid; e < LB * LB; e += blockDim.x) {
+      int i = e % LB, k = e / LB;
+      X[(int64_t)(LB * j + k) * BW2 + LB * j + i] =
+          (j < nb) ? I64[(int64_t)j * LB * LB + k * LB + i] : T(i == k ? 1 : 0);
+    }
+  __syncthreads();
+  const int r = tid % LB, cq = tid / LB;  // output row, 16-column quarter
+  for (int j = 0; j < nb; ++j)
+    for (int i = j + 1; i < nb; ++i) {
+      T acc[16];
+#pragma unroll
+      for (int q = 0; q < 16; ++q) acc[q] = T(0);
+      for (int k = j; k < i; ++k) {
+        for (int e = tid; e < LB * LB; e += blockDim.x) {
+          int rr = e % LB, kk = e / LB;
+          int grow = LB * i + rr, gcol = LB * k + kk;
+          As[kk * 65 + rr] = (grow < bw && gcol < bw) ? L[(int64_t)(c0 + gcol) * f.ld + c0 + grow] : T(0);
+          Bs[rr * 65 + kk] = X[(int64_t)(LB * j + rr) * BW2 + LB * k + kk];  // B(kk, rr) = X_kj
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < LB; ++kk) {
+          const T a = As[kk * 65 + r];
+#pragma unroll
+          for (int q = 0; q < 16; ++q) acc[q] += a * Bs[(cq * 16 + q) * 65 + kk];
+        }
+        __syncthreads();
+      }
+      // X_ij = -Inv64_i S
+#pragma unroll
+      for (int q = 0; q < 16; ++q) Bs[(cq * 16 + q) * 65 + r] = acc[q];
+      for (int e = tid; e < LB * LB; e += blockDim.x) {
+        int rr = e % LB, kk = e / LB;
+        As[kk * 65 + rr] = I64[(int64_t)i * LB * LB + kk * LB + rr];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 16; ++q) acc[q] = T(0);
+#pragma unroll 8
+      for (int kk = 0; kk < LB; ++kk) {
+        const T a = As[kk * 65 + r];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc[q] += a * Bs[(cq * 16 + q) * 65 + kk];
+      }
+#pragma unroll
+      for (int q = 0; q < 16; ++q) X[(int64_t)(LB * j + cq * 16 + q) * BW2 + LB * i + r] = -acc[q];
+      __syncthreads();
+    }
+}
+
+// y_b = X_b x_b (forward): thread (row i, half h of the columns), 512 threads
 template <typename T, typename ACC>
-__global__ void __launch_bounds__(128) k_lfwd_step(const LTask* __restrict__ tasks,
+__global__ void __launch_bounds__(512) k_fwd_diag3(const LTask* __restrict__ tasks,
                                                    LsArgs<T, ACC> a) {
-  __shared__ ACC xb[LB][MAXR + 1];
-  __shared__ ACC ysh[LB][MAXR];
+  constexpr int RG = RGn<ACC>::v;
+  __shared__ ACC xb[BW2][RG + 1];
+  __shared__ ACC part[BW2][RG + 1];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
-  const T* L = a.arena + f.off;
-  const int nrhs = a.nrhs, c0 = t.c0, bw = t.bw, c1 = c0 + bw, tid = threadIdx.x;
-  ACC* xs = a.scratch + a.scr_off[t.f] * nrhs;
-  const T* Li = a.inv + a.inv_off[t.f] + (int64_t)(c0 / LB) * LB * LB;
-  for (int e = tid; e < LB * nrhs; e += blockDim.x) {
-    int k = e % LB, r = e / LB;
-    xb[k][r] = (k < bw) ? xs[(int64_t)r * f.m + c0 + k] : ACC(0);
-  }
-  __syncthreads();
-  // y = L_bb^-1 x_b: thread (row i = tid % 64, half h = tid / 64) does 16 rhs
-  {
-    const int i = tid % LB, h = tid / LB;
-    ACC acc[16];
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, i = tid % BW2, h = tid / BW2;
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
+  const T* X = a.inv2 + a.inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
+  for (int rg = 0; rg < a.nrhs; rg += RG) {
+    const int nr = min(RG, a.nrhs - rg);
+    for (int e = tid; e < BW2 * RG; e += blockDim.x) {
+      int k = e % BW2, r = e / BW2;
+      xb[k][r] = (k < bw && r < nr) ? xs[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+    }
+    __syncthreads();
+    ACC acc[RG];
 #pragma unroll
-    for (int q = 0; q < 16; ++q) acc[q] = ACC(0);
+    for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
+    const int k0 = h * (BW2 / 2), k1 = min(k0 + BW2 / 2, i + 1);
 #pragma unroll 16
-    for (int k = 0; k < LB; ++k) {
-      const ACC l = (ACC)Li[(int64_t)k * LB + i];  // zero above the diagonal
+    for (int k = k0; k < k1; ++k) {
+      const ACC l = (ACC)X[(int64_t)k * BW2 + i];
 #pragma unroll
-      for (int q = 0; q < 16; ++q) acc[q] += l * xb[k][min(16 * h + q, MAXR - 1)];
+      for (int q = 0; q < RG; ++q) acc[q] += l * xb[k][q];
     }
+    if (h == 1)
 #pragma unroll
-    for (int q = 0; q < 16; ++q)
-      if (16 * h + q < MAXR) ysh[i][16 * h + q] = acc[q];
-  }
-  __syncthreads();
-  const int i = t.r0 + tid;
-  if (i >= f.m) return;
-  if (i < c1) {
-    if (i >= c0) {
-      ACC* ysl = a.ys + a.scr_off[t.f] * nrhs;
-      for (int r = 0; r < nrhs; ++r) ysl[(int64_t)r * f.m + i] = ysh[i - c0][r];
-    }
-    return;
-  }
-  // this row's 64 entries of the block column, all loads in flight together
-  ACC lr[LB];
+      for (int q = 0; q < RG; ++q) part[i][q] = acc[q];
+    __syncthreads();
+    if (h == 0 && i < bw)
 #pragma unroll
-  for (int k = 0; k < LB; ++k) lr[k] = (k < bw) ? (ACC)L[(int64_t)(c0 + k) * f.ld + i] : ACC(0);
-  for (int r0 = 0; r0 < nrhs; r0 += 16) {
-    ACC acc[16];
-#pragma unroll
-    for (int q = 0; q < 16; ++q) acc[q] = ACC(0);
-#pragma unroll
-    for (int k = 0; k < LB; ++k)
-#pragma unroll
-      for (int q = 0; q < 16; ++q) acc[q] += lr[k] * ysh[k][min(r0 + q, MAXR - 1)];
-#pragma unroll
-    for (int q = 0; q < 16; ++q)
-      if (r0 + q < nrhs) xs[(int64_t)(r0 + q) * f.m + i] -= acc[q];
+      for (int q = 0; q < RG; ++q)
+        if (q < nr) ysl[(int64_t)(rg + q) * f.m + c0 + i] = acc[q] + part[i][q];
+    __syncthreads();
   }
 }
 
+// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 32-column group g)
 template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_lbwd_step(const LTask* __restrict__ tasks,
-                                                   LsArgs<T, ACC> a) {
-  constexpr int SR = 32;  // rows per sub-tile
-  __shared__ ACC Lt[SR][LB + 1];
-  __shared__ ACC xt[SR][MAXR + 1];
-  __shared__ bool last;
+__global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ tasks,
+                                                  LsArgs<T, ACC> a) {
+  constexpr int RG = RGn<ACC>::v;
+  __shared__ ACC yb[BW2][RG];
+  __shared__ ACC red[8][32][RG + 1];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
-  const int nrhs = a.nrhs, c0 = t.c0, bw = t.bw, tid = threadIdx.x;
-  ACC* xs = a.scratch + a.scr_off[t.f] * nrhs;
-  ACC* tf = a.tt + (int64_t)t.f * LB * MAXR;
-  const int k = tid % LB, g = tid / LB;  // 4 groups share the right-hand sides
-  ACC acc[MAXR / 4];
-#pragma unroll
-  for (int q = 0; q < MAXR / 4; ++q) acc[q] = ACC(0);
-  const int rend = min(t.r0 + 128, f.m);
-  for (int s0 = t.r0; s0 < rend; s0 += SR) {
-    const int nr = min(SR, rend - s0);
-    for (int e = tid; e < SR * LB; e += blockDim.x) {
-      int i = e % SR, kk = e / SR;
-      Lt[i][kk] = (i < nr && kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * f.ld + s0 + i] : ACC(0);
-    }
-    for (int e = tid; e < SR * nrhs; e += blockDim.x) {
-      int i = e % SR, r = e / SR;
-      xt[i][r] = (i < nr) ? xs[(int64_t)r * f.m + s0 + i] : ACC(0);
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, rr = tid % 32, g = tid / 32;
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
+  const int i = t.r0 + rr;
+  for (int rg = 0; rg < a.nrhs; rg += RG) {
+    const int nr = min(RG, a.nrhs - rg);
+    for (int e = tid; e < BW2 * RG; e += blockDim.x) {
+      int k = e % BW2, r = e / BW2;
+      yb[k][r] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
     }
     __syncthreads();
+    ACC acc[RG];
 #pragma unroll
-    for (int q = 0; q < MAXR / 4; ++q) {
-      int r = g + 4 * q;
-      if (r < nrhs) {
+    for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
+    if (i < f.m) {
+#pragma unroll 16
+      for (int kk = 0; kk < 32; ++kk) {
+        const int k = g * 32 + kk;
+        const ACC l = (k < bw) ? (ACC)L[(int64_t)(c0 + k) * f.ld + i] : ACC(0);
+#pragma unroll
+        for (int q = 0; q < RG; ++q) acc[q] += l * yb[k][q];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RG; ++q) red[g][rr][q] = acc[q];
+    __syncthreads();
+    if (g == 0 && i < f.m) {
+#pragma unroll
+      for (int q = 0; q < RG; ++q) {
+        ACC s = ACC(0);
+#pragma unroll
+        for (int gg = 0; gg < 8; ++gg) s += red[gg][rr][q];
+        if (q < nr) xs[(int64_t)(rg + q) * f.m + i] -= s;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// rows [r0, r0+64) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ tasks,
+                                                  LsArgs<T, ACC> a) {
+  constexpr int RG = RGn<ACC>::v;
+  constexpr int SR = sizeof(ACC) == 8 ? 16 : 32;
+  __shared__ ACC Lt[SR][BW2 + 1];
+  __shared__ ACC xt[SR][RG + 1];
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  const T* L = a.arena + f.off;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  ACC* tf = a.tt + (int64_t)t.f * BW2 * MAXR;
+  const int rend = min(t.r0 + 64, f.m);
+  for (int rg = 0; rg < a.nrhs; rg += RG) {
+    const int nr = min(RG, a.nrhs - rg);
+    ACC acc[RG];
+#pragma unroll
+    for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
+    for (int s0 = t.r0; s0 < rend; s0 += SR) {
+      const int nrow = min(SR, rend - s0);
+#pragma unroll 4
+      for (int e = tid; e < SR * BW2; e += blockDim.x) {
+        int ii = e % SR, kk = e / SR;
+        Lt[ii][kk] = (ii < nrow && kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * f.ld + s0 + ii] : ACC(0);
+      }
+      for (int e = tid; e < SR * RG; e += blockDim.x) {
+        int ii = e % SR, r = e / SR;
+        xt[ii][r] = (ii < nrow && r < nr) ? xs[(int64_t)(rg + r) * f.m + s0 + ii] : ACC(0);
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int ii = 0; ii < SR; ++ii) {
+        const ACC l = Lt[ii][tid];
+#pragma unroll
+        for (int q = 0; q < RG; ++q) acc[q] += l * xt[ii][q];
+      }
+      __syncthreads();
+    }
+    if (tid < bw)
+#pragma unroll
+      for (int q = 0; q < RG; ++q)
+        if (q < nr) aadd(&tf[tid * MAXR + rg + q], acc[q]);
+  }
+}
+
+// z_b = X_b^T (x_b - tt): warp w computes columns k = w, w+16, ...; lanes
+// run down the column of X (coalesced) and reduce with shuffles
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(512) k_bwd_diag3(const LTask* __restrict__ tasks,
+                                                   LsArgs<T, ACC> a) {
+  constexpr int RG = RGn<ACC>::v;
+  __shared__ ACC vb[BW2][RG + 1];
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  ACC* tf = a.tt + (int64_t)t.f * BW2 * MAXR;
+  const T* X = a.inv2 + a.inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
+  for (int rg = 0; rg < a.nrhs; rg += RG) {
+    const int nr = min(RG, a.nrhs - rg);
+    __syncthreads();
+    for (int e = tid; e < BW2 * RG; e += blockDim.x) {
+      int k = e % BW2, r = e / BW2;
+      ACC v = ACC(0);
+      if (k < bw && r < nr) {
+        v = xs[(int64_t)(rg + r) * f.m + c0 + k] - tf[k * MAXR + rg + r];
+        tf[k * MAXR + rg + r] = ACC(0);
+      }
+      vb[k][r] = v;
+    }
+    __syncthreads();
+    for (int k = warp; k < bw; k += 16) {
+      ACC acc[RG];
+#pragma unroll
+      for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
+#pragma unroll
+      for (int u = 0; u < BW2 / 32; ++u) {
+        const int i = lane + 32 * u;
+        const ACC l = (i >= k) ? (ACC)X[(int64_t)k * BW2 + i] : ACC(0);
+#pragma unroll
+        for (int q = 0; q < RG; ++q) acc[q] += l * vb[i][q];
+      }
+#pragma unroll
+      for (int q = 0; q < RG; ++q) {
         ACC s = acc[q];
-        for (int i = 0; i < SR; ++i) s += Lt[i][k] * xt[i][r];
-        acc[q] = s;
-      }
-    }
-    __syncthreads();
-  }
-  if (t.r0 < f.m && k < bw)
-#pragma unroll
-    for (int q = 0; q < MAXR / 4; ++q) {
-      int r = g + 4 * q;
-      if (r < nrhs) aadd(&tf[k * MAXR + r], acc[q]);
-    }
-  __threadfence();
-  __syncthreads();
-  if (tid == 0) last = atomicAdd(&a.cnt[t.f], 1u) == (unsigned)(t.ntiles - 1);
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // z_b = L_bb^-T (x_b - tt): z(k) = sum_i Linv(i, k) v(i)
-  const T* Li = a.inv + a.inv_off[t.f] + (int64_t)(c0 / LB) * LB * LB;
-  __shared__ ACC vb[LB][MAXR + 1];
-  for (int e = tid; e < LB * nrhs; e += blockDim.x) {
-    int kk = e % LB, r = e / LB;
-    vb[kk][r] = (kk < bw) ? xs[(int64_t)r * f.m + c0 + kk] - __ldcg(&tf[kk * MAXR + r]) : ACC(0);
-  }
-  __syncthreads();
-  // warp per column kk of the inverse (coalesced), lanes over its 64 rows
-  {
-    const int lane = tid & 31, warp = tid >> 5;
-    for (int kk = warp; kk < bw; kk += blockDim.x / 32) {
-      const ACC l0 = (ACC)Li[(int64_t)kk * LB + lane];
-      const ACC l1 = (ACC)Li[(int64_t)kk * LB + 32 + lane];
-      for (int r = 0; r < nrhs; ++r) {
-        ACC z = l0 * vb[lane][r] + l1 * vb[32 + lane][r];
-        for (int o = 16; o > 0; o >>= 1) z += __shfl_xor_sync(0xffffffffu, z, o);
-        if (lane == 0) xs[(int64_t)r * f.m + c0 + kk] = z;
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0 && q < nr) xs[(int64_t)(rg + q) * f.m + c0 + k] = s;
       }
     }
   }
-  for (int e = tid; e < LB * MAXR; e += blockDim.x) tf[e] = ACC(0);
-  if (tid == 0) a.cnt[t.f] = 0u;
 }
 
 inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
@@ -557,11 +686,17 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
     case LS_SCATTER_BWD:
       k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
-    case LS_FWD_STEP:
-      k_lfwd_step<T, ACC><<<ntask, 128, 0, s>>>(tasks, a);
+    case LS_FWD_DIAG2:
+      k_fwd_diag3<T, ACC><<<ntask, 512, 0, s>>>(tasks, a);
       break;
-    case LS_BWD_STEP:
-      k_lbwd_step<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
+    case LS_FWD_UPD2:
+      k_fwd_upd3<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
+      break;
+    case LS_BWD_RED2:
+      k_bwd_red3<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
+      break;
+    case LS_BWD_DIAG2:
+      k_bwd_diag3<T, ACC><<<ntask, 512, 0, s>>>(tasks, a);
       break;
   }
 }
@@ -572,6 +707,29 @@ void launch_inv_diag(const T* arena, const FrontDesc* fr, const LTask* tasks, in
   if (ntask <= 0) return;
   k_inv_diag<T><<<ntask, LB, 0, s>>>(arena, fr, tasks, inv, inv_off, unit);
 }
+
+template <typename T>
+void prepare_solve_kernels() {
+  SG_CUDA(cudaFuncSetAttribute(k_inv256<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(2 * 64 * 65 * sizeof(T))));
+}
+
+template <typename T>
+void launch_inv256(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+                   const T* inv64, const int64_t* inv_off, T* inv2, const int64_t* inv2_off,
+                   cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_inv256<T><<<ntask, 256, 2 * 64 * 65 * sizeof(T), s>>>(arena, fr, tasks, inv64, inv_off,
+                                                           inv2, inv2_off);
+}
+template void prepare_solve_kernels<float>();
+template void prepare_solve_kernels<double>();
+template void launch_inv256<float>(const float*, const FrontDesc*, const LTask*, int,
+                                   const float*, const int64_t*, float*, const int64_t*,
+                                   cudaStream_t);
+template void launch_inv256<double>(const double*, const FrontDesc*, const LTask*, int,
+                                    const double*, const int64_t*, double*, const int64_t*,
+                                    cudaStream_t);
 
 template void launch_lsolve<float, float>(int, const LTask*, int, LsArgs<float, float>,
                                           cudaStream_t);

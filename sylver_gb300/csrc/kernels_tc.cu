@@ -2,10 +2,13 @@
 // 5th-generation tensor cores (tcgen05, kind::tf32) with the accumulator in
 // tensor memory and operands staged by TMA.
 //
-// Accuracy: 3xTF32.  Each operand is split into hi = rna_tf32(x) and
-// lo = x - hi (both FP32 containers), and C -= Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T
-// accumulates in FP32 -- close to an FP32 product, which keeps iterative
-// refinement convergence as for SIMT FP32 factors.
+// Accuracy: 4xTF32.  Each operand is split into hi = rna_tf32(x) and
+// lo = x - hi (both FP32 containers), and
+// C -= Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T + Alo Blo^T accumulates in FP32: the
+// products are within FP32 rounding of the exact ones, which keeps iterative
+// refinement converging as for SIMT FP32 factors.  (Dropping lo*lo, the usual
+// 3xTF32, cost one extra refinement iteration on the 80^3 workload; the
+// kernel is operand-bound, so the fourth MMA is nearly free.)
 //
 // Operand layout: TF32 MMAs read K-major shared-memory tiles, so A and B come
 // from a transposed copy of the contribution rows of L ("panel rows", one row
@@ -16,7 +19,7 @@
 //
 // One CTA computes one 128 x 128 tile (4 warps):
 //   warp 0 lane 0 : TMA producer over a 3-stage ring (full/empty mbarriers),
-//   warp 1 lane 0 : MMA issuer (12 MMAs per 32-wide k chunk), tcgen05.commit
+//   warp 1 lane 0 : MMA issuer (16 MMAs per 32-wide k chunk), tcgen05.commit
 //                   releases a stage and finally signals the accumulator,
 //   all 4 warps   : epilogue, tcgen05.ld of their 32 TMEM lanes, C -= acc.
 // Every mbarrier wait is bounded: on timeout the CTA records an error bit,
@@ -227,6 +230,7 @@ __global__ void __launch_bounds__(128, 1)
         mma_tf32(tmem, ahi + adv, bhi + adv, idesc, acc0);
         mma_tf32(tmem, ahi + adv, blo + adv, idesc, 1u);
         mma_tf32(tmem, alo + adv, bhi + adv, idesc, 1u);
+        mma_tf32(tmem, alo + adv, blo + adv, idesc, 1u);
       }
       mma_commit(&empty[s]);
     }

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 #include <type_traits>
@@ -42,8 +43,11 @@ bool Runtime::init() {
     prepare_factor_kernels<float>();
     prepare_factor_kernels<double>();
     prepare_tc_kernels();
+    prepare_solve_kernels<float>();
+    prepare_solve_kernels<double>();
   } catch (const std::exception& ex) {
     err = ex.what();
+    fprintf(stderr, "sylver_gb300: device set-up failed: %s\n", err.c_str());
     return false;
   }
   ok = true;
@@ -96,7 +100,7 @@ int64_t FKeep::nnz_orig() const {
 
 namespace {
 // fronts that get the blocked multi-CTA solve
-inline bool is_large(const FrontDesc& d) { return d.n >= 192 || (int64_t)d.m * d.n >= (1 << 18); }
+inline bool is_large(const FrontDesc& d) { return d.n >= 96 || (int64_t)d.m * d.n >= (1 << 16); }
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
 inline int64_t round_up64(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 }  // namespace
@@ -264,7 +268,7 @@ void FKeep::plan_cholesky() {
       if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
     }
     // contribution blocks: one Schur-complement update with K = n, on the
-    // tensor cores (FP32, 3xTF32) for blocks of at least 64 rows
+    // tensor cores (FP32, 4xTF32) for blocks of at least 64 rows
     int64_t u0 = (int64_t)upds.size();
     std::vector<int> tcf;
     for (int s : large) {
@@ -363,9 +367,12 @@ void FKeep::upload_static(cudaStream_t s) {
   status.ensure(sizeof(unsigned));
   anorm.ensure(sizeof(double));
   arena.ensure((size_t)arena_elems * (precision == 1 ? sizeof(float) : sizeof(double)));
-  if (posdef)
-    splan.inv.ensure((size_t)std::max<int64_t>(splan.inv_elems, 1) *
-                     (precision == 1 ? sizeof(float) : sizeof(double)));
+  if (posdef) {
+    // the inverses are formed inside the captured factor graph: allocate now
+    const size_t es = precision == 1 ? sizeof(float) : sizeof(double);
+    splan.inv.ensure((size_t)std::max<int64_t>(splan.inv_elems, 1) * es);
+    splan.inv2.ensure((size_t)std::max<int64_t>(splan.inv2_elems, 1) * es);
+  }
   tcerr.ensure(sizeof(unsigned));
   if (!tclev.empty()) {
     int64_t cap = 0;
@@ -545,6 +552,9 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
   hinv.clear();
   hinv_off.assign(hfr.size(), 0);
   inv_elems = 0;
+  hinv2.clear();
+  hinv2_off.assign(hfr.size(), 0);
+  inv2_elems = 0;
   max_large = 0;
   for (const Level& L : levels) {
     Lv v;
@@ -566,7 +576,14 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
         hinv_off[L.f0 + f] = inv_elems;
         for (int b = 0; b < nb; ++b)
           hinv.push_back({L.f0 + f, b * LB, std::min(LB, d.n - b * LB), 0, 0, 0});
-        inv_elems += (int64_t)nb * LB * LB;
+        // inverses are stored per 256-column block (four 64-blocks each)
+        const int nb2 = (d.n + LSOLVE_BW2 - 1) / LSOLVE_BW2;
+        inv_elems += (int64_t)nb2 * (LSOLVE_BW2 / LB) * LB * LB;
+        hinv2_off[L.f0 + f] = inv2_elems;
+        for (int b = 0; b < nb2; ++b)
+          hinv2.push_back({L.f0 + f, b * LSOLVE_BW2,
+                           std::min(LSOLVE_BW2, d.n - b * LSOLVE_BW2), 0, 0, 0});
+        inv2_elems += (int64_t)nb2 * LSOLVE_BW2 * LSOLVE_BW2;
       }
       auto rows = [&](std::vector<SOp>& ops, int kind) {
         int64_t a = (int64_t)htasks.size();
@@ -575,30 +592,33 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
         push(ops, kind, a);
       };
       rows(v.fwd, LS_GATHER_FWD);
-      for (int b = 0; b < maxb; ++b) {
+      const int LB2 = LSOLVE_BW2;
+      int maxb2 = 0;
+      for (int f = v.nsmall; f < v.nfront; ++f)
+        maxb2 = std::max(maxb2, (hfr[L.f0 + f].n + LB2 - 1) / LB2);
+      auto step = [&](std::vector<SOp>& ops, int kind, int b, bool diag) {
         int64_t a = (int64_t)htasks.size();
         for (int f = v.nsmall; f < v.nfront; ++f) {
           const FrontDesc& d = hfr[L.f0 + f];
-          int c0 = b * LB;
+          int c0 = b * LB2;
           if (c0 >= d.n) continue;
-          int bw = std::min(LB, d.n - c0);
-          for (int r0 = c0; r0 < d.m; r0 += 128) htasks.push_back({f, c0, bw, r0, 0, 0});
+          int bw = std::min(LB2, d.n - c0), c1 = c0 + bw;
+          if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
+          else
+            for (int r0 = c1; r0 < d.m; r0 += (kind == LS_FWD_UPD2 ? 32 : 64))
+              htasks.push_back({f, c0, bw, r0, 0, 0});
         }
-        push(v.fwd, LS_FWD_STEP, a);
+        push(ops, kind, a);
+      };
+      for (int b = 0; b < maxb2; ++b) {
+        step(v.fwd, LS_FWD_DIAG2, b, true);
+        step(v.fwd, LS_FWD_UPD2, b, false);
       }
       rows(v.fwd, LS_SCATTER_FWD);
       rows(v.bwd, LS_GATHER_BWD);
-      for (int b = maxb - 1; b >= 0; --b) {
-        int64_t a = (int64_t)htasks.size();
-        for (int f = v.nsmall; f < v.nfront; ++f) {
-          const FrontDesc& d = hfr[L.f0 + f];
-          int c0 = b * LB;
-          if (c0 >= d.n) continue;
-          int bw = std::min(LB, d.n - c0), c1 = c0 + bw;
-          int nt = std::max(1, (d.m - c1 + 127) / 128);
-          for (int q = 0; q < nt; ++q) htasks.push_back({f, c0, bw, c1 + q * 128, nt, 0});
-        }
-        push(v.bwd, LS_BWD_STEP, a);
+      for (int b = maxb2 - 1; b >= 0; --b) {
+        step(v.bwd, LS_BWD_RED2, b, false);
+        step(v.bwd, LS_BWD_DIAG2, b, true);
       }
       rows(v.bwd, LS_SCATTER_BWD);
     }
@@ -607,6 +627,8 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
   tasks.upload(htasks, s);
   invt.upload(hinv, s);
   inv_off.upload(hinv_off, s);
+  invt2.upload(hinv2, s);
+  inv2_off.upload(hinv2_off, s);
   cnt.ensure((size_t)std::max(max_large, 1) * sizeof(unsigned));
   SG_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes, s));
 }
@@ -614,8 +636,11 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
 template <typename T>
 void SolvePlan::compute_inverses(const T* arena, const FrontDesc* dfr, bool unit, cudaStream_t s) {
   inv.ensure((size_t)std::max<int64_t>(inv_elems, 1) * sizeof(T));
+  inv2.ensure((size_t)std::max<int64_t>(inv2_elems, 1) * sizeof(T));
   launch_inv_diag<T>(arena, dfr, invt.as<LTask>(), (int)hinv.size(), inv.as<T>(),
                      inv_off.as<int64_t>(), unit, s);
+  launch_inv256<T>(arena, dfr, invt2.as<LTask>(), (int)hinv2.size(), inv.as<T>(),
+                   inv_off.as<int64_t>(), inv2.as<T>(), inv2_off.as<int64_t>(), s);
 }
 template void SolvePlan::compute_inverses<float>(const float*, const FrontDesc*, bool,
                                                  cudaStream_t);
@@ -623,7 +648,10 @@ template void SolvePlan::compute_inverses<double>(const double*, const FrontDesc
                                                   cudaStream_t);
 
 void SolvePlan::ensure_tt(size_t elem, int64_t scratch_elems) {
-  tt.ensure((size_t)std::max(max_large, 1) * LSOLVE_BW * 32 * elem);
+  const void* before = tt.p;
+  tt.ensure((size_t)std::max(max_large, 1) * LSOLVE_BW2 * 32 * elem);
+  // the backward steps leave the accumulators zero; a new buffer starts zero
+  if (tt.p != before) SG_CUDA(cudaMemset(tt.p, 0, tt.bytes));
   ys.ensure((size_t)std::max<int64_t>(scratch_elems, 1) * elem);
 }
 
@@ -641,7 +669,8 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
                                     s);
     }
     LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),
-                     inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), cnt.as<unsigned>()};
+                     inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), cnt.as<unsigned>(),
+                     inv2.as<T>(), inv2_off.as<int64_t>() + v.f0};
     for (const SOp& op : fwd ? v.fwd : v.bwd)
       launch_lsolve<T, ACC>(op.kind, tasks.as<LTask>() + op.a, (int)(op.b - op.a), a, s);
   };

@@ -100,7 +100,10 @@ struct SolvePlan {
   std::vector<LTask> hinv;       // diagonal blocks to invert (f = level-ordered index)
   std::vector<int64_t> hinv_off; // per level-ordered front: offset of its inverses
   int64_t inv_elems = 0;
-  DevMem tasks, tt, cnt, ys, inv, invt, inv_off;
+  std::vector<LTask> hinv2;       // 256-column diagonal blocks (f = level-ordered index)
+  std::vector<int64_t> hinv2_off;
+  int64_t inv2_elems = 0;
+  DevMem tasks, tt, cnt, ys, inv, invt, inv_off, inv2, invt2, inv2_off;
   int max_large = 0;
   // Invert every diagonal block of the large fronts (after a factorization).
   template <typename T>

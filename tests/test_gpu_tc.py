@@ -1,8 +1,8 @@
-"""Tensor-core (tcgen05, 3xTF32) contribution-block update.
+"""Tensor-core (tcgen05, 4xTF32) contribution-block update.
 
 The self-check runs the same transposed split + TMA + tcgen05 path as the
 factorization on a synthetic panel and compares with an FP64 host product;
-3xTF32 must be close to FP32 accuracy: the bound 1e-5 is two orders of
+4xTF32 must be close to FP32 accuracy: the bound 1e-5 is two orders of
 magnitude below what a single TF32 product (unit roundoff ~5e-4) gives and
 about what FP32 accumulation over K <= 257 terms gives."""
 import ctypes
