@@ -218,6 +218,11 @@ void spldlt_solve_device(int job, int nrhs, double* x_dev, int ldx, void* akeep,
  * final max-over-RHS scaled backward error.  Returns 0, or -1 for a null fkeep. */
 int sylver_gb300_solve_stats(void const* fkeep, int* ir_iters, double* bwd_err);
 
+/* Scaled backward error after each solve of the last refinement on fkeep
+ * (first entry: after the initial solve); returns the number written
+ * (at most max_entries), or -1 for a null fkeep. */
+int sylver_gb300_solve_history(void const* fkeep, double* bwd_err, int max_entries);
+
 /* Symbolic arrays of an analysis (1-based, reference layout).  Pass null for
  * any array not wanted; sizes: sptr/rptr/nptr nnodes+1, sparent nnodes,
  * rlist rptr[nnodes]-1, nlist 2*(nptr[nnodes]-1), perm n (1-based position). */

@@ -77,7 +77,7 @@ EXPORTS = (
     "spldlt_solve_device", "sylver_gb300_solve_stats", "sylver_gb300_akeep_sizes",
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
-    "sylver_gb300_tc_selfcheck",
+    "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history",
 )
 
 
@@ -120,6 +120,7 @@ def load(path: str | None = None):
         "sylver_gb300_stream": (P, []),
         "sylver_gb300_profile_factor": (I, [P, P, P, P, P]),
         "sylver_gb300_tc_selfcheck": (I, [I, I, ctypes.POINTER(D)]),
+        "sylver_gb300_solve_history": (I, [P, P, I]),
         "spldlt_create_symbolic_tree": (P, [P, I, I, P, P, P, P, P, P, I, P, P, P, P]),
         "spldlt_destroy_symbolic_tree": (None, [P]),
         "spldlt_create_numeric_tree_dbl": (P, [B, P, P, P, P, P, P, P]),
@@ -238,6 +239,11 @@ class Factor:
         it, be = ctypes.c_int(), ctypes.c_double()
         load().sylver_gb300_solve_stats(self.fkeep, ctypes.byref(it), ctypes.byref(be))
         return it.value, be.value
+
+    def solve_history(self):
+        h = np.zeros(64)
+        k = load().sylver_gb300_solve_history(self.fkeep, _p(h), 64)
+        return h[:max(k, 0)].tolist()
 
     def counters(self):
         nl, lv, ms = ctypes.c_long(), ctypes.c_int(), ctypes.c_double()

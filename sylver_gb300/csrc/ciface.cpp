@@ -346,6 +346,18 @@ int sylver_gb300_solve_stats(void const* fkeep, int* ir_iters, double* bwd_err) 
   return 0;
 }
 
+int sylver_gb300_solve_history(void const* fkeep, double* bwd_err, int max_entries) {
+  const FKeep* fk = static_cast<const FKeep*>(fkeep);
+  if (!fk) return -1;
+  int k = 0;
+  for (double v : fk->ir_hist) {
+    if (k >= max_entries) break;
+    if (bwd_err) bwd_err[k] = v;
+    k++;
+  }
+  return k;
+}
+
 int sylver_gb300_akeep_sizes(void const* akeep, int* n, int* nnodes, long* rlist_len,
                              long* nlist_len) {
   const AKeep* ak = static_cast<const AKeep*>(akeep);

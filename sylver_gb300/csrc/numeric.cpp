@@ -733,6 +733,7 @@ int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
   const int* perm = perm0.as<int>();
   last_ir_iters = 0;
   last_bwd_err = -1.0;
+  ir_hist.clear();
   auto one_solve = [&](const double* rhs, int ldr, double* out, int ldo, bool add, int jb) {
     if (f32) {
       launch_permute_in<float>(rhs, ldr, xp.as<float>(), perm, n, nrhs, s);
@@ -780,6 +781,7 @@ int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
       worst = std::max(worst, be);
     }
     last_bwd_err = worst;
+    ir_hist.push_back(worst);
     last_ir_iters = it;
     if (worst <= ir_tol || it >= maxit) break;
     one_solve(resid.as<double>(), n, x, ldx, true, 0);

@@ -171,6 +171,7 @@ struct FKeep {
   double factor_ms = 0.0;
   int last_ir_iters = 0;
   double last_bwd_err = 0.0;
+  std::vector<double> ir_hist;  // backward error after each solve of the last refinement
   int flag = 0;
   int num_neg = 0, num_two = 0, num_delay = 0, num_zero = 0, rank = 0;
   int maxfront = 0;

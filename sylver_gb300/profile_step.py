@@ -38,6 +38,7 @@ def main(argv=None):
     print(f"analyse {t1 - t0:.3f}s factorize {t2 - t1:.3f}s solve {t3 - t2:.3f}s "
           f"ir_iters={it} bwd_err={be:.3e} (device {be_dev:.3e})")
     print("counters", f.counters())
+    print("refinement history", ["%.2e" % v for v in f.solve_history()])
     return 0 if (f.flag == 0 and np.isfinite(be) and be <= 1e-14) else 1
 
 
