@@ -275,6 +275,46 @@ int sylver_gb300_fkeep_counters(void const* fkeep, long* kernel_launches, int* n
 int spldlt_tree_solve_fwd_noalloc_dbl(bool posdef, void const* tree, int nrhs, double* x_dev,
                                       int ldx, void* stream);
 
+/* ---- schedule (kernel-path choices; no reference counterpart) ------------ */
+
+/* Kernel paths of the level schedule.  They select which kernels process a
+ * front, never the arithmetic.  0 keeps the built-in default. */
+typedef struct {
+  int small_front_rows;  /* Cholesky: fronts with at most this many rows are factorised whole
+                            by one CTA (capped at 96 FP64 / 128 FP32; default: the cap) */
+  int tc_min_cb_rows;    /* FP32 Cholesky: contribution blocks with at least this many rows
+                            use the tensor-core update (default 64; negative: never) */
+  int solve_large_cols;  /* fronts with at least this many eliminated columns use the blocked
+                            multi-CTA solve (default 96) */
+  int ldlt_tpp_cols;     /* LDL^T: fronts with at most this many fully-summed columns skip the
+                            a-posteriori block steps and use threshold partial pivoting only
+                            (default 0: none) */
+} sylver_gb300_schedule_t;
+
+/* Set the schedule used by factorizations planned afterwards (a new fkeep);
+ * null restores the defaults.  Process-wide, not thread-safe. */
+void sylver_gb300_set_schedule(sylver_gb300_schedule_t const* schedule);
+void sylver_gb300_get_schedule(sylver_gb300_schedule_t* schedule);
+
+/* ---- learned scheduler network (no reference counterpart) ---------------- */
+
+/* MLP nin -> nhidden -> nhidden -> 1 (ReLU) on the GPU, FP32, used to
+ * predict the log factorization time of a schedule from matrix features.
+ * Parameters (flat): W1 (nhidden x nin), b1, W2 (nhidden x nhidden), b2,
+ * W3 (1 x nhidden), b3.  Inputs are row-major batch x nin (host memory). */
+void* sylver_gb300_mlp_create(int nin, int nhidden, unsigned seed);
+void sylver_gb300_mlp_free(void* mlp);
+long sylver_gb300_mlp_num_params(void const* mlp);
+int sylver_gb300_mlp_set_params(void* mlp, float const* params);
+int sylver_gb300_mlp_get_params(void const* mlp, float* params);
+int sylver_gb300_mlp_forward(void* mlp, float const* x, int batch, float* y);
+/* Mean-squared-error loss and its gradient (np entries) for one batch. */
+int sylver_gb300_mlp_loss_grad(void* mlp, float const* x, float const* y, int batch,
+                               float* loss, float* grad);
+/* Full-batch Adam training for `epochs` steps; loss after the last step. */
+int sylver_gb300_mlp_train(void* mlp, float const* x, float const* y, int batch, int epochs,
+                           float lr, float* final_loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,6 +62,30 @@ class Options(ctypes.Structure):
                 ("scheduler", ctypes.c_int)]
 
 
+class Schedule(ctypes.Structure):
+    """sylver_gb300_schedule_t: kernel-path choices (0 = default)."""
+    _fields_ = [("small_front_rows", ctypes.c_int), ("tc_min_cb_rows", ctypes.c_int),
+                ("solve_large_cols", ctypes.c_int), ("ldlt_tpp_cols", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def set_schedule(**kw):
+    """Schedule for factorizations planned afterwards; no arguments = defaults."""
+    if not kw:
+        load().sylver_gb300_set_schedule(None)
+        return
+    s = Schedule(**{k: int(v) for k, v in kw.items()})
+    load().sylver_gb300_set_schedule(ctypes.byref(s))
+
+
+def get_schedule():
+    s = Schedule()
+    load().sylver_gb300_get_schedule(ctypes.byref(s))
+    return s.as_dict()
+
+
 _lib = None
 
 # every extern "C" entry point declared in include/sylver_gb300.h
@@ -77,7 +101,10 @@ EXPORTS = (
     "spldlt_solve_device", "sylver_gb300_solve_stats", "sylver_gb300_akeep_sizes",
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
-    "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history",
+    "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
+    "sylver_gb300_get_schedule", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
+    "sylver_gb300_mlp_num_params", "sylver_gb300_mlp_set_params", "sylver_gb300_mlp_get_params",
+    "sylver_gb300_mlp_forward", "sylver_gb300_mlp_loss_grad", "sylver_gb300_mlp_train",
 )
 
 
@@ -121,6 +148,16 @@ def load(path: str | None = None):
         "sylver_gb300_profile_factor": (I, [P, P, P, P, P]),
         "sylver_gb300_tc_selfcheck": (I, [I, I, ctypes.POINTER(D)]),
         "sylver_gb300_solve_history": (I, [P, P, I]),
+        "sylver_gb300_set_schedule": (None, [ctypes.POINTER(Schedule)]),
+        "sylver_gb300_get_schedule": (None, [ctypes.POINTER(Schedule)]),
+        "sylver_gb300_mlp_create": (P, [I, I, ctypes.c_uint]),
+        "sylver_gb300_mlp_free": (None, [P]),
+        "sylver_gb300_mlp_num_params": (L, [P]),
+        "sylver_gb300_mlp_set_params": (I, [P, P]),
+        "sylver_gb300_mlp_get_params": (I, [P, P]),
+        "sylver_gb300_mlp_forward": (I, [P, P, I, P]),
+        "sylver_gb300_mlp_loss_grad": (I, [P, P, P, I, P, P]),
+        "sylver_gb300_mlp_train": (I, [P, P, P, I, I, ctypes.c_float, P]),
         "spldlt_create_symbolic_tree": (P, [P, I, I, P, P, P, P, P, P, I, P, P, P, P]),
         "spldlt_destroy_symbolic_tree": (None, [P]),
         "spldlt_create_numeric_tree_dbl": (P, [B, P, P, P, P, P, P, P]),

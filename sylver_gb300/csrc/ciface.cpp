@@ -553,3 +553,26 @@ int spldlt_tree_solve_bwd_posdef_dbl(void const* tree, int nrhs, double* x, int 
 }
 
 }  // extern "C"
+
+extern "C" {
+
+void sylver_gb300_set_schedule(sylver_gb300_schedule_t const* s) {
+  Schedule& c = Schedule::current();
+  c = Schedule();
+  if (!s) return;
+  c.small_front_rows = s->small_front_rows;
+  c.tc_min_cb_rows = s->tc_min_cb_rows;
+  c.solve_large_cols = s->solve_large_cols;
+  c.ldlt_tpp_cols = s->ldlt_tpp_cols;
+}
+
+void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
+  if (!s) return;
+  const Schedule& c = Schedule::current();
+  s->small_front_rows = c.small_front_rows;
+  s->tc_min_cb_rows = c.tc_min_cb_rows;
+  s->solve_large_cols = c.solve_large_cols;
+  s->ldlt_tpp_cols = c.ldlt_tpp_cols;
+}
+
+}  // extern "C"

@@ -17,11 +17,11 @@
 // level covers it.  TMA boxes are 32 (k) x 128 (rows) FP32 with 128-byte
 // swizzle, matching the tcgen05 K-major SWIZZLE_128B canonical layout.
 //
-// One CTA computes one 128 x 128 tile (4 warps):
-//   warp 0 lane 0 : TMA producer over a 3-stage ring (full/empty mbarriers),
-//   warp 1 lane 0 : MMA issuer (16 MMAs per 32-wide k chunk), tcgen05.commit
-//                   releases a stage and finally signals the accumulator,
-//   all 4 warps   : epilogue, tcgen05.ld of their 32 TMEM lanes, C -= acc.
+// A persistent CTA per SM walks the level's 128 x 128 tiles (10 warps): a TMA
+// producer, an MMA issuer (16 MMAs per 32-wide k chunk; tcgen05.commit
+// releases a stage and signals an accumulator) and eight epilogue warps that
+// tcgen05.ld their 32 TMEM lanes and apply C -= acc while the next tile's
+// MMAs run in the other accumulator.
 // Every mbarrier wait is bounded: on timeout the CTA records an error bit,
 // skips the epilogue, waits (bounded) for its own copies and frees TMEM.
 #include <cuda.h>
@@ -154,34 +154,72 @@ __device__ __forceinline__ void tmem_ld32<32>(uint32_t taddr, float (&v)[32]) {
 
 // ---------------------------------------------------------------------------
 
-__global__ void __launch_bounds__(128, 1)
+constexpr int TC_EPI_WARP0 = 2;                  // warps 2..9 run the epilogue
+constexpr int TC_EPI_WARPS = 8;                  // two per TMEM lane quarter
+constexpr int TC_EPI_COLS = TC_N / 2;            // columns per epilogue thread
+constexpr int TC_THREADS = 32 * (TC_EPI_WARP0 + TC_EPI_WARPS);
+constexpr int TC_TMEM_COLS = 2 * TC_N;           // two accumulators (double buffer)
+
+// arrive on an mbarrier (one arrival)
+__device__ __forceinline__ void mbar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+
+// bounded wait that also gives up once another role has aborted
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* b, uint32_t parity, unsigned* err,
+                                                   volatile int* abort_flag) {
+  const uint64_t t0 = global_ns();
+  for (long it = 0; it < WAIT_LIMIT; ++it) {
+    if (mbar_try(b, parity)) return true;
+    if ((it & 255) == 255) {
+      if (*abort_flag) return false;
+      if (global_ns() - t0 > 1000000000ull) break;
+    }
+  }
+  atomicOr(err, ST_TIMEOUT);
+  *abort_flag = 1;
+  return false;
+}
+
+// Persistent: CTA b processes tiles b, b + gridDim.x, ...
+//   warp 0 lane 0 : TMA producer over a TC_STAGES ring shared by all tiles,
+//   warp 1 lane 0 : MMA issuer; tile i accumulates in TMEM columns
+//                   [(i & 1) * 128, +128) so the epilogue of tile i overlaps
+//                   the MMAs of tile i + 1,
+//   warps 2..9    : epilogue; each thread owns half a row of the tile, loads
+//                   its 64 C values before the accumulator is ready, then
+//                   C -= acc and releases the accumulator.
+__global__ void __launch_bounds__(TC_THREADS, 1)
     k_update_tc(const __grid_constant__ CUtensorMap map_hi,
                 const __grid_constant__ CUtensorMap map_lo, float* __restrict__ arena,
-                const TcTask* __restrict__ tasks, unsigned* __restrict__ err) {
+                const TcTask* __restrict__ tasks, int ntask, unsigned* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1 KiB alignment for the swizzled tiles
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], done;
+  __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], acc_full[2], acc_empty[2], done;
   __shared__ uint32_t tmem_slot;
-  __shared__ int failed;
+  __shared__ int abort_flag;
+  volatile int* abortp = &abort_flag;
 
-  const TcTask t = tasks[blockIdx.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nk = t.nk;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < TC_STAGES; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(&acc_full[a], 1);
+      mbar_init(&acc_empty[a], TC_EPI_WARPS);  // one arrival per epilogue warp
+    }
     mbar_init(&done, 1);
-    failed = 0;
+    abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      su32(&tmem_slot)),
-                 "r"(TC_N)
+                 "r"(TC_TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -190,83 +228,140 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
 
-  int issued = 0;  // TMA chunks issued (producer)
-  if (warp == 0 && lane == 0) {
-    for (int kc = 0; kc < nk; ++kc) {
-      const int s = kc % TC_STAGES;
-      if (kc >= TC_STAGES && !mbar_wait(&empty[s], ((kc / TC_STAGES) - 1) & 1, err)) {
-        failed = 1;
-        break;
+  int issued = 0;  // TMA chunks issued by the producer
+  if (warp == 0) {
+    if (lane == 0) {
+      int g = 0;
+      for (int ti = blockIdx.x; ti < ntask && !*abortp; ti += gridDim.x) {
+        const TcTask t = tasks[ti];
+        bool ok = true;
+        for (int kc = 0; kc < t.nk; ++kc, ++g) {
+          const int s = g % TC_STAGES;
+          if (g >= TC_STAGES &&
+              !mbar_wait_or_abort(&empty[s], ((g / TC_STAGES) - 1) & 1, err, abortp)) {
+            ok = false;
+            break;
+          }
+          unsigned char* st = smem + s * STAGE_BYTES;
+          mbar_expect_tx(&full[s], STAGE_BYTES);
+          const int x = kc * TC_KC;
+          tma_load_2d(st + 0 * TILE_BYTES, &map_hi, x, t.a_row, &full[s]);
+          tma_load_2d(st + 1 * TILE_BYTES, &map_lo, x, t.a_row, &full[s]);
+          tma_load_2d(st + 2 * TILE_BYTES, &map_hi, x, t.b_row, &full[s]);
+          tma_load_2d(st + 3 * TILE_BYTES, &map_lo, x, t.b_row, &full[s]);
+          issued = g + 1;
+        }
+        if (!ok) break;
       }
-      unsigned char* st = smem + s * STAGE_BYTES;
-      mbar_expect_tx(&full[s], STAGE_BYTES);
-      const int x = kc * TC_KC;
-      tma_load_2d(st + 0 * TILE_BYTES, &map_hi, x, t.a_row, &full[s]);
-      tma_load_2d(st + 1 * TILE_BYTES, &map_lo, x, t.a_row, &full[s]);
-      tma_load_2d(st + 2 * TILE_BYTES, &map_hi, x, t.b_row, &full[s]);
-      tma_load_2d(st + 3 * TILE_BYTES, &map_lo, x, t.b_row, &full[s]);
-      issued = kc + 1;
     }
-  } else if (warp == 1 && lane == 0) {
-    const uint32_t idesc = tf32_idesc();
-    int kc = 0;
-    for (; kc < nk; ++kc) {
-      const int s = kc % TC_STAGES;
-      if (!mbar_wait(&full[s], (kc / TC_STAGES) & 1, err)) {
-        failed = 1;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      unsigned char* st = smem + s * STAGE_BYTES;
-      const uint64_t ahi = sw128_desc(su32(st + 0 * TILE_BYTES));
-      const uint64_t alo = sw128_desc(su32(st + 1 * TILE_BYTES));
-      const uint64_t bhi = sw128_desc(su32(st + 2 * TILE_BYTES));
-      const uint64_t blo = sw128_desc(su32(st + 3 * TILE_BYTES));
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = tf32_idesc();
+      int g = 0, it = 0;
+      for (int ti = blockIdx.x; ti < ntask; ti += gridDim.x, ++it) {
+        const int a = it & 1;
+        // accumulator a was last used by tile it - 2: wait for its epilogue
+        if (it >= 2 && !mbar_wait_or_abort(&acc_empty[a], ((it >> 1) - 1) & 1, err, abortp))
+          break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int nk = tasks[ti].nk;
+        const uint32_t d = tmem + (uint32_t)(a * TC_N);
+        bool ok = true;
+        for (int kc = 0; kc < nk; ++kc, ++g) {
+          const int s = g % TC_STAGES;
+          if (!mbar_wait_or_abort(&full[s], (g / TC_STAGES) & 1, err, abortp)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          unsigned char* st = smem + s * STAGE_BYTES;
+          const uint64_t ahi = sw128_desc(su32(st + 0 * TILE_BYTES));
+          const uint64_t alo = sw128_desc(su32(st + 1 * TILE_BYTES));
+          const uint64_t bhi = sw128_desc(su32(st + 2 * TILE_BYTES));
+          const uint64_t blo = sw128_desc(su32(st + 3 * TILE_BYTES));
 #pragma unroll
-      for (int kk = 0; kk < TC_KC / 8; ++kk) {
-        // 8 tf32 = 32 bytes further along k inside the swizzled row
-        const uint64_t adv = (uint64_t)((kk * 32) >> 4);
-        const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
-        mma_tf32(tmem, ahi + adv, bhi + adv, idesc, acc0);
-        mma_tf32(tmem, ahi + adv, blo + adv, idesc, 1u);
-        mma_tf32(tmem, alo + adv, bhi + adv, idesc, 1u);
-        mma_tf32(tmem, alo + adv, blo + adv, idesc, 1u);
+          for (int kk = 0; kk < TC_KC / 8; ++kk) {
+            // 8 tf32 = 32 bytes further along k inside the swizzled row
+            const uint64_t adv = (uint64_t)((kk * 32) >> 4);
+            const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
+            mma_tf32(d, ahi + adv, bhi + adv, idesc, acc0);
+            mma_tf32(d, ahi + adv, blo + adv, idesc, 1u);
+            mma_tf32(d, alo + adv, bhi + adv, idesc, 1u);
+            mma_tf32(d, alo + adv, blo + adv, idesc, 1u);
+          }
+          mma_commit(&empty[s]);
+        }
+        if (!ok) break;
+        mma_commit(&acc_full[a]);
       }
-      mma_commit(&empty[s]);
+      // every MMA issued so far has completed once `done` fires
+      mma_commit(&done);
     }
-    mma_commit(&done);
-  }
-  __syncthreads();
-  // the accumulator is complete (or the MMAs issued so far have drained)
-  // once `done` fires; wait for it even after a failure, before TMEM is freed
-  const bool drained = mbar_wait(&done, 0, err);
-  const bool ok = drained && !failed;
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (ok) {
-    const int row = t.row0 + warp * 32 + lane;
-    float* C = arena + t.c_off;
-#pragma unroll 1
-    for (int c = 0; c < TC_N / 32; ++c) {
-      float v[32];
-      tmem_ld32<32>(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 32), v);
-      if (row < t.rowEnd) {
+  } else {
+    // TMEM lanes [32q, 32q + 32) are this warp's; it owns columns
+    // [h * 64, h * 64 + 64) of each tile
+    const int q = warp & 3, h = (warp - TC_EPI_WARP0) >> 2;
+    int it = 0;
+    for (int ti = blockIdx.x; ti < ntask; ti += gridDim.x, ++it) {
+      const int a = it & 1;
+      const TcTask t = tasks[ti];
+      const int row = t.row0 + q * 32 + lane;
+      const int c0 = t.col0 + h * TC_EPI_COLS;
+      // columns [c0, cend) of this row are updated (lower triangle, in range)
+      const int cend = row < t.rowEnd ? min(t.colEnd, row + 1) : c0;
+      const int64_t ldc = t.ldc;
+      const float* src = arena + t.c_off + row + (int64_t)c0 * ldc;
+      float cv[TC_EPI_COLS];
+#pragma unroll
+      for (int j = 0; j < TC_EPI_COLS; ++j) {
+        cv[j] = c0 + j < cend ? *src : 0.f;
+        src += ldc;
+      }
+      // warp-uniform wait: tcgen05.ld below is a warp-collective instruction
+      int ready = 0;
+      if (lane == 0) ready = mbar_wait_or_abort(&acc_full[a], (it >> 1) & 1, err, abortp);
+      ready = __shfl_sync(0xffffffffu, ready, 0);
+      if (!ready) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // recompute the store addresses and bounds here (opaque copies):
+      // reusing the load-side ones would keep 64 of each live across the wait
+      float* dst = arena + t.c_off + row + (int64_t)c0 * ldc;
+      int cst = c0, cen = cend;
+      asm volatile("mov.b64 %0, %0;" : "+l"(dst));
+      asm volatile("mov.b32 %0, %0;" : "+r"(cst));
+      asm volatile("mov.b32 %0, %0;" : "+r"(cen));
+#pragma unroll
+      for (int c = 0; c < TC_EPI_COLS / 32; ++c) {
+        float v[32];
+        tmem_ld32<32>(tmem + ((uint32_t)(q * 32) << 16) +
+                          (uint32_t)(a * TC_N + h * TC_EPI_COLS + c * 32),
+                      v);
 #pragma unroll
         for (int j = 0; j < 32; ++j) {
-          const int col = t.col0 + c * 32 + j;
-          if (col < t.colEnd && col <= row) C[(int64_t)col * t.ldc + row] -= v[j];
+          if (cst + c * 32 + j < cen) *dst = cv[c * 32 + j] - v[j];
+          dst += ldc;
         }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acc_empty[a]);
     }
   }
-  // copies still in flight after a timeout: wait for them (bounded) before
-  // the shared memory they target goes away
-  if (!ok && warp == 0 && lane == 0) {
-    for (int kc = 0; kc < issued; ++kc) mbar_wait(&full[kc % TC_STAGES], (kc / TC_STAGES) & 1, err);
+  __syncthreads();
+  // all MMAs this CTA issued have drained once `done` fires; wait for it even
+  // after a failure, before TMEM is freed
+  mbar_wait(&done, 0, err);
+  // copies still in flight after a failure: wait (bounded) for the last one
+  // issued on each stage before the shared memory they target goes away
+  if (*abortp && warp == 0 && lane == 0) {
+    for (int g = issued - 1; g >= 0 && g >= issued - TC_STAGES; --g)
+      mbar_wait(&full[g % TC_STAGES], (g / TC_STAGES) & 1, err);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_N)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TC_TMEM_COLS)
                  : "memory");
 }
 
@@ -308,9 +403,14 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 size_t tc_smem_bytes() { return (size_t)TC_STAGES * STAGE_BYTES + 1024; }
 
+static int g_num_sms = 0;
+
 void prepare_tc_kernels() {
   SG_CUDA(cudaFuncSetAttribute(k_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)tc_smem_bytes()));
+  int dev = 0;
+  SG_CUDA(cudaGetDevice(&dev));
+  SG_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
 }
 
 void make_panel_map(CUtensorMap* map, const float* base, int64_t rows, int pitch) {
@@ -335,7 +435,9 @@ void launch_split_t(const float* arena, const TcSplit* sp, int nsplit, int64_t m
 void launch_update_tc(const CUtensorMap& hi, const CUtensorMap& lo, float* arena,
                       const TcTask* t, int ntask, unsigned* err, cudaStream_t s) {
   if (ntask <= 0) return;
-  k_update_tc<<<ntask, 128, tc_smem_bytes(), s>>>(hi, lo, arena, t, err);
+  // one persistent CTA per SM (the shared-memory ring admits one per SM)
+  const int grid = std::min(ntask, g_num_sms > 0 ? g_num_sms : 148);
+  k_update_tc<<<grid, TC_THREADS, tc_smem_bytes(), s>>>(hi, lo, arena, t, ntask, err);
 }
 
 }  // namespace sylver_gb300

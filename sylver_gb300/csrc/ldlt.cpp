@@ -230,7 +230,9 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
                  u, small, fk.action ? 1 : 0};
     std::vector<int> p(nslot, 0);
     std::vector<char> app_done(nslot, 0);
-    for (int q = 0; q < nslot; ++q) app_done[q] = L.n[F[q]] == 0;
+    // small fronts may skip the block steps and go to TPP directly
+    const int tpp_cols = Schedule::current().ldlt_tpp_cols;
+    for (int q = 0; q < nslot; ++q) app_done[q] = L.n[F[q]] == 0 || L.n[F[q]] <= tpp_cols;
     std::vector<int> hraw, hnp;
     std::vector<double> hdv;
     for (;;) {

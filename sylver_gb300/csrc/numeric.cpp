@@ -23,6 +23,11 @@ Runtime& Runtime::get() {
   return rt;
 }
 
+Schedule& Schedule::current() {
+  static Schedule s;
+  return s;
+}
+
 bool Runtime::init() {
   if (ok) return true;
   int count = 0;
@@ -100,7 +105,9 @@ int64_t FKeep::nnz_orig() const {
 
 namespace {
 // fronts that get the blocked multi-CTA solve
-inline bool is_large(const FrontDesc& d) { return d.n >= 96 || (int64_t)d.m * d.n >= (1 << 16); }
+inline bool is_large(const FrontDesc& d) {
+  return d.n >= Schedule::current().solve_cols() || (int64_t)d.m * d.n >= (1 << 16);
+}
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
 inline int64_t round_up64(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 }  // namespace
@@ -116,7 +123,9 @@ void FKeep::plan_cholesky() {
   const int TM = f32 ? Tiles<float>::TM : Tiles<double>::TM;
   const int NB = f32 ? Tiles<float>::NB : Tiles<double>::NB;
   const int RT = f32 ? Tiles<float>::RT : Tiles<double>::RT;
-  const int SMALL_M = f32 ? Tiles<float>::SMALL_M : Tiles<double>::SMALL_M;
+  const Schedule& sched = Schedule::current();
+  const int SMALL_M = sched.small_rows(f32 ? Tiles<float>::SMALL_M : Tiles<double>::SMALL_M);
+  const int TC_ROWS = sched.tc_rows();
 
   order.resize(ns);
   std::iota(order.begin(), order.end(), 0);
@@ -274,7 +283,7 @@ void FKeep::plan_cholesky() {
     for (int s : large) {
       int m = st.nrow[s], n = st.ncol[s];
       if (m <= n) continue;
-      if (f32 && use_tc && m - n >= 64) {
+      if (f32 && use_tc && TC_ROWS > 0 && m - n >= TC_ROWS) {
         tcf.push_back(s);
         continue;
       }

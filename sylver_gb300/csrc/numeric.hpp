@@ -47,6 +47,21 @@ struct DevMem {
   }
 };
 
+// Kernel-path choices of the schedule (never the arithmetic).  Read when a
+// factorization is planned; 0 selects the built-in default.
+struct Schedule {
+  int small_front_rows = 0;  // Cholesky: fronts with <= rows factorised whole by one CTA
+  int tc_min_cb_rows = 0;    // FP32 Cholesky: CB rows for the tensor-core update (<0: never)
+  int solve_large_cols = 0;  // fronts with >= eliminated columns use the blocked solve
+  int ldlt_tpp_cols = 0;     // LDL^T: fronts with <= fully-summed columns use TPP only
+  static Schedule& current();
+  int small_rows(int compiled_max) const {
+    return small_front_rows > 0 ? std::min(small_front_rows, compiled_max) : compiled_max;
+  }
+  int tc_rows() const { return tc_min_cb_rows == 0 ? 64 : tc_min_cb_rows; }
+  int solve_cols() const { return solve_large_cols > 0 ? solve_large_cols : 96; }
+};
+
 // Process-wide device context: device 0, one non-blocking stream.
 struct Runtime {
   int device = -1;

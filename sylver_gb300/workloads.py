@@ -313,3 +313,40 @@ def backward_error(full: sp.spmatrix, x: np.ndarray, b: np.ndarray):
         den = anorm * np.abs(x[:, j]).max() + np.abs(b[:, j]).max()
         out.append(np.abs(r[:, j]).max() / den if den > 0 else 0.0)
     return np.array(out)
+
+
+def block_diagonal(problems):
+    """Stack independent instances into one block-diagonal system (their
+    assembly trees form a forest, so one analysis / factorization / solve
+    processes every instance level by level in shared launches).  Returns
+    (Problem, offsets) with offsets[k] the first row of instance k."""
+    ptrs, rows, vals, orders, rhs = [], [], [], [], []
+    offs = [0]
+    nz = 0
+    for p in problems:
+        n0 = offs[-1]
+        a = p.a
+        ptrs.append(a.ptr[:-1] - 1 + nz)
+        rows.append(a.row + n0)
+        vals.append(a.val)
+        orders.append(p.order + n0)
+        rhs.append(p.rhs[:, 0])
+        nz += a.nnz
+        offs.append(n0 + a.n)
+    n = offs[-1]
+    ptr = np.concatenate(ptrs + [np.array([nz], dtype=np.int64)]) + 1
+    big = SymMatrix(n, ptr.astype(np.int64), np.concatenate(rows).astype(np.int32),
+                    np.concatenate(vals))
+    b = np.asfortranarray(np.concatenate(rhs).reshape(-1, 1))
+    inert = (0, 0, n) if all(p.posdef for p in problems) else None
+    return Problem(f"batch{len(problems)}", big, np.concatenate(orders).astype(np.int32),
+                   all(p.posdef for p in problems), b, inertia=inert), np.array(offs)
+
+
+def instance_backward_errors(problems, offs, x):
+    """Scaled backward error of each instance of a block-diagonal solve."""
+    out = []
+    for k, p in enumerate(problems):
+        xs = x[offs[k]:offs[k + 1]]
+        out.append(backward_error(p.a.to_scipy_full(), xs, p.rhs).max())
+    return np.array(out)

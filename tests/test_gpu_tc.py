@@ -4,7 +4,9 @@ The self-check runs the same transposed split + TMA + tcgen05 path as the
 factorization on a synthetic panel and compares with an FP64 host product;
 4xTF32 must be close to FP32 accuracy: the bound 1e-5 is two orders of
 magnitude below what a single TF32 product (unit roundoff ~5e-4) gives and
-about what FP32 accumulation over K <= 257 terms gives."""
+about what FP32 accumulation over K <= 257 terms gives.  The larger cases
+have more tiles than the GPU has SMs, so persistent CTAs walk several tiles
+and reuse both accumulators and every pipeline stage."""
 import ctypes
 
 import pytest
@@ -12,7 +14,8 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("rows,k", [(128, 32), (200, 70), (300, 257), (1000, 96)])
+@pytest.mark.parametrize("rows,k", [(128, 32), (200, 70), (300, 257), (1000, 96),
+                                    (2500, 160), (4000, 64)])
 def test_tc_update_selfcheck(sylver, gpu, rows, k):
     lib = sylver.load()
     err = ctypes.c_double(-1.0)
