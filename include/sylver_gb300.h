@@ -243,9 +243,11 @@ void* sylver_gb300_stream(void);
 /* Re-run the factorization held by fkeep with one CUDA event pair around
  * every launch (no graph) and accumulate per kernel kind:
  * 0 memset, 1 init-A, 2 extend-add, 3 small fronts, 4 panel triangular solve,
- * 5 tile update, 6 diagonal-block Cholesky (Cholesky factorizations only).  ms[k] = total milliseconds, launches[k] = count,
- * flops[k] = algorithmic flops (update kernels: lower-triangle tile work).
- * Arrays hold 8 entries.  Returns 0 or a reference flag. */
+ * 5 SIMT tile update, 6 diagonal-block Cholesky, 7 solve inverses, 8 tensor-core
+ * panel split, 9 tensor-core update, 10 blocked diagonal block, 11 blocked panel
+ * (Cholesky factorizations only).  ms[k] = total milliseconds, launches[k] =
+ * count, flops[k] = algorithmic flops (update kernels: lower-triangle tile work).
+ * Arrays hold 12 entries.  Returns 0 or a reference flag. */
 int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, long* launches,
                                 double* flops);
 
@@ -289,6 +291,11 @@ typedef struct {
   int ldlt_tpp_cols;     /* LDL^T: fronts with at most this many fully-summed columns skip the
                             a-posteriori block steps and use threshold partial pivoting only
                             (default 0: none) */
+  int fs_panel_cols;     /* FP32 Cholesky: width of the outer panels in which the fully-summed
+                            columns of large fronts are eliminated, a multiple of 64 up to 256
+                            (default 256); the trailing fully-summed update after each panel
+                            runs on the tensor cores.  Negative: 64-column steps with SIMT
+                            updates throughout */
 } sylver_gb300_schedule_t;
 
 /* Set the schedule used by factorizations planned afterwards (a new fkeep);

@@ -65,7 +65,8 @@ class Options(ctypes.Structure):
 class Schedule(ctypes.Structure):
     """sylver_gb300_schedule_t: kernel-path choices (0 = default)."""
     _fields_ = [("small_front_rows", ctypes.c_int), ("tc_min_cb_rows", ctypes.c_int),
-                ("solve_large_cols", ctypes.c_int), ("ldlt_tpp_cols", ctypes.c_int)]
+                ("solve_large_cols", ctypes.c_int), ("ldlt_tpp_cols", ctypes.c_int),
+                ("fs_panel_cols", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -289,7 +290,7 @@ class Factor:
         return dict(kernel_launches=nl.value, nlevels=lv.value, factor_ms=ms.value)
 
     KINDS = ("memset", "init_a", "extend_add", "small_fronts", "panel_trsm", "update",
-             "diag_chol", "diag_inverse", "panel_split", "update_tc", "other10", "other11")
+             "diag_chol", "diag_inverse", "panel_split", "update_tc", "blk_diag", "blk_panel")
 
     def profile(self, val_dev_ptr=None):
         """Per-kernel-kind timing of one extra factorization (no graph)."""

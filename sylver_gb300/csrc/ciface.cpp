@@ -564,6 +564,7 @@ void sylver_gb300_set_schedule(sylver_gb300_schedule_t const* s) {
   c.tc_min_cb_rows = s->tc_min_cb_rows;
   c.solve_large_cols = s->solve_large_cols;
   c.ldlt_tpp_cols = s->ldlt_tpp_cols;
+  c.fs_panel_cols = s->fs_panel_cols;
 }
 
 void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
@@ -573,6 +574,7 @@ void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
   s->tc_min_cb_rows = c.tc_min_cb_rows;
   s->solve_large_cols = c.solve_large_cols;
   s->ldlt_tpp_cols = c.ldlt_tpp_cols;
+  s->fs_panel_cols = c.fs_panel_cols;
 }
 
 }  // extern "C"

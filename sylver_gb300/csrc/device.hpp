@@ -67,6 +67,18 @@ struct UpdTask {
   int ldc, lda, ldb, row0, col0, rowEnd, colEnd, k0, k1, pad;
 };
 
+// Blocked FP32 Cholesky of large fronts (kernels_blocked.cu): inner steps of
+// BLK_B columns inside outer panels of at most BLK_W columns.
+constexpr int BLK_B = 64;
+constexpr int BLK_W = 256;
+// Diagonal block [c, c+bw) of a front inside the outer panel ending at
+// column pend; xi indexes the block's inverse in the launch's scratch.  For
+// the panel kernel r0 is the first of the CTA's 64 rows (>= c + bw).
+struct BlkTask {
+  int64_t off;
+  int ld, m, c, bw, pend, r0, xi, pad;
+};
+
 // Extend-add of one child contribution column into its parent; the entry
 // (i, j), i >= j, of the child block lands at (max, min) of the mapped rows
 // (maps are monotone for Cholesky, not once delayed columns move up).
@@ -101,6 +113,14 @@ template <typename T>
 void launch_panel_trsm(T* arena, const PanelTask* t, int ntask, cudaStream_t s);
 template <typename T>
 void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStream_t s);
+
+// Launchers (kernels_blocked.cu), FP32 only.  xinv holds one 64 x 64
+// inverse per diagonal-block task of the launch.
+void prepare_blocked_kernels();
+void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, unsigned* status,
+                     cudaStream_t s);
+void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
+                      cudaStream_t s);
 
 template <typename T> struct Tiles;
 template <> struct Tiles<double> {
@@ -138,8 +158,9 @@ constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
 constexpr int LSOLVE_BW2 = 256;  // columns per solve step
 // Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
 // explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
-// index), tt: 64 x 32 accumulators per front, cnt: one ticket counter per
-// front (both zero on entry and left zero).
+// index), tt: two 256 x 32 accumulators per front (backward steps alternate
+// between them; the backward gather clears both), cnt: one ticket counter
+// per front.
 template <typename T, typename ACC>
 struct LsArgs {
   const T* arena;
@@ -156,15 +177,17 @@ struct LsArgs {
   unsigned* cnt;
   const T* inv2;            // 256x256 inverses of the solve-step diagonal blocks
   const int64_t* inv2_off;  // per front of the level
+  const T* inv2t;           // the same inverses transposed (row-major)
 };
 // Inverse of each 256-column diagonal block from its 64x64 inverses: task
-// (front f, c0, bw), output at inv2 + inv2_off[f] + (c0/256)*256*256.
+// (front f, c0, bw), output at inv2 + inv2_off[f] + (c0/256)*256*256
+// (column-major) and, transposed, at the same offset of inv2t.
 template <typename T>
 void prepare_solve_kernels();
 template <typename T>
 void launch_inv256(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
-                   const T* inv64, const int64_t* inv_off, T* inv2, const int64_t* inv2_off,
-                   cudaStream_t s);
+                   const T* inv64, const int64_t* inv_off, T* inv2, T* inv2t,
+                   const int64_t* inv2_off, cudaStream_t s);
 template <typename T, typename ACC>
 void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cudaStream_t s);
 // Explicit inverse of each diagonal block: task (front f, c0, bw), output at

@@ -44,22 +44,28 @@ __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
     int i = idx % m, r = idx / m;
     xs[idx] = (i < nc) ? x[(int64_t)r * n + rl[i]] : ACC(0);
   }
+  __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
+  const int nwarps = blockDim.x >> 5;
   __syncthreads();
   for (int c0 = 0; c0 < nc; c0 += SB) {
     const int bw = min(SB, nc - c0);
-    if (warp == 0) {
-      for (int r = 0; r < nrhs; ++r) {
-        ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] : ACC(0);
-        for (int kk = 0; kk < bw; ++kk) {
-          ACC vk = __shfl_sync(0xffffffffu, v, kk);
-          if (!unit) vk = vk / (ACC)L[(int64_t)(c0 + kk) * ld + c0 + kk];
-          if (lane == kk) v = vk;
-          if (lane > kk && lane < bw) v -= (ACC)L[(int64_t)(c0 + kk) * ld + c0 + lane] * vk;
-        }
-        if (lane < bw) {
-          xs[(int64_t)r * m + c0 + lane] = v;
-          y[lane][r] = v;
-        }
+    for (int e = tid; e < SB * SB; e += blockDim.x) {
+      const int i = e % SB, k = e / SB;
+      Ld[k][i] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+    }
+    __syncthreads();
+    // diagonal block: one right-hand side per warp at a time
+    for (int r = warp; r < nrhs; r += nwarps) {
+      ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] : ACC(0);
+      for (int kk = 0; kk < bw; ++kk) {
+        ACC vk = __shfl_sync(0xffffffffu, v, kk);
+        if (!unit) vk = vk / Ld[kk][kk];
+        if (lane == kk) v = vk;
+        if (lane > kk && lane < bw) v -= Ld[kk][lane] * vk;
+      }
+      if (lane < bw) {
+        xs[(int64_t)r * m + c0 + lane] = v;
+        y[lane][r] = v;
       }
     }
     __syncthreads();
@@ -99,6 +105,7 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
                                                    const int64_t* __restrict__ scr_off,
                                                    bool unit) {
   __shared__ ACC tt[SB][MAXR];
+  __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
   const FrontDesc f = fr[blockIdx.x];
   const T* L = arena + f.off;
   const int ld = f.ld, m = f.m, nc = f.n;
@@ -135,17 +142,20 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
         }
       }
     }
+    for (int e = tid; e < SB * SB; e += blockDim.x) {
+      const int i = e % SB, k = e / SB;
+      Ld[k][i] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+    }
     __syncthreads();
-    if (warp == 0) {
-      for (int r = 0; r < nrhs; ++r) {
-        ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] - tt[lane][r] : ACC(0);
-        for (int kk = bw - 1; kk >= 0; --kk) {
-          if (lane == kk && !unit) v = v / (ACC)L[(int64_t)(c0 + kk) * ld + c0 + kk];
-          ACC zk = __shfl_sync(0xffffffffu, v, kk);
-          if (lane < kk) v -= (ACC)L[(int64_t)(c0 + lane) * ld + c0 + kk] * zk;
-        }
-        if (lane < bw) xs[(int64_t)r * m + c0 + lane] = v;
+    // diagonal block (transposed): one right-hand side per warp at a time
+    for (int r = warp; r < nrhs; r += nwarps) {
+      ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] - tt[lane][r] : ACC(0);
+      for (int kk = bw - 1; kk >= 0; --kk) {
+        if (lane == kk && !unit) v = v / Ld[kk][kk];
+        ACC zk = __shfl_sync(0xffffffffu, v, kk);
+        if (lane < kk) v -= Ld[lane][kk] * zk;
       }
+      if (lane < bw) xs[(int64_t)r * m + c0 + lane] = v;
     }
     __syncthreads();
   }
@@ -275,6 +285,11 @@ template <typename T, typename ACC>
 __global__ void k_lgather(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
+  if (!fwd && t.r0 == 0) {
+    // both backward accumulators of this front start at zero
+    ACC* tf = a.tt + (int64_t)t.f * 2 * LSOLVE_BW2 * MAXR;
+    for (int e = threadIdx.x; e < 2 * LSOLVE_BW2 * MAXR; e += blockDim.x) tf[e] = ACC(0);
+  }
   const int i = t.r0 + threadIdx.x;
   if (i >= f.m) return;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
@@ -296,7 +311,7 @@ __global__ void k_lscatter(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bo
     const int64_t e = so + (int64_t)r * f.m + i;
     ACC* dst = a.x + (int64_t)r * a.n + v;
     if (i >= f.n) aadd(dst, a.scratch[e]);
-    else *dst = fwd ? a.ys[e] : a.scratch[e];
+    else *dst = a.ys[e];
   }
 }
 
@@ -346,6 +361,7 @@ __global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
                                                 const T* __restrict__ inv64,
                                                 const int64_t* __restrict__ inv_off,
                                                 T* __restrict__ inv2,
+                                                T* __restrict__ inv2t,
                                                 const int64_t* __restrict__ inv2_off) {
   extern __shared__ __align__(16) unsigned char sm_raw[];
   T* As = reinterpret_cast<T*>(sm_raw);  // As[k*65 + r] = A(r, k)
@@ -408,56 +424,129 @@ __global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
       for (int q = 0; q < 16; ++q) X[(int64_t)(LB * j + cq * 16 + q) * BW2 + LB * i + r] = -acc[q];
       __syncthreads();
     }
+  // transposed copy, XT[k*256 + i] = X(k, i), through 64 x 64 shared tiles
+  T* XT = inv2t + inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
+  for (int bj = 0; bj < BW2 / LB; ++bj)
+    for (int bi = 0; bi < BW2 / LB; ++bi) {
+      for (int e = tid; e < LB * LB; e += blockDim.x) {
+        const int rr = e % LB, kk = e / LB;  // X(LB*bi + rr, LB*bj + kk)
+        As[kk * 65 + rr] = X[(int64_t)(LB * bj + kk) * BW2 + LB * bi + rr];
+      }
+      __syncthreads();
+      for (int e = tid; e < LB * LB; e += blockDim.x) {
+        const int kk = e % LB, rr = e / LB;  // XT(LB*bj + kk, LB*bi + rr)
+        XT[(int64_t)(LB * bi + rr) * BW2 + LB * bj + kk] = As[kk * 65 + rr];
+      }
+      __syncthreads();
+    }
 }
 
-// y_b = X_b x_b (forward): thread (row i, half h of the columns), 512 threads
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(512) k_fwd_diag3(const LTask* __restrict__ tasks,
-                                                   LsArgs<T, ACC> a) {
+// Diagonal block of a 256-column solve step, as a product with its explicit
+// inverse, split over gridDim.y = 4 CTAs of 64 output rows:
+//   forward   y_b = X v,    v = xs(block)        -> ys(block)
+//   backward  z_b = X^T v,  v = xs(block) - tt   -> ys(block)
+// Solved rows (< n) live in ys in both directions, so no CTA overwrites
+// values another CTA of the same launch still reads.
+// (X^T read from the transposed copy, so both directions read the matrix
+// coalesced down a column).  Thread (row i, k-phase g) sums k = g (mod 4);
+// the four phases are reduced through shared memory.  The backward step
+// reads accumulator (c0/256)&1 and clears the other one, which the next
+// (lower) block's reduction fills.
+template <typename ACC> struct Vec4;
+template <> struct Vec4<float> {
+  using V = float4;
+  static constexpr int W = 4;
+};
+template <> struct Vec4<double> {
+  using V = double2;
+  static constexpr int W = 2;
+};
+
+template <typename T, typename ACC, bool BWD>
+__global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks,
+                                                 LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
-  __shared__ ACC xb[BW2][RG + 1];
-  __shared__ ACC part[BW2][RG + 1];
+  using V = typename Vec4<ACC>::V;
+  constexpr int VW = Vec4<ACC>::W;
+  __shared__ __align__(16) ACC vb[BW2 * RG];
+  __shared__ ACC part[4][64][RG + 1];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, i = tid % BW2, h = tid / BW2;
+  const int c0 = t.c0, bw = t.bw, i0 = 64 * blockIdx.y;
+  const int tid = threadIdx.x, il = tid & 63, g = tid >> 6, i = i0 + il;
+  const int64_t m = f.m;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  const T* X = a.inv2 + a.inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
-  for (int rg = 0; rg < a.nrhs; rg += RG) {
+  const int64_t moff = a.inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
+  const T* M = (BWD ? a.inv2t : a.inv2) + moff;
+  ACC* tf = a.tt + (int64_t)t.f * 2 * BW2 * MAXR;
+  ACC* tcur = tf + ((c0 / BW2) & 1) * BW2 * MAXR;
+  ACC* tnext = tf + (((c0 / BW2) + 1) & 1) * BW2 * MAXR;
+  // entries k of v this CTA needs
+  const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + 64), nk = khi - klo;
+  // rows [i0, i0+64) beyond the block: nothing to compute (uniform per CTA)
+  for (int rg = 0; rg < (i0 < bw ? a.nrhs : 0); rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
-    for (int e = tid; e < BW2 * RG; e += blockDim.x) {
-      int k = e % BW2, r = e / BW2;
-      xb[k][r] = (k < bw && r < nr) ? xs[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+    __syncthreads();
+    for (int e = tid; e < nk * RG; e += 256) {
+      const int k = klo + e % nk, r = e / nk;
+      ACC v = ACC(0);
+      if (r < nr) {
+        v = xs[(int64_t)(rg + r) * m + c0 + k];
+        if (BWD) v -= tcur[k * MAXR + rg + r];
+      }
+      vb[k * RG + r] = v;
     }
     __syncthreads();
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    const int k0 = h * (BW2 / 2), k1 = min(k0 + BW2 / 2, i + 1);
-#pragma unroll 16
-    for (int k = k0; k < k1; ++k) {
-      const ACC l = (ACC)X[(int64_t)k * BW2 + i];
+    if (i < bw) {
+      const int k0 = BWD ? i : 0, k1 = BWD ? bw : i + 1;
+      const int kst = k0 + ((g - k0) & 3);
+#pragma unroll 4
+      for (int k = kst; k < k1; k += 4) {
+        const ACC l = (ACC)M[(int64_t)k * BW2 + i];
+        const V* vv = reinterpret_cast<const V*>(vb + k * RG);
 #pragma unroll
-      for (int q = 0; q < RG; ++q) acc[q] += l * xb[k][q];
+        for (int q = 0; q < RG / VW; ++q) {
+          const V x4 = vv[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l * x4.x;
+            acc[4 * q + 1] += l * x4.y;
+            acc[4 * q + 2] += l * x4.z;
+            acc[4 * q + 3] += l * x4.w;
+          } else {
+            acc[2 * q + 0] += l * x4.x;
+            acc[2 * q + 1] += l * x4.y;
+          }
+        }
+      }
     }
-    if (h == 1)
 #pragma unroll
-      for (int q = 0; q < RG; ++q) part[i][q] = acc[q];
+    for (int q = 0; q < RG; ++q) part[g][il][q] = acc[q];
     __syncthreads();
-    if (h == 0 && i < bw)
-#pragma unroll
-      for (int q = 0; q < RG; ++q)
-        if (q < nr) ysl[(int64_t)(rg + q) * f.m + c0 + i] = acc[q] + part[i][q];
-    __syncthreads();
+    for (int e = tid; e < 64 * RG; e += 256) {
+      const int rr = e % 64, q = e / 64, ii = i0 + rr;
+      if (ii < bw && q < nr) {
+        ysl[(int64_t)(rg + q) * m + c0 + ii] =
+            part[0][rr][q] + part[1][rr][q] + part[2][rr][q] + part[3][rr][q];
+      }
+    }
   }
+  if (BWD)
+    for (int e = tid; e < 64 * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
 }
 
-// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 32-column group g)
+// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 32-column group g);
+// y is read from shared memory as 16-byte vectors (one broadcast per warp)
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
-  __shared__ ACC yb[BW2][RG];
+  using V = typename Vec4<ACC>::V;
+  constexpr int VW = Vec4<ACC>::W;
+  __shared__ __align__(16) ACC yb[BW2 * RG];
   __shared__ ACC red[8][32][RG + 1];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
@@ -470,31 +559,44 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
     const int nr = min(RG, a.nrhs - rg);
     for (int e = tid; e < BW2 * RG; e += blockDim.x) {
       int k = e % BW2, r = e / BW2;
-      yb[k][r] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+      yb[k * RG + r] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
     }
     __syncthreads();
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
     if (i < f.m) {
-#pragma unroll 16
+#pragma unroll 8
       for (int kk = 0; kk < 32; ++kk) {
         const int k = g * 32 + kk;
         const ACC l = (k < bw) ? (ACC)L[(int64_t)(c0 + k) * f.ld + i] : ACC(0);
+        const V* yv = reinterpret_cast<const V*>(yb + k * RG);
 #pragma unroll
-        for (int q = 0; q < RG; ++q) acc[q] += l * yb[k][q];
+        for (int q = 0; q < RG / VW; ++q) {
+          const V y4 = yv[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l * y4.x;
+            acc[4 * q + 1] += l * y4.y;
+            acc[4 * q + 2] += l * y4.z;
+            acc[4 * q + 3] += l * y4.w;
+          } else {
+            acc[2 * q + 0] += l * y4.x;
+            acc[2 * q + 1] += l * y4.y;
+          }
+        }
       }
     }
 #pragma unroll
     for (int q = 0; q < RG; ++q) red[g][rr][q] = acc[q];
     __syncthreads();
-    if (g == 0 && i < f.m) {
+    // 32 rows x RG sums, spread over all threads
+    for (int e = tid; e < 32 * RG; e += blockDim.x) {
+      const int r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
+      if (i2 < f.m && q < nr) {
+        ACC sum = ACC(0);
 #pragma unroll
-      for (int q = 0; q < RG; ++q) {
-        ACC s = ACC(0);
-#pragma unroll
-        for (int gg = 0; gg < 8; ++gg) s += red[gg][rr][q];
-        if (q < nr) xs[(int64_t)(rg + q) * f.m + i] -= s;
+        for (int gg = 0; gg < 8; ++gg) sum += red[gg][r2][q];
+        xs[(int64_t)(rg + q) * f.m + i2] -= sum;
       }
     }
     __syncthreads();
@@ -507,14 +609,18 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
                                                   LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
   constexpr int SR = sizeof(ACC) == 8 ? 16 : 32;
+  using V = typename Vec4<ACC>::V;
+  constexpr int VW = Vec4<ACC>::W;
   __shared__ ACC Lt[SR][BW2 + 1];
-  __shared__ ACC xt[SR][RG + 1];
+  __shared__ __align__(16) ACC xt[SR][RG];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
   const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  // rows below the block: solved rows (< n) in ys, contribution rows in xs
   const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
-  ACC* tf = a.tt + (int64_t)t.f * BW2 * MAXR;
+  const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
+  ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / BW2) & 1)) * BW2 * MAXR;
   const int rend = min(t.r0 + 64, f.m);
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
@@ -530,14 +636,27 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
       }
       for (int e = tid; e < SR * RG; e += blockDim.x) {
         int ii = e % SR, r = e / SR;
-        xt[ii][r] = (ii < nrow && r < nr) ? xs[(int64_t)(rg + r) * f.m + s0 + ii] : ACC(0);
+        const ACC* src = (s0 + ii < f.n) ? ysl : xs;
+        xt[ii][r] = (ii < nrow && r < nr) ? src[(int64_t)(rg + r) * f.m + s0 + ii] : ACC(0);
       }
       __syncthreads();
 #pragma unroll 8
       for (int ii = 0; ii < SR; ++ii) {
         const ACC l = Lt[ii][tid];
+        const V* xv = reinterpret_cast<const V*>(&xt[ii][0]);
 #pragma unroll
-        for (int q = 0; q < RG; ++q) acc[q] += l * xt[ii][q];
+        for (int q = 0; q < RG / VW; ++q) {
+          const V x4 = xv[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l * x4.x;
+            acc[4 * q + 1] += l * x4.y;
+            acc[4 * q + 2] += l * x4.z;
+            acc[4 * q + 3] += l * x4.w;
+          } else {
+            acc[2 * q + 0] += l * x4.x;
+            acc[2 * q + 1] += l * x4.y;
+          }
+        }
       }
       __syncthreads();
     }
@@ -545,53 +664,6 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
 #pragma unroll
       for (int q = 0; q < RG; ++q)
         if (q < nr) aadd(&tf[tid * MAXR + rg + q], acc[q]);
-  }
-}
-
-// z_b = X_b^T (x_b - tt): warp w computes columns k = w, w+16, ...; lanes
-// run down the column of X (coalesced) and reduce with shuffles
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(512) k_bwd_diag3(const LTask* __restrict__ tasks,
-                                                   LsArgs<T, ACC> a) {
-  constexpr int RG = RGn<ACC>::v;
-  __shared__ ACC vb[BW2][RG + 1];
-  const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = a.fr[t.f];
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
-  ACC* tf = a.tt + (int64_t)t.f * BW2 * MAXR;
-  const T* X = a.inv2 + a.inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
-  for (int rg = 0; rg < a.nrhs; rg += RG) {
-    const int nr = min(RG, a.nrhs - rg);
-    __syncthreads();
-    for (int e = tid; e < BW2 * RG; e += blockDim.x) {
-      int k = e % BW2, r = e / BW2;
-      ACC v = ACC(0);
-      if (k < bw && r < nr) {
-        v = xs[(int64_t)(rg + r) * f.m + c0 + k] - tf[k * MAXR + rg + r];
-        tf[k * MAXR + rg + r] = ACC(0);
-      }
-      vb[k][r] = v;
-    }
-    __syncthreads();
-    for (int k = warp; k < bw; k += 16) {
-      ACC acc[RG];
-#pragma unroll
-      for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-#pragma unroll
-      for (int u = 0; u < BW2 / 32; ++u) {
-        const int i = lane + 32 * u;
-        const ACC l = (i >= k) ? (ACC)X[(int64_t)k * BW2 + i] : ACC(0);
-#pragma unroll
-        for (int q = 0; q < RG; ++q) acc[q] += l * vb[i][q];
-      }
-#pragma unroll
-      for (int q = 0; q < RG; ++q) {
-        ACC s = acc[q];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0 && q < nr) xs[(int64_t)(rg + q) * f.m + c0 + k] = s;
-      }
-    }
   }
 }
 
@@ -687,7 +759,7 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
       k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
     case LS_FWD_DIAG2:
-      k_fwd_diag3<T, ACC><<<ntask, 512, 0, s>>>(tasks, a);
+      k_diag_mv<T, ACC, false><<<dim3(ntask, BW2 / 64), 256, 0, s>>>(tasks, a);
       break;
     case LS_FWD_UPD2:
       k_fwd_upd3<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
@@ -696,7 +768,7 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
       k_bwd_red3<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
       break;
     case LS_BWD_DIAG2:
-      k_bwd_diag3<T, ACC><<<ntask, 512, 0, s>>>(tasks, a);
+      k_diag_mv<T, ACC, true><<<dim3(ntask, BW2 / 64), 256, 0, s>>>(tasks, a);
       break;
   }
 }
@@ -716,20 +788,20 @@ void prepare_solve_kernels() {
 
 template <typename T>
 void launch_inv256(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
-                   const T* inv64, const int64_t* inv_off, T* inv2, const int64_t* inv2_off,
-                   cudaStream_t s) {
+                   const T* inv64, const int64_t* inv_off, T* inv2, T* inv2t,
+                   const int64_t* inv2_off, cudaStream_t s) {
   if (ntask <= 0) return;
   k_inv256<T><<<ntask, 256, 2 * 64 * 65 * sizeof(T), s>>>(arena, fr, tasks, inv64, inv_off,
-                                                           inv2, inv2_off);
+                                                           inv2, inv2t, inv2_off);
 }
 template void prepare_solve_kernels<float>();
 template void prepare_solve_kernels<double>();
 template void launch_inv256<float>(const float*, const FrontDesc*, const LTask*, int,
-                                   const float*, const int64_t*, float*, const int64_t*,
-                                   cudaStream_t);
+                                   const float*, const int64_t*, float*, float*,
+                                   const int64_t*, cudaStream_t);
 template void launch_inv256<double>(const double*, const FrontDesc*, const LTask*, int,
-                                    const double*, const int64_t*, double*, const int64_t*,
-                                    cudaStream_t);
+                                    const double*, const int64_t*, double*, double*,
+                                    const int64_t*, cudaStream_t);
 
 template void launch_lsolve<float, float>(int, const LTask*, int, LsArgs<float, float>,
                                           cudaStream_t);

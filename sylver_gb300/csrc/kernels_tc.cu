@@ -365,26 +365,38 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                  : "memory");
 }
 
-// Transposed, hi/lo-split copy of rows [n, m) x cols [0, K) of one front into
-// the stacked panel buffer: out[(base + i - n) * pitch + k]; columns
-// [K, pitch) are zero.  One thread per (row, k) pair, k fastest in a warp for
-// coalesced writes; reads are strided (one column per k) but each front row
-// block is read once.
-__global__ void k_split_t(const float* __restrict__ arena, const TcSplit* __restrict__ sp,
-                          float* __restrict__ hi, float* __restrict__ lo, int pitch) {
-  const TcSplit t = sp[blockIdx.y];
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Transposed, hi/lo-split copy of rows [n, m) x cols [c0, c0 + K) of one
+// front into the stacked panel buffer: out[(base + i - n) * pitch + k];
+// columns [K, pitch) are zero.  A 32 x 32 tile per CTA (32 x 8 threads)
+// goes through shared memory, so both the column reads from the front and
+// the row writes to the panel are coalesced.
+__global__ void __launch_bounds__(256) k_split_t(const float* __restrict__ arena,
+                                                 const TcSplit* __restrict__ sp,
+                                                 float* __restrict__ hi, float* __restrict__ lo,
+                                                 int pitch) {
+  __shared__ float tile[32][33];  // tile[k][i]
+  const TcSplit t = sp[blockIdx.z];
   const int rows = t.m - t.n;
-  if (e >= (int64_t)rows * pitch) return;
-  const int i = (int)(e / pitch), k = (int)(e % pitch);
-  float v = 0.f;
-  if (k < t.K) v = arena[t.off + (int64_t)k * t.ld + t.n + i];
-  uint32_t h;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-  const float fh = __uint_as_float(h);
-  const int64_t o = (int64_t)(t.base + i) * pitch + k;
-  hi[o] = fh;
-  lo[o] = v - fh;
+  const int i0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  if (i0 >= rows) return;  // uniform over the CTA
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int kk = ty; kk < 32; kk += 8) {
+    const int k = k0 + kk, i = i0 + tx;
+    tile[kk][tx] = (k < t.K && i < rows)
+                       ? arena[t.off + (int64_t)(t.c0 + k) * t.ld + t.n + i] : 0.f;
+  }
+  __syncthreads();
+  for (int ii = ty; ii < 32; ii += 8) {
+    const int i = i0 + ii;
+    if (i >= rows) break;
+    const float v = tile[tx][ii];
+    uint32_t h;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+    const float fh = __uint_as_float(h);
+    const int64_t o = (int64_t)(t.base + i) * pitch + k0 + tx;
+    hi[o] = fh;
+    lo[o] = v - fh;
+  }
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -425,10 +437,11 @@ void make_panel_map(CUtensorMap* map, const float* base, int64_t rows, int pitch
   if (r != CUDA_SUCCESS) throw CudaError("cuTensorMapEncodeTiled failed");
 }
 
-void launch_split_t(const float* arena, const TcSplit* sp, int nsplit, int64_t max_elems,
+void launch_split_t(const float* arena, const TcSplit* sp, int nsplit, int64_t max_rows,
                     float* hi, float* lo, int pitch, cudaStream_t s) {
-  if (nsplit <= 0 || max_elems <= 0) return;
-  dim3 grid((unsigned)((max_elems + 255) / 256), (unsigned)nsplit);
+  if (nsplit <= 0 || max_rows <= 0) return;
+  // pitch is a multiple of 32: every k of a tile lies inside the row
+  dim3 grid((unsigned)((max_rows + 31) / 32), (unsigned)(pitch / 32), (unsigned)nsplit);
   k_split_t<<<grid, 256, 0, s>>>(arena, sp, hi, lo, pitch);
 }
 

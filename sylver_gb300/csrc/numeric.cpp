@@ -48,6 +48,7 @@ bool Runtime::init() {
     prepare_factor_kernels<float>();
     prepare_factor_kernels<double>();
     prepare_tc_kernels();
+    prepare_blocked_kernels();
     prepare_solve_kernels<float>();
     prepare_solve_kernels<double>();
   } catch (const std::exception& ex) {
@@ -207,7 +208,10 @@ void FKeep::plan_cholesky() {
   std::vector<TcSplit> tcs;
   std::vector<TcTask> tct;
   std::vector<double> tc_flops;
+  std::vector<BlkTask> blkd, blkp;
   tclev.clear();
+  blkinv_count = 0;
+  const int PW = (f32 && use_tc) ? sched.panel_cols() : 0;
   std::vector<int> pos(st.n, -1);
   ops.clear();
   ops.push_back({Op::MEMSET, 0, 0, 0});
@@ -252,7 +256,61 @@ void FKeep::plan_cholesky() {
     if ((int64_t)smalls.size() > s0) ops.push_back({Op::SMALL, s0, (int64_t)smalls.size(), maxm});
     // large fronts: panel steps over the fully-summed columns, batched
     int maxsteps = 0;
-    for (int s : large) maxsteps = std::max(maxsteps, (st.ncol[s] + NB - 1) / NB);
+    if (PW > 0) {
+      // blocked path: 64-column steps inside outer panels of PW columns; the
+      // trailing fully-summed columns are updated once per outer panel on
+      // the tensor cores
+      int maxn = 0;
+      for (int s : large) maxn = std::max(maxn, st.ncol[s]);
+      for (int k0 = 0; k0 < maxn; k0 += PW) {
+        for (int c = k0; c < k0 + PW && c < maxn; c += BLK_B) {
+          const int64_t d0 = (int64_t)blkd.size(), p0 = (int64_t)blkp.size();
+          for (int s : large) {
+            const int m = st.nrow[s], n = st.ncol[s];
+            if (c >= n) continue;
+            const int pend = std::min(k0 + PW, n);
+            const int bw = std::min(BLK_B, pend - c);
+            const int xi = (int)((int64_t)blkd.size() - d0);
+            blkd.push_back({off[s], ld[s], m, c, bw, pend, 0, xi, 0});
+            for (int r0 = c + bw; r0 < m; r0 += BLK_B)
+              blkp.push_back({off[s], ld[s], m, c, bw, pend, r0, xi, 0});
+          }
+          if ((int64_t)blkd.size() > d0) {
+            ops.push_back({Op::BDIAG, d0, (int64_t)blkd.size(), 0});
+            blkinv_count = std::max(blkinv_count, (int64_t)blkd.size() - d0);
+          }
+          if ((int64_t)blkp.size() > p0) ops.push_back({Op::BPANEL, p0, (int64_t)blkp.size(), 0});
+        }
+        const int p = k0 + PW;
+        std::vector<int> tf;
+        for (int s : large)
+          if (p < st.ncol[s]) tf.push_back(s);
+        if (tf.empty()) continue;
+        int64_t rows = 0, mxr = 0;
+        double fl = 0.0;
+        const int64_t sp0 = (int64_t)tcs.size(), tk0 = (int64_t)tct.size();
+        for (int s : tf) {
+          const int m = st.nrow[s], n = st.ncol[s];
+          tcs.push_back({off[s], ld[s], m, p, PW, (int)rows, k0});
+          for (int col0 = p; col0 < n; col0 += 128)
+            for (int row0 = col0; row0 < m; row0 += 128)
+              tct.push_back({off[s], ld[s], row0, col0, m, n, (int)rows + row0 - p,
+                             (int)rows + col0 - p, PW / 32});
+          mxr = std::max<int64_t>(mxr, m - p);
+          rows += m - p;
+          // lower-triangle entries of rows [p, m) x cols [p, n), times 2K
+          const double cnt = (double)(n - p) * m - (0.5 * n * (n - 1.0) - 0.5 * p * (p - 1.0));
+          fl += 2.0 * PW * cnt;
+        }
+        const int lvl = (int)tclev.size();
+        tclev.push_back({PW, rows, mxr});
+        tc_flops.push_back(fl);
+        ops.push_back({Op::SPLIT, sp0, (int64_t)tcs.size(), lvl});
+        ops.push_back({Op::TCUPD, tk0, (int64_t)tct.size(), lvl});
+      }
+    } else {
+      for (int s : large) maxsteps = std::max(maxsteps, (st.ncol[s] + NB - 1) / NB);
+    }
     for (int step = 0; step < maxsteps; ++step) {
       int64_t p0 = (int64_t)panels.size(), u0 = (int64_t)upds.size();
       int64_t d0 = (int64_t)diags.size();
@@ -305,7 +363,7 @@ void FKeep::plan_cholesky() {
           for (int ri = cj; ri * 128 < m - n; ++ri)
             tct.push_back({off[s], ld[s], n + ri * 128, n + cj * 128, m, m,
                            (int)rows + ri * 128, (int)rows + cj * 128, (n + 31) / 32});
-        mx = std::max(mx, (int64_t)(m - n) * pitch);
+        mx = std::max(mx, (int64_t)(m - n));
         rows += m - n;
       }
       int lvl = (int)tclev.size();
@@ -351,6 +409,8 @@ void FKeep::plan_cholesky() {
   diagt.upload(diags, s);
   tcsplit.upload(tcs, s);
   tctask.upload(tct, s);
+  blkdiag.upload(blkd, s);
+  blkpanel.upload(blkp, s);
   upd.upload(upds, s);
   dfr.upload(hfr, s);
   dscr.upload(hscr, s);
@@ -381,8 +441,10 @@ void FKeep::upload_static(cudaStream_t s) {
     const size_t es = precision == 1 ? sizeof(float) : sizeof(double);
     splan.inv.ensure((size_t)std::max<int64_t>(splan.inv_elems, 1) * es);
     splan.inv2.ensure((size_t)std::max<int64_t>(splan.inv2_elems, 1) * es);
+    splan.inv2t.ensure((size_t)std::max<int64_t>(splan.inv2_elems, 1) * es);
   }
   tcerr.ensure(sizeof(unsigned));
+  if (blkinv_count > 0) blkinv.ensure((size_t)blkinv_count * BLK_B * BLK_B * sizeof(float));
   if (!tclev.empty()) {
     int64_t cap = 0;
     for (auto& L : tclev) cap = std::max(cap, L.rows * L.pitch);
@@ -432,8 +494,16 @@ void FKeep::run_ops(cudaStream_t s) {
         break;
       case Op::SPLIT:
         if constexpr (std::is_same<T, float>::value)
-          launch_split_t(A, tcsplit.as<TcSplit>() + op.a, (int)cnt, tclev[op.aux].max_elems,
+          launch_split_t(A, tcsplit.as<TcSplit>() + op.a, (int)cnt, tclev[op.aux].max_rows,
                          panel_hi.as<float>(), panel_lo.as<float>(), tclev[op.aux].pitch, s);
+        break;
+      case Op::BDIAG:
+        if constexpr (std::is_same<T, float>::value)
+          launch_blk_diag(A, blkdiag.as<BlkTask>() + op.a, (int)cnt, blkinv.as<float>(), stp, s);
+        break;
+      case Op::BPANEL:
+        if constexpr (std::is_same<T, float>::value)
+          launch_blk_panel(A, blkpanel.as<BlkTask>() + op.a, (int)cnt, blkinv.as<float>(), s);
         break;
       case Op::TCUPD:
         if constexpr (std::is_same<T, float>::value)
@@ -646,10 +716,12 @@ template <typename T>
 void SolvePlan::compute_inverses(const T* arena, const FrontDesc* dfr, bool unit, cudaStream_t s) {
   inv.ensure((size_t)std::max<int64_t>(inv_elems, 1) * sizeof(T));
   inv2.ensure((size_t)std::max<int64_t>(inv2_elems, 1) * sizeof(T));
+  inv2t.ensure((size_t)std::max<int64_t>(inv2_elems, 1) * sizeof(T));
   launch_inv_diag<T>(arena, dfr, invt.as<LTask>(), (int)hinv.size(), inv.as<T>(),
                      inv_off.as<int64_t>(), unit, s);
   launch_inv256<T>(arena, dfr, invt2.as<LTask>(), (int)hinv2.size(), inv.as<T>(),
-                   inv_off.as<int64_t>(), inv2.as<T>(), inv2_off.as<int64_t>(), s);
+                   inv_off.as<int64_t>(), inv2.as<T>(), inv2t.as<T>(), inv2_off.as<int64_t>(),
+                   s);
 }
 template void SolvePlan::compute_inverses<float>(const float*, const FrontDesc*, bool,
                                                  cudaStream_t);
@@ -658,7 +730,7 @@ template void SolvePlan::compute_inverses<double>(const double*, const FrontDesc
 
 void SolvePlan::ensure_tt(size_t elem, int64_t scratch_elems) {
   const void* before = tt.p;
-  tt.ensure((size_t)std::max(max_large, 1) * LSOLVE_BW2 * 32 * elem);
+  tt.ensure((size_t)std::max(max_large, 1) * 2 * LSOLVE_BW2 * 32 * elem);
   // the backward steps leave the accumulators zero; a new buffer starts zero
   if (tt.p != before) SG_CUDA(cudaMemset(tt.p, 0, tt.bytes));
   ys.ensure((size_t)std::max<int64_t>(scratch_elems, 1) * elem);
@@ -679,7 +751,7 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
     }
     LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),
                      inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), cnt.as<unsigned>(),
-                     inv2.as<T>(), inv2_off.as<int64_t>() + v.f0};
+                     inv2.as<T>(), inv2_off.as<int64_t>() + v.f0, inv2t.as<T>()};
     for (const SOp& op : fwd ? v.fwd : v.bwd)
       launch_lsolve<T, ACC>(op.kind, tasks.as<LTask>() + op.a, (int)(op.b - op.a), a, s);
   };

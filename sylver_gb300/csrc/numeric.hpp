@@ -8,6 +8,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <memory>
 #include <string>
@@ -54,12 +55,20 @@ struct Schedule {
   int tc_min_cb_rows = 0;    // FP32 Cholesky: CB rows for the tensor-core update (<0: never)
   int solve_large_cols = 0;  // fronts with >= eliminated columns use the blocked solve
   int ldlt_tpp_cols = 0;     // LDL^T: fronts with <= fully-summed columns use TPP only
+  int fs_panel_cols = 0;     // FP32 Cholesky: outer panel width of the blocked large-front
+                             // path (multiple of 64, <= 256; <0: 64-column SIMT steps)
   static Schedule& current();
   int small_rows(int compiled_max) const {
     return small_front_rows > 0 ? std::min(small_front_rows, compiled_max) : compiled_max;
   }
   int tc_rows() const { return tc_min_cb_rows == 0 ? 64 : tc_min_cb_rows; }
   int solve_cols() const { return solve_large_cols > 0 ? solve_large_cols : 96; }
+  // 0: legacy SIMT panel steps, else the outer panel width
+  int panel_cols() const {
+    if (fs_panel_cols < 0) return 0;
+    if (fs_panel_cols == 0) return BLK_W;
+    return std::max(BLK_B, std::min(BLK_W, fs_panel_cols / BLK_B * BLK_B));
+  }
 };
 
 // Process-wide device context: device 0, one non-blocking stream.
@@ -89,7 +98,7 @@ struct AKeep {
 
 // One kernel launch of the factor schedule.
 struct Op {
-  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV, SPLIT, TCUPD } kind;
+  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV, SPLIT, TCUPD, BDIAG, BPANEL } kind;
   int64_t a = 0, b = 0;  // task range [a, b)
   int aux = 0;           // SMALL: max front rows; SPLIT/TCUPD: tensor-core level
 };
@@ -118,7 +127,7 @@ struct SolvePlan {
   std::vector<LTask> hinv2;       // 256-column diagonal blocks (f = level-ordered index)
   std::vector<int64_t> hinv2_off;
   int64_t inv2_elems = 0;
-  DevMem tasks, tt, cnt, ys, inv, invt, inv_off, inv2, invt2, inv2_off;
+  DevMem tasks, tt, cnt, ys, inv, invt, inv_off, inv2, inv2t, invt2, inv2_off;
   int max_large = 0;
   // Invert every diagonal block of the large fronts (after a factorization).
   template <typename T>
@@ -153,11 +162,15 @@ struct FKeep {
   bool use_tc = true;
   struct TcLevel {
     int pitch;
-    int64_t rows, max_elems;
+    int64_t rows, max_rows;  // stacked panel rows; most rows of one split
   };
   std::vector<TcLevel> tclev;
   std::vector<CUtensorMap> tmap_hi, tmap_lo;
   DevMem tcsplit, tctask, panel_hi, panel_lo, tcerr;
+  // blocked large-front path (FP32): diagonal-block and panel tasks, and the
+  // 64 x 64 inverses of one diagonal-block launch
+  DevMem blkdiag, blkpanel, blkinv;
+  int64_t blkinv_count = 0;
 
   // host plan
   std::vector<int> order;            // level-ordered front indices

@@ -16,17 +16,17 @@ struct TcTask {
   int ldc, row0, col0, rowEnd, colEnd, a_row, b_row, nk;
 };
 
-// Transposed hi/lo copy of front rows [n, m) x columns [0, K) into stacked
-// panel rows [base, base + m - n).
+// Transposed hi/lo copy of front rows [n, m) x columns [c0, c0 + K) into
+// stacked panel rows [base, base + m - n).
 struct TcSplit {
   int64_t off;
-  int ld, m, n, K, base, pad;
+  int ld, m, n, K, base, c0;
 };
 
 size_t tc_smem_bytes();
 void prepare_tc_kernels();
 void make_panel_map(CUtensorMap* map, const float* base, int64_t rows, int pitch);
-void launch_split_t(const float* arena, const TcSplit* sp, int nsplit, int64_t max_elems,
+void launch_split_t(const float* arena, const TcSplit* sp, int nsplit, int64_t max_rows,
                     float* hi, float* lo, int pitch, cudaStream_t s);
 void launch_update_tc(const CUtensorMap& hi, const CUtensorMap& lo, float* arena,
                       const TcTask* t, int ntask, unsigned* err, cudaStream_t s);

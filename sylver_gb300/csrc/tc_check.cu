@@ -41,7 +41,7 @@ extern "C" int sylver_gb300_tc_selfcheck(int rows, int k, double* max_rel_err) {
     CUtensorMap mhi, mlo;
     make_panel_map(&mhi, hi.as<float>(), rows, pitch);
     make_panel_map(&mlo, lo.as<float>(), rows, pitch);
-    launch_split_t(arena.as<float>(), sp.as<TcSplit>(), 1, (int64_t)rows * pitch, hi.as<float>(),
+    launch_split_t(arena.as<float>(), sp.as<TcSplit>(), 1, (int64_t)rows, hi.as<float>(),
                    lo.as<float>(), pitch, rt.stream);
     launch_update_tc(mhi, mlo, arena.as<float>(), tk.as<TcTask>(), (int)ht.size(),
                      err.as<unsigned>(), rt.stream);

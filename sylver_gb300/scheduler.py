@@ -44,10 +44,10 @@ HIDDEN = 64
 
 def kkt_instance(seed):
     """Training / evaluation instance of the saddle-point family: H a 7-point
-    Laplacian on k^3 with k ~ U{12..24}, B with n_H/4 rows of 4 N(0,1)
+    Laplacian on k^3 with k ~ U{8..16}, B with n_H/4 rows of 4 N(0,1)
     entries, delta = 1e-8 (the 40^3 configuration at small scale)."""
     rng = np.random.default_rng(seed)
-    k = int(rng.integers(12, 25))
+    k = int(rng.integers(8, 17))
     return w.kkt(k, nnz_per_row=4, delta=1e-8, seed=seed, nrhs=1)
 
 
@@ -226,6 +226,9 @@ def record(out, count=200, seed0=100):
             meta.append((s, c, ms))
         print(f"seed {s} n={p.a.n} base {base_ms:.2f} ms delays {delays} "
               f"({time.time() - t0:.0f}s)", flush=True)
+        if (s - seed0) % 20 == 19:  # keep what was recorded so far
+            np.savez_compressed(out, x=np.array(rows_x, np.float32),
+                                y=np.array(rows_y, np.float32), meta=np.array(meta))
     np.savez_compressed(out, x=np.array(rows_x, np.float32), y=np.array(rows_y, np.float32),
                         meta=np.array(meta))
 

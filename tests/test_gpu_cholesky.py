@@ -143,3 +143,61 @@ def test_trivial_sizes(sylver, gpu):
     d = np.arange(1.0, n + 1)
     f = sylver.Factor(an, True, d)
     np.testing.assert_allclose(f.solve(np.ones((n, 1)))[:, 0], 1.0 / d, rtol=1e-15)
+
+
+def _dense_spd(n, seed):
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    g = rng.standard_normal((n, n))
+    a = g @ g.T / n + np.eye(n)
+    return w.SymMatrix.from_scipy(sp.csc_matrix(a)), a
+
+
+@pytest.mark.parametrize("width", [64, 128, 192, 256, -1])
+def test_fp32_panel_widths(sylver, orc, gpu, width):
+    """Blocked FP32 large-front path: every outer panel width (and the
+    64-column SIMT path, width < 0) gives FP32-accurate factors, and FP64
+    refinement reaches the 1e-14 backward error.  One dense 700 x 700 front
+    (11 diagonal blocks, the last one ragged) and a 3D grid whose separators
+    exceed one panel."""
+    sylver.set_schedule(fs_panel_cols=width)
+    try:
+        a, dense = _dense_spd(700, 3)
+        rng = np.random.default_rng(4)
+        b = rng.standard_normal((700, 2))
+        an = sylver.Analysis(a.n, a.ptr, a.row)
+        assert an.inform.maxfront >= 600
+        f = sylver.Factor(an, True, a.val, precision=sylver.FP32, ir_max_iter=0)
+        assert f.flag == 0
+        x0 = f.solve(b)
+        xt = np.linalg.solve(dense, b)
+        assert np.abs(x0 - xt).max() <= 1e-4 * np.abs(xt).max()
+        f2 = sylver.Factor(an, True, a.val, precision=sylver.FP32, ir_max_iter=10)
+        x = f2.solve(b)
+        assert np.abs(x - xt).max() <= 1e-12 * np.abs(xt).max()
+        p = w.lognormal27(22, nrhs=2)
+        an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+        assert an.inform.maxfront > 256
+        f = sylver.Factor(an, True, p.a.val, precision=sylver.FP32, ir_max_iter=10)
+        assert f.flag == 0
+        x = f.solve(p.rhs)
+        full = p.a.to_scipy_full()
+        assert w.backward_error(full, x, p.rhs).max() <= 1e-14, f.solve_stats()
+        o = orc.OracleFactor(True, an.symbolic(), p.a.val)
+        xo = o.solve(p.rhs)
+        xo = xo + o.solve(p.rhs - full @ xo)
+        assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
+    finally:
+        sylver.set_schedule()
+
+
+def test_fp32_blocked_not_posdef(sylver, gpu):
+    """A non-positive pivot inside a blocked diagonal block is reported."""
+    a, dense = _dense_spd(400, 5)
+    dense = dense.copy()
+    dense[300, 300] = -50.0
+    import scipy.sparse as sp
+    m = w.SymMatrix.from_scipy(sp.csc_matrix(dense))
+    an = sylver.Analysis(m.n, m.ptr, m.row)
+    f = sylver.Factor(an, True, m.val, precision=sylver.FP32)
+    assert f.flag == -6
