@@ -31,6 +31,23 @@ enum : unsigned {
   ST_TIMEOUT = 32u,       // a bounded wait inside a kernel gave up
 };
 
+// Asynchronous global -> shared copy of one element (cp.async, 4/8 bytes):
+// every copy a thread issued lands once it passes cp_async_wait_all(); a
+// __syncthreads() afterwards makes them visible to the whole CTA.  Lets a
+// thread keep many loads in flight instead of one per loop iteration.
+template <typename T>
+__device__ __forceinline__ void cp_async(T* smem, const T* gmem) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "cp.async element size");
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Task descriptors (one per CTA unless stated).
 

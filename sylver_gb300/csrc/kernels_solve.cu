@@ -504,21 +504,31 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
     if (i < bw) {
       const int k0 = BWD ? i : 0, k1 = BWD ? bw : i + 1;
       const int kst = k0 + ((g - k0) & 3);
-#pragma unroll 4
-      for (int k = kst; k < k1; k += 4) {
-        const ACC l = (ACC)M[(int64_t)k * BW2 + i];
-        const V* vv = reinterpret_cast<const V*>(vb + k * RG);
+      // batches of 16 matrix entries in flight per thread
+      for (int kb = kst; kb < k1; kb += 64) {
+        ACC lb[16];
 #pragma unroll
-        for (int q = 0; q < RG / VW; ++q) {
-          const V x4 = vv[q];
-          if constexpr (VW == 4) {
-            acc[4 * q + 0] += l * x4.x;
-            acc[4 * q + 1] += l * x4.y;
-            acc[4 * q + 2] += l * x4.z;
-            acc[4 * q + 3] += l * x4.w;
-          } else {
-            acc[2 * q + 0] += l * x4.x;
-            acc[2 * q + 1] += l * x4.y;
+        for (int u = 0; u < 16; ++u) {
+          const int k = kb + 4 * u;
+          lb[u] = k < k1 ? (ACC)M[(int64_t)k * BW2 + i] : ACC(0);
+        }
+#pragma unroll
+        for (int u = 0; u < 16; ++u) {
+          const int k = min(kb + 4 * u, k1 - 1);  // l = 0 beyond k1; v is finite there
+          const ACC l = lb[u];
+          const V* vv = reinterpret_cast<const V*>(vb + k * RG);
+#pragma unroll
+          for (int q = 0; q < RG / VW; ++q) {
+            const V x4 = vv[q];
+            if constexpr (VW == 4) {
+              acc[4 * q + 0] += l * x4.x;
+              acc[4 * q + 1] += l * x4.y;
+              acc[4 * q + 2] += l * x4.z;
+              acc[4 * q + 3] += l * x4.w;
+            } else {
+              acc[2 * q + 0] += l * x4.x;
+              acc[2 * q + 1] += l * x4.y;
+            }
           }
         }
       }
@@ -566,10 +576,16 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
     if (i < f.m) {
-#pragma unroll 8
+      ACC lb[32];
+#pragma unroll
       for (int kk = 0; kk < 32; ++kk) {
         const int k = g * 32 + kk;
-        const ACC l = (k < bw) ? (ACC)L[(int64_t)(c0 + k) * f.ld + i] : ACC(0);
+        lb[kk] = (k < bw) ? (ACC)L[(int64_t)(c0 + k) * f.ld + i] : ACC(0);
+      }
+#pragma unroll
+      for (int kk = 0; kk < 32; ++kk) {
+        const int k = g * 32 + kk;
+        const ACC l = lb[kk];
         const V* yv = reinterpret_cast<const V*>(yb + k * RG);
 #pragma unroll
         for (int q = 0; q < RG / VW; ++q) {
@@ -629,16 +645,22 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
     for (int s0 = t.r0; s0 < rend; s0 += SR) {
       const int nrow = min(SR, rend - s0);
-#pragma unroll 4
       for (int e = tid; e < SR * BW2; e += blockDim.x) {
         int ii = e % SR, kk = e / SR;
-        Lt[ii][kk] = (ii < nrow && kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * f.ld + s0 + ii] : ACC(0);
+        if constexpr (sizeof(T) == sizeof(ACC)) {
+          if (ii < nrow && kk < bw) cp_async(&Lt[ii][kk], reinterpret_cast<const ACC*>(
+                                                              &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]));
+          else Lt[ii][kk] = ACC(0);
+        } else {
+          Lt[ii][kk] = (ii < nrow && kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * f.ld + s0 + ii] : ACC(0);
+        }
       }
       for (int e = tid; e < SR * RG; e += blockDim.x) {
         int ii = e % SR, r = e / SR;
         const ACC* src = (s0 + ii < f.n) ? ysl : xs;
         xt[ii][r] = (ii < nrow && r < nr) ? src[(int64_t)(rg + r) * f.m + s0 + ii] : ACC(0);
       }
+      cp_async_wait_all();
       __syncthreads();
 #pragma unroll 8
       for (int ii = 0; ii < SR; ++ii) {

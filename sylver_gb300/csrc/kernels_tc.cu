@@ -3,12 +3,13 @@
 // tensor memory and operands staged by TMA.
 //
 // Accuracy: 4xTF32.  Each operand is split into hi = rna_tf32(x) and
-// lo = x - hi (both FP32 containers), and
-// C -= Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T + Alo Blo^T accumulates in FP32: the
-// products are within FP32 rounding of the exact ones, which keeps iterative
-// refinement converging as for SIMT FP32 factors.  (Dropping lo*lo, the usual
-// 3xTF32, cost one extra refinement iteration on the 80^3 workload; the
-// kernel is operand-bound, so the fourth MMA is nearly free.)
+// lo = rna_tf32(x - hi), and C -= Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T +
+// Alo Blo^T: the products are within FP32 rounding of the exact ones.  The
+// tensor-core accumulator does not round to nearest, so its error over a long
+// k range grows linearly (measured: 16x an FP32 dot product at k = 4096); the
+// accumulator is therefore drained into FP32 registers after every 32-wide k
+// chunk and the chunks are summed there, which brings the update to FP32
+// accuracy and lets FP64 refinement converge as for SIMT FP32 factors.
 //
 // Operand layout: TF32 MMAs read K-major shared-memory tiles, so A and B come
 // from a transposed copy of the contribution rows of L ("panel rows", one row
@@ -20,8 +21,10 @@
 // A persistent CTA per SM walks the level's 128 x 128 tiles (10 warps): a TMA
 // producer, an MMA issuer (16 MMAs per 32-wide k chunk; tcgen05.commit
 // releases a stage and signals an accumulator) and eight epilogue warps that
-// tcgen05.ld their 32 TMEM lanes and apply C -= acc while the next tile's
-// MMAs run in the other accumulator.
+// tcgen05.ld their 32 TMEM lanes after every chunk and subtract it from the
+// C values they hold in registers while the next chunks' MMAs run in the
+// other three accumulators of a four-deep TMEM ring; C is written once per
+// tile.
 // Every mbarrier wait is bounded: on timeout the CTA records an error bit,
 // skips the epilogue, waits (bounded) for its own copies and frees TMEM.
 #include <cuda.h>
@@ -158,7 +161,8 @@ constexpr int TC_EPI_WARP0 = 2;                  // warps 2..9 run the epilogue
 constexpr int TC_EPI_WARPS = 8;                  // two per TMEM lane quarter
 constexpr int TC_EPI_COLS = TC_N / 2;            // columns per epilogue thread
 constexpr int TC_THREADS = 32 * (TC_EPI_WARP0 + TC_EPI_WARPS);
-constexpr int TC_TMEM_COLS = 2 * TC_N;           // two accumulators (double buffer)
+constexpr int TC_NACC = 4;                       // accumulators in the TMEM ring
+constexpr int TC_TMEM_COLS = TC_NACC * TC_N;     // all 512 TMEM columns
 
 // arrive on an mbarrier (one arrival)
 __device__ __forceinline__ void mbar_arrive(uint64_t* b) {
@@ -183,12 +187,14 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* b, uint32_t parity,
 
 // Persistent: CTA b processes tiles b, b + gridDim.x, ...
 //   warp 0 lane 0 : TMA producer over a TC_STAGES ring shared by all tiles,
-//   warp 1 lane 0 : MMA issuer; tile i accumulates in TMEM columns
-//                   [(i & 1) * 128, +128) so the epilogue of tile i overlaps
-//                   the MMAs of tile i + 1,
+//   warp 1 lane 0 : MMA issuer; k chunk i (counted over all tiles of the
+//                   CTA) accumulates in TMEM columns [(i % 4) * 128, +128) so
+//                   the epilogue's read of chunk i overlaps the MMAs of the
+//                   next three chunks,
 //   warps 2..9    : epilogue; each thread owns half a row of the tile, loads
-//                   its 64 C values before the accumulator is ready, then
-//                   C -= acc and releases the accumulator.
+//                   its 64 C values before the first chunk is ready,
+//                   subtracts every chunk, releases the accumulator after
+//                   each, and stores C after the tile's last chunk.
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_update_tc(const __grid_constant__ CUtensorMap map_hi,
                 const __grid_constant__ CUtensorMap map_lo, float* __restrict__ arena,
@@ -196,7 +202,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1 KiB alignment for the swizzled tiles
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], acc_full[2], acc_empty[2], done;
+  __shared__ uint64_t full[TC_STAGES], empty[TC_STAGES], acc_full[TC_NACC], acc_empty[TC_NACC],
+      done;
   __shared__ uint32_t tmem_slot;
   __shared__ int abort_flag;
   volatile int* abortp = &abort_flag;
@@ -208,7 +215,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], 1);
     }
-    for (int a = 0; a < 2; ++a) {
+    for (int a = 0; a < TC_NACC; ++a) {
       mbar_init(&acc_full[a], 1);
       mbar_init(&acc_empty[a], TC_EPI_WARPS);  // one arrival per epilogue warp
     }
@@ -257,23 +264,26 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   } else if (warp == 1) {
     if (lane == 0) {
       const uint32_t idesc = tf32_idesc();
-      int g = 0, it = 0;
-      for (int ti = blockIdx.x; ti < ntask; ti += gridDim.x, ++it) {
-        const int a = it & 1;
-        // accumulator a was last used by tile it - 2: wait for its epilogue
-        if (it >= 2 && !mbar_wait_or_abort(&acc_empty[a], ((it >> 1) - 1) & 1, err, abortp))
-          break;
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      int g = 0, it = 0;  // it counts accumulator uses (one per k chunk)
+      bool ok = true;
+      for (int ti = blockIdx.x; ti < ntask && ok; ti += gridDim.x) {
         const int nk = tasks[ti].nk;
-        const uint32_t d = tmem + (uint32_t)(a * TC_N);
-        bool ok = true;
-        for (int kc = 0; kc < nk; ++kc, ++g) {
+        for (int kc = 0; kc < nk; ++kc, ++g, ++it) {
+          const int a = it % TC_NACC;
+          // accumulator a was last used by chunk it - TC_NACC: wait until the
+          // epilogue has read it
+          if (it >= TC_NACC &&
+              !mbar_wait_or_abort(&acc_empty[a], ((it / TC_NACC) - 1) & 1, err, abortp)) {
+            ok = false;
+            break;
+          }
           const int s = g % TC_STAGES;
           if (!mbar_wait_or_abort(&full[s], (g / TC_STAGES) & 1, err, abortp)) {
             ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t d = tmem + (uint32_t)(a * TC_N);
           unsigned char* st = smem + s * STAGE_BYTES;
           const uint64_t ahi = sw128_desc(su32(st + 0 * TILE_BYTES));
           const uint64_t alo = sw128_desc(su32(st + 1 * TILE_BYTES));
@@ -281,29 +291,31 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           const uint64_t blo = sw128_desc(su32(st + 3 * TILE_BYTES));
 #pragma unroll
           for (int kk = 0; kk < TC_KC / 8; ++kk) {
-            // 8 tf32 = 32 bytes further along k inside the swizzled row
+            // 8 tf32 = 32 bytes further along k inside the swizzled row;
+            // small products first
             const uint64_t adv = (uint64_t)((kk * 32) >> 4);
-            const uint32_t acc0 = (kc > 0 || kk > 0) ? 1u : 0u;
-            mma_tf32(d, ahi + adv, bhi + adv, idesc, acc0);
+            mma_tf32(d, alo + adv, blo + adv, idesc, kk > 0 ? 1u : 0u);
             mma_tf32(d, ahi + adv, blo + adv, idesc, 1u);
             mma_tf32(d, alo + adv, bhi + adv, idesc, 1u);
-            mma_tf32(d, alo + adv, blo + adv, idesc, 1u);
+            mma_tf32(d, ahi + adv, bhi + adv, idesc, 1u);
           }
           mma_commit(&empty[s]);
+          mma_commit(&acc_full[a]);
         }
-        if (!ok) break;
-        mma_commit(&acc_full[a]);
       }
       // every MMA issued so far has completed once `done` fires
       mma_commit(&done);
     }
   } else {
     // TMEM lanes [32q, 32q + 32) are this warp's; it owns columns
-    // [h * 64, h * 64 + 64) of each tile
+    // [h * 64, h * 64 + 64) of each tile.  The tensor cores accumulate one
+    // 32-wide k chunk at a time; the running sum over chunks is kept in
+    // registers and added with IEEE FP32 arithmetic, so the error of a long
+    // update grows like that of an FP32 dot product, not linearly in k.
     const int q = warp & 3, h = (warp - TC_EPI_WARP0) >> 2;
     int it = 0;
-    for (int ti = blockIdx.x; ti < ntask; ti += gridDim.x, ++it) {
-      const int a = it & 1;
+    bool ok = true;
+    for (int ti = blockIdx.x; ti < ntask && ok; ti += gridDim.x) {
       const TcTask t = tasks[ti];
       const int row = t.row0 + q * 32 + lane;
       const int c0 = t.col0 + h * TC_EPI_COLS;
@@ -317,34 +329,43 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         cv[j] = c0 + j < cend ? *src : 0.f;
         src += ldc;
       }
-      // warp-uniform wait: tcgen05.ld below is a warp-collective instruction
-      int ready = 0;
-      if (lane == 0) ready = mbar_wait_or_abort(&acc_full[a], (it >> 1) & 1, err, abortp);
-      ready = __shfl_sync(0xffffffffu, ready, 0);
-      if (!ready) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      for (int kc = 0; kc < t.nk; ++kc, ++it) {
+        const int a = it % TC_NACC;
+        // warp-uniform wait: tcgen05.ld below is a warp-collective instruction
+        int ready = 0;
+        if (lane == 0) ready = mbar_wait_or_abort(&acc_full[a], (it / TC_NACC) & 1, err, abortp);
+        ready = __shfl_sync(0xffffffffu, ready, 0);
+        if (!ready) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int c = 0; c < TC_EPI_COLS / 32; ++c) {
+          float v[32];
+          tmem_ld32<32>(tmem + ((uint32_t)(q * 32) << 16) +
+                            (uint32_t)(a * TC_N + h * TC_EPI_COLS + c * 32),
+                        v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) cv[c * 32 + j] -= v[j];
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acc_empty[a]);
+      }
+      if (!ok) break;
       // recompute the store addresses and bounds here (opaque copies):
-      // reusing the load-side ones would keep 64 of each live across the wait
+      // reusing the load-side ones would keep 64 of each live across the loop
       float* dst = arena + t.c_off + row + (int64_t)c0 * ldc;
       int cst = c0, cen = cend;
       asm volatile("mov.b64 %0, %0;" : "+l"(dst));
       asm volatile("mov.b32 %0, %0;" : "+r"(cst));
       asm volatile("mov.b32 %0, %0;" : "+r"(cen));
 #pragma unroll
-      for (int c = 0; c < TC_EPI_COLS / 32; ++c) {
-        float v[32];
-        tmem_ld32<32>(tmem + ((uint32_t)(q * 32) << 16) +
-                          (uint32_t)(a * TC_N + h * TC_EPI_COLS + c * 32),
-                      v);
-#pragma unroll
-        for (int j = 0; j < 32; ++j) {
-          if (cst + c * 32 + j < cen) *dst = cv[c * 32 + j] - v[j];
-          dst += ldc;
-        }
+      for (int j = 0; j < TC_EPI_COLS; ++j) {
+        if (cst + j < cen) *dst = cv[j];
+        dst += ldc;
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&acc_empty[a]);
     }
   }
   __syncthreads();
@@ -390,12 +411,16 @@ __global__ void __launch_bounds__(256) k_split_t(const float* __restrict__ arena
     const int i = i0 + ii;
     if (i >= rows) break;
     const float v = tile[tx][ii];
-    uint32_t h;
+    uint32_t h, l;
     asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
     const float fh = __uint_as_float(h);
+    // the tensor core ignores the low 13 bits of a TF32 operand: round the
+    // remainder to TF32 here so that its error is unbiased instead of a
+    // truncation that accumulates along k
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - fh));
     const int64_t o = (int64_t)(t.base + i) * pitch + k0 + tx;
     hi[o] = fh;
-    lo[o] = v - fh;
+    lo[o] = __uint_as_float(l);
   }
 }
 
