@@ -293,7 +293,7 @@ typedef struct {
                             (default 0: none) */
   int fs_panel_cols;     /* FP32 Cholesky: width of the outer panels in which the fully-summed
                             columns of large fronts are eliminated, a multiple of 64 up to 256
-                            (default 256); the trailing fully-summed update after each panel
+                            (default 128); the trailing fully-summed update after each panel
                             runs on the tensor cores.  Negative: 64-column steps with SIMT
                             updates throughout */
 } sylver_gb300_schedule_t;

@@ -84,13 +84,14 @@ struct UpdTask {
   int ldc, lda, ldb, row0, col0, rowEnd, colEnd, k0, k1, pad;
 };
 
-// Blocked FP32 Cholesky of large fronts (kernels_blocked.cu): inner steps of
-// BLK_B columns inside outer panels of at most BLK_W columns.
+// Blocked FP32 Cholesky of large fronts (kernels_blocked.cu): panels of at
+// most BLK_W columns (a multiple of BLK_B by schedule choice).
 constexpr int BLK_B = 64;
 constexpr int BLK_W = 256;
-// Diagonal block [c, c+bw) of a front inside the outer panel ending at
-// column pend; xi indexes the block's inverse in the launch's scratch.  For
-// the panel kernel r0 is the first of the CTA's 64 rows (>= c + bw).
+// Panel [c, c + bw) of a front (pend = c + bw); xi indexes the panel's
+// 16 x 16 sub-block inverses (BLK_B * BLK_B floats) in the launch's
+// scratch.  For the panel kernel r0 is the first of the CTA's 64 rows
+// (>= pend).
 struct BlkTask {
   int64_t off;
   int ld, m, c, bw, pend, r0, xi, pad;

@@ -21,6 +21,7 @@ namespace {
 constexpr int SB = 32;      // column block
 constexpr int MAXR = 32;    // right-hand sides per launch
 constexpr int RC = 8;       // right-hand sides per register chunk
+constexpr int GB = 8;       // gather/scatter elements in flight per thread
 
 template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
 
@@ -40,26 +41,46 @@ __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
   const int* rl = rlist + f.rl;
   ACC* xs = scratch + scr_off[blockIdx.x] * nrhs;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
-    int i = idx % m, r = idx / m;
-    xs[idx] = (i < nc) ? x[(int64_t)r * n + rl[i]] : ACC(0);
+  // gather in batches of GB elements per thread, all loads in flight
+  for (int base = 0; base < m * nrhs; base += GB * 256) {
+    ACC v[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u, i = idx % m, r = idx / m;
+      v[u] = (idx < m * nrhs && i < nc) ? x[(int64_t)r * n + rl[i]] : ACC(0);
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u;
+      if (idx < m * nrhs) xs[idx] = v[u];
+    }
   }
   __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
+  __shared__ ACC rdg[SB];         // 1 / L(c0 + k, c0 + k)
   const int nwarps = blockDim.x >> 5;
   __syncthreads();
   for (int c0 = 0; c0 < nc; c0 += SB) {
     const int bw = min(SB, nc - c0);
-    for (int e = tid; e < SB * SB; e += blockDim.x) {
-      const int i = e % SB, k = e / SB;
-      Ld[k][i] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+    {
+      ACC lv[SB * SB / 256];
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u, i = e % SB, k = e / SB;
+        lv[u] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+      }
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u;
+        Ld[e / SB][e % SB] = lv[u];
+        if (e % SB == e / SB) rdg[e % SB] = (e % SB < bw && !unit) ? ACC(1) / lv[u] : ACC(1);
+      }
     }
     __syncthreads();
     // diagonal block: one right-hand side per warp at a time
     for (int r = warp; r < nrhs; r += nwarps) {
       ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] : ACC(0);
       for (int kk = 0; kk < bw; ++kk) {
-        ACC vk = __shfl_sync(0xffffffffu, v, kk);
-        if (!unit) vk = vk / Ld[kk][kk];
+        const ACC vk = __shfl_sync(0xffffffffu, v, kk) * rdg[kk];
         if (lane == kk) v = vk;
         if (lane > kk && lane < bw) v -= Ld[kk][lane] * vk;
       }
@@ -71,28 +92,45 @@ __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
     __syncthreads();
     const int c1 = c0 + bw;
     for (int i = c1 + tid; i < m; i += blockDim.x) {
+      ACC lv[SB];
+#pragma unroll
+      for (int kk = 0; kk < SB; ++kk) lv[kk] = (kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * ld + i] : ACC(0);
       for (int r0 = 0; r0 < nrhs; r0 += RC) {
-        ACC acc[RC];
+        ACC acc[RC], xo[RC];
 #pragma unroll
-        for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
-#pragma unroll 8
+        for (int q = 0; q < RC; ++q) {
+          acc[q] = ACC(0);
+          xo[q] = (r0 + q < nrhs) ? xs[(int64_t)(r0 + q) * m + i] : ACC(0);
+        }
+#pragma unroll
         for (int kk = 0; kk < SB; ++kk) {
-          const ACC l = (kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * ld + i] : ACC(0);
 #pragma unroll
-          for (int q = 0; q < RC; ++q) acc[q] += l * y[kk][min(r0 + q, MAXR - 1)];
+          for (int q = 0; q < RC; ++q) acc[q] += lv[kk] * y[kk][min(r0 + q, MAXR - 1)];
         }
 #pragma unroll
         for (int q = 0; q < RC; ++q)
-          if (r0 + q < nrhs) xs[(int64_t)(r0 + q) * m + i] -= acc[q];
+          if (r0 + q < nrhs) xs[(int64_t)(r0 + q) * m + i] = xo[q] - acc[q];
       }
     }
     __syncthreads();
   }
-  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
-    int i = idx % m, r = idx / m;
-    ACC* dst = x + (int64_t)r * n + rl[i];
-    if (i < nc) *dst = xs[idx];
-    else aadd(dst, xs[idx]);
+  for (int base = 0; base < m * nrhs; base += GB * 256) {
+    ACC v[GB];
+    int dsti[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u, i = idx % m;
+      v[u] = idx < m * nrhs ? xs[idx] : ACC(0);
+      dsti[u] = idx < m * nrhs ? rl[i] : 0;
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u, i = idx % m, r = idx / m;
+      if (idx >= m * nrhs) break;
+      ACC* dst = x + (int64_t)r * n + dsti[u];
+      if (i < nc) *dst = v[u];
+      else aadd(dst, v[u]);
+    }
   }
 }
 
@@ -113,10 +151,20 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
   ACC* xs = scratch + scr_off[blockIdx.x] * nrhs;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = blockDim.x >> 5;
-  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
-    int i = idx % m, r = idx / m;
-    xs[idx] = x[(int64_t)r * n + rl[i]];
+  for (int base = 0; base < m * nrhs; base += GB * 256) {
+    ACC v[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u, i = idx % m, r = idx / m;
+      v[u] = idx < m * nrhs ? x[(int64_t)r * n + rl[i]] : ACC(0);
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u;
+      if (idx < m * nrhs) xs[idx] = v[u];
+    }
   }
+  __shared__ ACC rdg[SB];
   __syncthreads();
   const int nblk = (nc + SB - 1) / SB;
   for (int b = nblk - 1; b >= 0; --b) {
@@ -142,16 +190,26 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
         }
       }
     }
-    for (int e = tid; e < SB * SB; e += blockDim.x) {
-      const int i = e % SB, k = e / SB;
-      Ld[k][i] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+    {
+      ACC lv[SB * SB / 256];
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u, i = e % SB, k = e / SB;
+        lv[u] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+      }
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u;
+        Ld[e / SB][e % SB] = lv[u];
+        if (e % SB == e / SB) rdg[e % SB] = (e % SB < bw && !unit) ? ACC(1) / lv[u] : ACC(1);
+      }
     }
     __syncthreads();
     // diagonal block (transposed): one right-hand side per warp at a time
     for (int r = warp; r < nrhs; r += nwarps) {
       ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] - tt[lane][r] : ACC(0);
       for (int kk = bw - 1; kk >= 0; --kk) {
-        if (lane == kk && !unit) v = v / Ld[kk][kk];
+        if (lane == kk) v = v * rdg[kk];
         ACC zk = __shfl_sync(0xffffffffu, v, kk);
         if (lane < kk) v -= Ld[lane][kk] * zk;
       }
@@ -159,9 +217,21 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
     }
     __syncthreads();
   }
-  for (int idx = tid; idx < m * nrhs; idx += blockDim.x) {
-    int i = idx % m, r = idx / m;
-    if (i < nc) x[(int64_t)r * n + rl[i]] = xs[idx];
+  for (int base = 0; base < m * nrhs; base += GB * 256) {
+    ACC v[GB];
+    int dsti[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u, i = idx % m;
+      const bool ok = idx < m * nrhs && i < nc;
+      v[u] = ok ? xs[idx] : ACC(0);
+      dsti[u] = ok ? rl[i] : -1;
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u;
+      if (dsti[u] >= 0) x[(int64_t)(idx / m) * n + dsti[u]] = v[u];
+    }
   }
 }
 
@@ -294,8 +364,14 @@ __global__ void k_lgather(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, boo
   if (i >= f.m) return;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const int v = a.rlist[f.rl + i];
-  for (int r = 0; r < a.nrhs; ++r)
-    xs[(int64_t)r * f.m + i] = (fwd && i >= f.n) ? ACC(0) : a.x[(int64_t)r * a.n + v];
+  const bool zero = fwd && i >= f.n;
+  ACC val[MAXR];  // every load in flight before the first store
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r)
+    val[r] = (r < a.nrhs && !zero) ? a.x[(int64_t)r * a.n + v] : ACC(0);
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r)
+    if (r < a.nrhs) xs[(int64_t)r * f.m + i] = val[r];
 }
 
 template <typename T, typename ACC>
@@ -307,11 +383,16 @@ __global__ void k_lscatter(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bo
   if (!fwd && i >= f.n) return;
   const int64_t so = a.scr_off[t.f] * a.nrhs;
   const int v = a.rlist[f.rl + i];
-  for (int r = 0; r < a.nrhs; ++r) {
-    const int64_t e = so + (int64_t)r * f.m + i;
+  const ACC* src = (i >= f.n ? a.scratch : a.ys) + so + i;
+  ACC val[MAXR];
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r) val[r] = r < a.nrhs ? src[(int64_t)r * f.m] : ACC(0);
+#pragma unroll
+  for (int r = 0; r < MAXR; ++r) {
+    if (r >= a.nrhs) break;
     ACC* dst = a.x + (int64_t)r * a.n + v;
-    if (i >= f.n) aadd(dst, a.scratch[e]);
-    else *dst = a.ys[e];
+    if (i >= f.n) aadd(dst, val[r]);
+    else *dst = val[r];
   }
 }
 
@@ -488,14 +569,25 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
   for (int rg = 0; rg < (i0 < bw ? a.nrhs : 0); rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     __syncthreads();
-    for (int e = tid; e < nk * RG; e += 256) {
-      const int k = klo + e % nk, r = e / nk;
-      ACC v = ACC(0);
-      if (r < nr) {
-        v = xs[(int64_t)(rg + r) * m + c0 + k];
-        if (BWD) v -= tcur[k * MAXR + rg + r];
+    {
+      // all loads of the slab issued before any is used (nk * RG <= 256 NL)
+      constexpr int NL = BW2 * RG / 256;
+      ACC v[NL];
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int e = tid + 256 * u;
+        const int k = klo + e % max(nk, 1), r = e / max(nk, 1);
+        v[u] = ACC(0);
+        if (e < nk * RG && r < nr) {
+          v[u] = xs[(int64_t)(rg + r) * m + c0 + k];
+          if (BWD) v[u] -= tcur[k * MAXR + rg + r];
+        }
       }
-      vb[k * RG + r] = v;
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int e = tid + 256 * u;
+        if (e < nk * RG) vb[(klo + e % nk) * RG + e / nk] = v[u];
+      }
     }
     __syncthreads();
     ACC acc[RG];
@@ -567,9 +659,19 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
   const int i = t.r0 + rr;
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
-    for (int e = tid; e < BW2 * RG; e += blockDim.x) {
-      int k = e % BW2, r = e / BW2;
-      yb[k * RG + r] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+    {
+      constexpr int NL = BW2 * RG / 256;  // blockDim.x == 256
+      ACC v[NL];
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int e = tid + 256 * u, k = e % BW2, r = e / BW2;
+        v[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+      }
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int e = tid + 256 * u;
+        yb[(e % BW2) * RG + e / BW2] = v[u];
+      }
     }
     __syncthreads();
     ACC acc[RG];

@@ -257,30 +257,28 @@ void FKeep::plan_cholesky() {
     // large fronts: panel steps over the fully-summed columns, batched
     int maxsteps = 0;
     if (PW > 0) {
-      // blocked path: 64-column steps inside outer panels of PW columns; the
-      // trailing fully-summed columns are updated once per outer panel on
-      // the tensor cores
+      // blocked path: outer panels of PW columns; the trailing fully-summed
+      // columns are updated once per panel on the tensor cores
       int maxn = 0;
       for (int s : large) maxn = std::max(maxn, st.ncol[s]);
       for (int k0 = 0; k0 < maxn; k0 += PW) {
-        for (int c = k0; c < k0 + PW && c < maxn; c += BLK_B) {
-          const int64_t d0 = (int64_t)blkd.size(), p0 = (int64_t)blkp.size();
-          for (int s : large) {
-            const int m = st.nrow[s], n = st.ncol[s];
-            if (c >= n) continue;
-            const int pend = std::min(k0 + PW, n);
-            const int bw = std::min(BLK_B, pend - c);
-            const int xi = (int)((int64_t)blkd.size() - d0);
-            blkd.push_back({off[s], ld[s], m, c, bw, pend, 0, xi, 0});
-            for (int r0 = c + bw; r0 < m; r0 += BLK_B)
-              blkp.push_back({off[s], ld[s], m, c, bw, pend, r0, xi, 0});
-          }
-          if ((int64_t)blkd.size() > d0) {
-            ops.push_back({Op::BDIAG, d0, (int64_t)blkd.size(), 0});
-            blkinv_count = std::max(blkinv_count, (int64_t)blkd.size() - d0);
-          }
-          if ((int64_t)blkp.size() > p0) ops.push_back({Op::BPANEL, p0, (int64_t)blkp.size(), 0});
+        // the panel's diagonal block (one CTA per front), then the rows below
+        // it (one CTA per 64 rows)
+        const int64_t d0 = (int64_t)blkd.size(), p0 = (int64_t)blkp.size();
+        for (int s : large) {
+          const int m = st.nrow[s], n = st.ncol[s];
+          if (k0 >= n) continue;
+          const int pend = std::min(k0 + PW, n);
+          const int xi = (int)((int64_t)blkd.size() - d0);
+          blkd.push_back({off[s], ld[s], m, k0, pend - k0, pend, 0, xi, 0});
+          for (int r0 = pend; r0 < m; r0 += 64)
+            blkp.push_back({off[s], ld[s], m, k0, pend - k0, pend, r0, xi, 0});
         }
+        if ((int64_t)blkd.size() > d0) {
+          ops.push_back({Op::BDIAG, d0, (int64_t)blkd.size(), 0});
+          blkinv_count = std::max(blkinv_count, (int64_t)blkd.size() - d0);
+        }
+        if ((int64_t)blkp.size() > p0) ops.push_back({Op::BPANEL, p0, (int64_t)blkp.size(), 0});
         const int p = k0 + PW;
         std::vector<int> tf;
         for (int s : large)

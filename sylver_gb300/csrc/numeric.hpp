@@ -66,7 +66,7 @@ struct Schedule {
   // 0: legacy SIMT panel steps, else the outer panel width
   int panel_cols() const {
     if (fs_panel_cols < 0) return 0;
-    if (fs_panel_cols == 0) return BLK_W;
+    if (fs_panel_cols == 0) return 128;
     return std::max(BLK_B, std::min(BLK_W, fs_panel_cols / BLK_B * BLK_B));
   }
 };
