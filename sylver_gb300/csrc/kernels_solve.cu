@@ -549,6 +549,8 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
   constexpr int RG = RGn<ACC>::v;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* Ms = reinterpret_cast<T*>(dsm);  // Ms[(k - klo)*64 + il] = M(i0 + il, k)
   __shared__ __align__(16) ACC vb[BW2 * RG];
   __shared__ ACC part[4][64][RG + 1];
   const LTask t = tasks[blockIdx.x];
@@ -563,8 +565,15 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
   ACC* tf = a.tt + (int64_t)t.f * 2 * BW2 * MAXR;
   ACC* tcur = tf + ((c0 / BW2) & 1) * BW2 * MAXR;
   ACC* tnext = tf + (((c0 / BW2) + 1) & 1) * BW2 * MAXR;
-  // entries k of v this CTA needs
+  // entries k of v (and columns of the matrix slice) this CTA needs
   const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + 64), nk = khi - klo;
+  if (i0 < bw) {
+    // the CTA's 64-row slice of the inverse, one wave of asynchronous copies
+    for (int e = tid; e < nk * 64; e += 256) {
+      const int rr = e & 63, k = klo + (e >> 6);
+      cp_async(&Ms[e], &M[(int64_t)k * BW2 + i0 + rr]);
+    }
+  }
   // rows [i0, i0+64) beyond the block: nothing to compute (uniform per CTA)
   for (int rg = 0; rg < (i0 < bw ? a.nrhs : 0); rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
@@ -589,38 +598,28 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
         if (e < nk * RG) vb[(klo + e % nk) * RG + e / nk] = v[u];
       }
     }
+    cp_async_wait_all();
     __syncthreads();
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
     if (i < bw) {
       const int k0 = BWD ? i : 0, k1 = BWD ? bw : i + 1;
-      const int kst = k0 + ((g - k0) & 3);
-      // batches of 16 matrix entries in flight per thread
-      for (int kb = kst; kb < k1; kb += 64) {
-        ACC lb[16];
+#pragma unroll 4
+      for (int k = k0 + ((g - k0) & 3); k < k1; k += 4) {
+        const ACC l = (ACC)Ms[(k - klo) * 64 + il];
+        const V* vv = reinterpret_cast<const V*>(vb + k * RG);
 #pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int k = kb + 4 * u;
-          lb[u] = k < k1 ? (ACC)M[(int64_t)k * BW2 + i] : ACC(0);
-        }
-#pragma unroll
-        for (int u = 0; u < 16; ++u) {
-          const int k = min(kb + 4 * u, k1 - 1);  // l = 0 beyond k1; v is finite there
-          const ACC l = lb[u];
-          const V* vv = reinterpret_cast<const V*>(vb + k * RG);
-#pragma unroll
-          for (int q = 0; q < RG / VW; ++q) {
-            const V x4 = vv[q];
-            if constexpr (VW == 4) {
-              acc[4 * q + 0] += l * x4.x;
-              acc[4 * q + 1] += l * x4.y;
-              acc[4 * q + 2] += l * x4.z;
-              acc[4 * q + 3] += l * x4.w;
-            } else {
-              acc[2 * q + 0] += l * x4.x;
-              acc[2 * q + 1] += l * x4.y;
-            }
+        for (int q = 0; q < RG / VW; ++q) {
+          const V x4 = vv[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l * x4.x;
+            acc[4 * q + 1] += l * x4.y;
+            acc[4 * q + 2] += l * x4.z;
+            acc[4 * q + 3] += l * x4.w;
+          } else {
+            acc[2 * q + 0] += l * x4.x;
+            acc[2 * q + 1] += l * x4.y;
           }
         }
       }
@@ -640,14 +639,17 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
     for (int e = tid; e < 64 * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
 }
 
-// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 32-column group g);
-// y is read from shared memory as 16-byte vectors (one broadcast per warp)
+// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 32-column group g).
+// The 32 x 256 tile of L is staged in shared memory by one wave of
+// asynchronous copies; y is read as 16-byte vectors (one broadcast per warp).
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* Lt = reinterpret_cast<T*>(dsm);  // Lt[k*32 + rr] = L(r0 + rr, c0 + k)
   __shared__ __align__(16) ACC yb[BW2 * RG];
   __shared__ ACC red[8][32][RG + 1];
   const LTask t = tasks[blockIdx.x];
@@ -657,6 +659,12 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   const int i = t.r0 + rr;
+  const int nrow = min(32, f.m - t.r0);
+  for (int e = tid; e < BW2 * 32; e += 256) {
+    const int r2 = e & 31, k = e >> 5;
+    if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
+    else Lt[e] = T(0);
+  }
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     {
@@ -673,34 +681,27 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
         yb[(e % BW2) * RG + e / BW2] = v[u];
       }
     }
+    cp_async_wait_all();
     __syncthreads();
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    if (i < f.m) {
-      ACC lb[32];
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      const int k = g * 32 + kk;
+      const ACC l = (ACC)Lt[k * 32 + rr];
+      const V* yv = reinterpret_cast<const V*>(yb + k * RG);
 #pragma unroll
-      for (int kk = 0; kk < 32; ++kk) {
-        const int k = g * 32 + kk;
-        lb[kk] = (k < bw) ? (ACC)L[(int64_t)(c0 + k) * f.ld + i] : ACC(0);
-      }
-#pragma unroll
-      for (int kk = 0; kk < 32; ++kk) {
-        const int k = g * 32 + kk;
-        const ACC l = lb[kk];
-        const V* yv = reinterpret_cast<const V*>(yb + k * RG);
-#pragma unroll
-        for (int q = 0; q < RG / VW; ++q) {
-          const V y4 = yv[q];
-          if constexpr (VW == 4) {
-            acc[4 * q + 0] += l * y4.x;
-            acc[4 * q + 1] += l * y4.y;
-            acc[4 * q + 2] += l * y4.z;
-            acc[4 * q + 3] += l * y4.w;
-          } else {
-            acc[2 * q + 0] += l * y4.x;
-            acc[2 * q + 1] += l * y4.y;
-          }
+      for (int q = 0; q < RG / VW; ++q) {
+        const V y4 = yv[q];
+        if constexpr (VW == 4) {
+          acc[4 * q + 0] += l * y4.x;
+          acc[4 * q + 1] += l * y4.y;
+          acc[4 * q + 2] += l * y4.z;
+          acc[4 * q + 3] += l * y4.w;
+        } else {
+          acc[2 * q + 0] += l * y4.x;
+          acc[2 * q + 1] += l * y4.y;
         }
       }
     }
@@ -719,18 +720,21 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
     }
     __syncthreads();
   }
+  (void)i;
 }
 
-// rows [r0, r0+64) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw
+// rows [r0, r0+64) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw.
+// The 64 x 256 tile of L is staged in shared memory by one wave of
+// asynchronous copies; thread tid owns column k = tid.
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
-  constexpr int SR = sizeof(ACC) == 8 ? 16 : 32;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
-  __shared__ ACC Lt[SR][BW2 + 1];
-  __shared__ __align__(16) ACC xt[SR][RG];
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(BW2+1) + k] = L(r0 + ii, c0 + k)
+  __shared__ __align__(16) ACC xt[64][RG];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
@@ -739,51 +743,44 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
   const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / BW2) & 1)) * BW2 * MAXR;
-  const int rend = min(t.r0 + 64, f.m);
+  const int nrow = min(64, f.m - t.r0);
+  for (int e = tid; e < 64 * BW2; e += 256) {
+    const int ii = e % 64, k = e / 64;
+    T* dst = &Lt[ii * (BW2 + 1) + k];
+    if (ii < nrow && k < bw) cp_async(dst, &L[(int64_t)(c0 + k) * f.ld + t.r0 + ii]);
+    else *dst = T(0);
+  }
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    for (int s0 = t.r0; s0 < rend; s0 += SR) {
-      const int nrow = min(SR, rend - s0);
-      for (int e = tid; e < SR * BW2; e += blockDim.x) {
-        int ii = e % SR, kk = e / SR;
-        if constexpr (sizeof(T) == sizeof(ACC)) {
-          if (ii < nrow && kk < bw) cp_async(&Lt[ii][kk], reinterpret_cast<const ACC*>(
-                                                              &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]));
-          else Lt[ii][kk] = ACC(0);
-        } else {
-          Lt[ii][kk] = (ii < nrow && kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * f.ld + s0 + ii] : ACC(0);
-        }
-      }
-      for (int e = tid; e < SR * RG; e += blockDim.x) {
-        int ii = e % SR, r = e / SR;
-        const ACC* src = (s0 + ii < f.n) ? ysl : xs;
-        xt[ii][r] = (ii < nrow && r < nr) ? src[(int64_t)(rg + r) * f.m + s0 + ii] : ACC(0);
-      }
-      cp_async_wait_all();
-      __syncthreads();
-#pragma unroll 8
-      for (int ii = 0; ii < SR; ++ii) {
-        const ACC l = Lt[ii][tid];
-        const V* xv = reinterpret_cast<const V*>(&xt[ii][0]);
-#pragma unroll
-        for (int q = 0; q < RG / VW; ++q) {
-          const V x4 = xv[q];
-          if constexpr (VW == 4) {
-            acc[4 * q + 0] += l * x4.x;
-            acc[4 * q + 1] += l * x4.y;
-            acc[4 * q + 2] += l * x4.z;
-            acc[4 * q + 3] += l * x4.w;
-          } else {
-            acc[2 * q + 0] += l * x4.x;
-            acc[2 * q + 1] += l * x4.y;
-          }
-        }
-      }
-      __syncthreads();
+    for (int e = tid; e < 64 * RG; e += blockDim.x) {
+      const int ii = e % 64, r = e / 64, row = t.r0 + ii;
+      const ACC* src = (row < f.n) ? ysl : xs;
+      xt[ii][r] = (ii < nrow && r < nr) ? src[(int64_t)(rg + r) * f.m + row] : ACC(0);
     }
+    cp_async_wait_all();
+    __syncthreads();
+#pragma unroll 8
+    for (int ii = 0; ii < 64; ++ii) {
+      const ACC l = (ACC)Lt[ii * (BW2 + 1) + tid];
+      const V* xv = reinterpret_cast<const V*>(&xt[ii][0]);
+#pragma unroll
+      for (int q = 0; q < RG / VW; ++q) {
+        const V x4 = xv[q];
+        if constexpr (VW == 4) {
+          acc[4 * q + 0] += l * x4.x;
+          acc[4 * q + 1] += l * x4.y;
+          acc[4 * q + 2] += l * x4.z;
+          acc[4 * q + 3] += l * x4.w;
+        } else {
+          acc[2 * q + 0] += l * x4.x;
+          acc[2 * q + 1] += l * x4.y;
+        }
+      }
+    }
+    __syncthreads();
     if (tid < bw)
 #pragma unroll
       for (int q = 0; q < RG; ++q)
@@ -792,6 +789,11 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
 }
 
 inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
+
+// dynamic shared memory of the staged solve-step kernels
+template <typename T> constexpr size_t diag_mv_smem() { return sizeof(T) * 64 * BW2; }
+template <typename T> constexpr size_t fwd_upd_smem() { return sizeof(T) * 32 * BW2; }
+template <typename T> constexpr size_t bwd_red_smem() { return sizeof(T) * 64 * (BW2 + 1); }
 
 }  // namespace
 
@@ -883,16 +885,16 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
       k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
     case LS_FWD_DIAG2:
-      k_diag_mv<T, ACC, false><<<dim3(ntask, BW2 / 64), 256, 0, s>>>(tasks, a);
+      k_diag_mv<T, ACC, false><<<dim3(ntask, BW2 / 64), 256, diag_mv_smem<T>(), s>>>(tasks, a);
       break;
     case LS_FWD_UPD2:
-      k_fwd_upd3<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
+      k_fwd_upd3<T, ACC><<<ntask, 256, fwd_upd_smem<T>(), s>>>(tasks, a);
       break;
     case LS_BWD_RED2:
-      k_bwd_red3<T, ACC><<<ntask, 256, 0, s>>>(tasks, a);
+      k_bwd_red3<T, ACC><<<ntask, 256, bwd_red_smem<T>(), s>>>(tasks, a);
       break;
     case LS_BWD_DIAG2:
-      k_diag_mv<T, ACC, true><<<dim3(ntask, BW2 / 64), 256, 0, s>>>(tasks, a);
+      k_diag_mv<T, ACC, true><<<dim3(ntask, BW2 / 64), 256, diag_mv_smem<T>(), s>>>(tasks, a);
       break;
   }
 }
@@ -908,6 +910,14 @@ template <typename T>
 void prepare_solve_kernels() {
   SG_CUDA(cudaFuncSetAttribute(k_inv256<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(2 * 64 * 65 * sizeof(T))));
+  SG_CUDA(cudaFuncSetAttribute(k_diag_mv<T, T, false>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
+  SG_CUDA(cudaFuncSetAttribute(k_diag_mv<T, T, true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
+  SG_CUDA(cudaFuncSetAttribute(k_fwd_upd3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)fwd_upd_smem<T>()));
+  SG_CUDA(cudaFuncSetAttribute(k_bwd_red3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)bwd_red_smem<T>()));
 }
 
 template <typename T>
