@@ -251,6 +251,16 @@ void* sylver_gb300_stream(void);
 int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, long* launches,
                                 double* flops);
 
+/* Time one forward + backward sweep of the Cholesky factor held by fkeep for
+ * nrhs (1..32) right-hand sides (zeros, in an internal buffer), launch by
+ * launch with CUDA events and no graph, accumulated per kernel kind:
+ * 0 small fronts forward, 1 small fronts backward, 2 + k for the large-front
+ * launches (k: 0/1 gather forward/backward, 2/3 scatter forward/backward,
+ * 4 diagonal block forward, 5 rows below forward, 6 rows below backward,
+ * 7 diagonal block backward).  Arrays hold 10 entries.  Returns 0, or -98 for
+ * an LDL^T factor or nrhs outside 1..32.  No reference counterpart. */
+int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches);
+
 /* Diagnostic: run the tensor-core (tcgen05, 4xTF32) contribution-block
  * update on a synthetic rows x k panel and report max|C - C_ref| / max|C_ref|
  * against an FP64 host product.  Returns 0 or a reference flag. */

@@ -103,7 +103,7 @@ EXPORTS = (
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
     "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
-    "sylver_gb300_get_schedule", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
+    "sylver_gb300_get_schedule", "sylver_gb300_profile_solve", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
     "sylver_gb300_mlp_num_params", "sylver_gb300_mlp_set_params", "sylver_gb300_mlp_get_params",
     "sylver_gb300_mlp_forward", "sylver_gb300_mlp_loss_grad", "sylver_gb300_mlp_train",
 )
@@ -147,6 +147,7 @@ def load(path: str | None = None):
                                             ctypes.POINTER(D)]),
         "sylver_gb300_stream": (P, []),
         "sylver_gb300_profile_factor": (I, [P, P, P, P, P]),
+        "sylver_gb300_profile_solve": (I, [P, I, P, P]),
         "sylver_gb300_tc_selfcheck": (I, [I, I, ctypes.POINTER(D)]),
         "sylver_gb300_solve_history": (I, [P, P, I]),
         "sylver_gb300_set_schedule": (None, [ctypes.POINTER(Schedule)]),
@@ -300,6 +301,17 @@ class Factor:
             raise RuntimeError(f"profile failed: {rc}")
         return {k: dict(ms=float(ms[i]), launches=int(nl[i]), flops=float(fl[i]))
                 for i, k in enumerate(self.KINDS)}
+
+    SOLVE_KINDS = ("small_fwd", "small_bwd", "gather_fwd", "gather_bwd", "scatter_fwd",
+                   "scatter_bwd", "diag_fwd", "rows_fwd", "rows_bwd", "diag_bwd")
+
+    def profile_solve(self, nrhs=16):
+        """Per-kernel-kind timing of one forward + backward sweep (no graph)."""
+        ms = np.zeros(10); nl = np.zeros(10, dtype=np.int64)
+        rc = load().sylver_gb300_profile_solve(self.fkeep, int(nrhs), _p(ms), _p(nl))
+        if rc != 0:
+            raise RuntimeError(f"profile_solve failed: {rc}")
+        return {k: dict(ms=float(ms[i]), launches=int(nl[i])) for i, k in enumerate(self.SOLVE_KINDS)}
 
     def diag(self, n):
         d = np.zeros(2 * max(n, 1), dtype=np.float64)

@@ -95,8 +95,7 @@ void factorize_common(bool posdef, const double* val_host, const double* val_dev
       fk->small_piv = opt->small;
       fk->action = opt->action;
     }
-    int64_t nz = 0;
-    for (int64_t s : ak->clean.src) nz = std::max<int64_t>(nz, s + 1);
+    const int64_t nz = ak->nnz_val();
     const double* vdev = val_dev;
     if (val_host) {
       std::vector<double> scaled;
@@ -402,6 +401,16 @@ int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, 
   if (!fk) return SYLVER_ERROR_CALL_SEQUENCE;
   try {
     return fk->profile(val_dev, ms, launches, flops, Runtime::get().stream);
+  } catch (const std::exception&) {
+    return SYLVER_ERROR_CUDA_UNKNOWN;
+  }
+}
+
+int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches) {
+  FKeep* fk = static_cast<FKeep*>(fkeep);
+  if (!fk || !ms || !launches) return SYLVER_ERROR_CALL_SEQUENCE;
+  try {
+    return fk->profile_solve(nrhs, ms, launches, Runtime::get().stream);
   } catch (const std::exception&) {
     return SYLVER_ERROR_CUDA_UNKNOWN;
   }

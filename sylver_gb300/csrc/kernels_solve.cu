@@ -430,6 +430,7 @@ __global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
 // step is one parallel mat-vec on the diagonal block plus one update (forward)
 // or reduction (backward) of the rows below, spread over many small CTAs.
 constexpr int BW2 = LSOLVE_BW2;
+constexpr int DMV_ROWS = 16;  // rows of the diagonal mat-vec per CTA (16 CTAs per block)
 template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
 
 // X = inverse of the 256-column diagonal block (column-major, ld 256, lower):
@@ -547,16 +548,18 @@ template <typename T, typename ACC, bool BWD>
 __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks,
                                                  LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
+  constexpr int DR = DMV_ROWS;  // output rows per CTA; 256 / DR k-phases per row
+  constexpr int NG = 256 / DR;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   extern __shared__ __align__(16) unsigned char dsm[];
-  T* Ms = reinterpret_cast<T*>(dsm);  // Ms[(k - klo)*64 + il] = M(i0 + il, k)
+  T* Ms = reinterpret_cast<T*>(dsm);  // Ms[(k - klo)*DR + il] = M(i0 + il, k)
+  ACC* part = reinterpret_cast<ACC*>(dsm + sizeof(T) * DR * BW2);  // [NG][DR][RG + 1]
   __shared__ __align__(16) ACC vb[BW2 * RG];
-  __shared__ ACC part[4][64][RG + 1];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
-  const int c0 = t.c0, bw = t.bw, i0 = 64 * blockIdx.y;
-  const int tid = threadIdx.x, il = tid & 63, g = tid >> 6, i = i0 + il;
+  const int c0 = t.c0, bw = t.bw, i0 = DR * blockIdx.y;
+  const int tid = threadIdx.x, il = tid % DR, g = tid / DR, i = i0 + il;
   const int64_t m = f.m;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
@@ -566,15 +569,15 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
   ACC* tcur = tf + ((c0 / BW2) & 1) * BW2 * MAXR;
   ACC* tnext = tf + (((c0 / BW2) + 1) & 1) * BW2 * MAXR;
   // entries k of v (and columns of the matrix slice) this CTA needs
-  const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + 64), nk = khi - klo;
+  const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + DR), nk = khi - klo;
   if (i0 < bw) {
-    // the CTA's 64-row slice of the inverse, one wave of asynchronous copies
-    for (int e = tid; e < nk * 64; e += 256) {
-      const int rr = e & 63, k = klo + (e >> 6);
+    // the CTA's slice of the inverse, one wave of asynchronous copies
+    for (int e = tid; e < nk * DR; e += 256) {
+      const int rr = e % DR, k = klo + e / DR;
       cp_async(&Ms[e], &M[(int64_t)k * BW2 + i0 + rr]);
     }
   }
-  // rows [i0, i0+64) beyond the block: nothing to compute (uniform per CTA)
+  // rows beyond the block: nothing to compute (uniform per CTA)
   for (int rg = 0; rg < (i0 < bw ? a.nrhs : 0); rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     __syncthreads();
@@ -606,8 +609,8 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
     if (i < bw) {
       const int k0 = BWD ? i : 0, k1 = BWD ? bw : i + 1;
 #pragma unroll 4
-      for (int k = k0 + ((g - k0) & 3); k < k1; k += 4) {
-        const ACC l = (ACC)Ms[(k - klo) * 64 + il];
+      for (int k = k0 + ((g - k0) % NG + NG) % NG; k < k1; k += NG) {
+        const ACC l = (ACC)Ms[(k - klo) * DR + il];
         const V* vv = reinterpret_cast<const V*>(vb + k * RG);
 #pragma unroll
         for (int q = 0; q < RG / VW; ++q) {
@@ -625,42 +628,44 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
       }
     }
 #pragma unroll
-    for (int q = 0; q < RG; ++q) part[g][il][q] = acc[q];
+    for (int q = 0; q < RG; ++q) part[(g * DR + il) * (RG + 1) + q] = acc[q];
     __syncthreads();
-    for (int e = tid; e < 64 * RG; e += 256) {
-      const int rr = e % 64, q = e / 64, ii = i0 + rr;
+    for (int e = tid; e < DR * RG; e += 256) {
+      const int rr = e % DR, q = e / DR, ii = i0 + rr;
       if (ii < bw && q < nr) {
-        ysl[(int64_t)(rg + q) * m + c0 + ii] =
-            part[0][rr][q] + part[1][rr][q] + part[2][rr][q] + part[3][rr][q];
+        ACC sum = ACC(0);
+#pragma unroll
+        for (int gg = 0; gg < NG; ++gg) sum += part[(gg * DR + rr) * (RG + 1) + q];
+        ysl[(int64_t)(rg + q) * m + c0 + ii] = sum;
       }
     }
   }
   if (BWD)
-    for (int e = tid; e < 64 * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
+    for (int e = tid; e < DR * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
 }
 
-// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 32-column group g).
-// The 32 x 256 tile of L is staged in shared memory by one wave of
-// asynchronous copies; y is read as 16-byte vectors (one broadcast per warp).
+// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 16-column group g),
+// 512 threads.  The 32 x 256 tile of L is staged in shared memory by one wave
+// of asynchronous copies; y is read as 16-byte vectors (one broadcast per
+// warp).
 template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ tasks,
+__global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   extern __shared__ __align__(16) unsigned char dsm[];
   T* Lt = reinterpret_cast<T*>(dsm);  // Lt[k*32 + rr] = L(r0 + rr, c0 + k)
+  ACC* red = reinterpret_cast<ACC*>(dsm + sizeof(T) * 32 * BW2);  // [16][32][RG + 1]
   __shared__ __align__(16) ACC yb[BW2 * RG];
-  __shared__ ACC red[8][32][RG + 1];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
   const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, rr = tid % 32, g = tid / 32;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  const int i = t.r0 + rr;
   const int nrow = min(32, f.m - t.r0);
-  for (int e = tid; e < BW2 * 32; e += 256) {
+  for (int e = tid; e < BW2 * 32; e += 512) {
     const int r2 = e & 31, k = e >> 5;
     if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
     else Lt[e] = T(0);
@@ -668,16 +673,16 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     {
-      constexpr int NL = BW2 * RG / 256;  // blockDim.x == 256
+      constexpr int NL = BW2 * RG / 512;
       ACC v[NL];
 #pragma unroll
       for (int u = 0; u < NL; ++u) {
-        const int e = tid + 256 * u, k = e % BW2, r = e / BW2;
+        const int e = tid + 512 * u, k = e % BW2, r = e / BW2;
         v[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
       }
 #pragma unroll
       for (int u = 0; u < NL; ++u) {
-        const int e = tid + 256 * u;
+        const int e = tid + 512 * u;
         yb[(e % BW2) * RG + e / BW2] = v[u];
       }
     }
@@ -687,8 +692,8 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
 #pragma unroll 8
-    for (int kk = 0; kk < 32; ++kk) {
-      const int k = g * 32 + kk;
+    for (int kk = 0; kk < 16; ++kk) {
+      const int k = g * 16 + kk;
       const ACC l = (ACC)Lt[k * 32 + rr];
       const V* yv = reinterpret_cast<const V*>(yb + k * RG);
 #pragma unroll
@@ -706,48 +711,49 @@ __global__ void __launch_bounds__(256) k_fwd_upd3(const LTask* __restrict__ task
       }
     }
 #pragma unroll
-    for (int q = 0; q < RG; ++q) red[g][rr][q] = acc[q];
+    for (int q = 0; q < RG; ++q) red[(g * 32 + rr) * (RG + 1) + q] = acc[q];
     __syncthreads();
     // 32 rows x RG sums, spread over all threads
-    for (int e = tid; e < 32 * RG; e += blockDim.x) {
+    for (int e = tid; e < 32 * RG; e += 512) {
       const int r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
       if (i2 < f.m && q < nr) {
         ACC sum = ACC(0);
 #pragma unroll
-        for (int gg = 0; gg < 8; ++gg) sum += red[gg][r2][q];
+        for (int gg = 0; gg < 16; ++gg) sum += red[(gg * 32 + r2) * (RG + 1) + q];
         xs[(int64_t)(rg + q) * f.m + i2] -= sum;
       }
     }
     __syncthreads();
   }
-  (void)i;
 }
 
-// rows [r0, r0+64) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw.
-// The 64 x 256 tile of L is staged in shared memory by one wave of
-// asynchronous copies; thread tid owns column k = tid.
+// rows [r0, r0+32) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw.
+// The 32 x 256 tile of L is staged in shared memory by one wave of
+// asynchronous copies; thread (column k = tid % 256, row half h = tid / 256),
+// 512 threads, the halves reduced through shared memory.
 template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ tasks,
+__global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
   constexpr int RG = RGn<ACC>::v;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   extern __shared__ __align__(16) unsigned char dsm[];
   T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(BW2+1) + k] = L(r0 + ii, c0 + k)
-  __shared__ __align__(16) ACC xt[64][RG];
+  ACC* half = reinterpret_cast<ACC*>(dsm + sizeof(T) * 32 * (BW2 + 1));  // [BW2][RG + 1]
+  __shared__ __align__(16) ACC xt[32][RG];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, k = tid % BW2, h = tid / BW2;
   // rows below the block: solved rows (< n) in ys, contribution rows in xs
   const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / BW2) & 1)) * BW2 * MAXR;
-  const int nrow = min(64, f.m - t.r0);
-  for (int e = tid; e < 64 * BW2; e += 256) {
-    const int ii = e % 64, k = e / 64;
-    T* dst = &Lt[ii * (BW2 + 1) + k];
-    if (ii < nrow && k < bw) cp_async(dst, &L[(int64_t)(c0 + k) * f.ld + t.r0 + ii]);
+  const int nrow = min(32, f.m - t.r0);
+  for (int e = tid; e < 32 * BW2; e += 512) {
+    const int ii = e % 32, kk = e / 32;
+    T* dst = &Lt[ii * (BW2 + 1) + kk];
+    if (ii < nrow && kk < bw) cp_async(dst, &L[(int64_t)(c0 + kk) * f.ld + t.r0 + ii]);
     else *dst = T(0);
   }
   for (int rg = 0; rg < a.nrhs; rg += RG) {
@@ -755,16 +761,17 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    for (int e = tid; e < 64 * RG; e += blockDim.x) {
-      const int ii = e % 64, r = e / 64, row = t.r0 + ii;
+    for (int e = tid; e < 32 * RG; e += blockDim.x) {
+      const int ii = e % 32, r = e / 32, row = t.r0 + ii;
       const ACC* src = (row < f.n) ? ysl : xs;
       xt[ii][r] = (ii < nrow && r < nr) ? src[(int64_t)(rg + r) * f.m + row] : ACC(0);
     }
     cp_async_wait_all();
     __syncthreads();
 #pragma unroll 8
-    for (int ii = 0; ii < 64; ++ii) {
-      const ACC l = (ACC)Lt[ii * (BW2 + 1) + tid];
+    for (int i2 = 0; i2 < 16; ++i2) {
+      const int ii = h * 16 + i2;
+      const ACC l = (ACC)Lt[ii * (BW2 + 1) + k];
       const V* xv = reinterpret_cast<const V*>(&xt[ii][0]);
 #pragma unroll
       for (int q = 0; q < RG / VW; ++q) {
@@ -780,20 +787,30 @@ __global__ void __launch_bounds__(256) k_bwd_red3(const LTask* __restrict__ task
         }
       }
     }
+    if (h == 1)
+#pragma unroll
+      for (int q = 0; q < RG; ++q) half[k * (RG + 1) + q] = acc[q];
     __syncthreads();
-    if (tid < bw)
+    if (h == 0 && k < bw)
 #pragma unroll
       for (int q = 0; q < RG; ++q)
-        if (q < nr) aadd(&tf[tid * MAXR + rg + q], acc[q]);
+        if (q < nr) aadd(&tf[k * MAXR + rg + q], acc[q] + half[k * (RG + 1) + q]);
+    __syncthreads();
   }
 }
 
 inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
 
 // dynamic shared memory of the staged solve-step kernels
-template <typename T> constexpr size_t diag_mv_smem() { return sizeof(T) * 64 * BW2; }
-template <typename T> constexpr size_t fwd_upd_smem() { return sizeof(T) * 32 * BW2; }
-template <typename T> constexpr size_t bwd_red_smem() { return sizeof(T) * 64 * (BW2 + 1); }
+template <typename T> constexpr size_t diag_mv_smem() {
+  return sizeof(T) * DMV_ROWS * BW2 + sizeof(T) * 256 * (RGn<T>::v + 1);
+}
+template <typename T> constexpr size_t fwd_upd_smem() {
+  return sizeof(T) * 32 * BW2 + sizeof(T) * 16 * 32 * (RGn<T>::v + 1);
+}
+template <typename T> constexpr size_t bwd_red_smem() {
+  return sizeof(T) * 32 * (BW2 + 1) + sizeof(T) * BW2 * (RGn<T>::v + 1);
+}
 
 }  // namespace
 
@@ -885,16 +902,16 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
       k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
     case LS_FWD_DIAG2:
-      k_diag_mv<T, ACC, false><<<dim3(ntask, BW2 / 64), 256, diag_mv_smem<T>(), s>>>(tasks, a);
+      k_diag_mv<T, ACC, false><<<dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s>>>(tasks, a);
       break;
     case LS_FWD_UPD2:
-      k_fwd_upd3<T, ACC><<<ntask, 256, fwd_upd_smem<T>(), s>>>(tasks, a);
+      k_fwd_upd3<T, ACC><<<ntask, 512, fwd_upd_smem<T>(), s>>>(tasks, a);
       break;
     case LS_BWD_RED2:
-      k_bwd_red3<T, ACC><<<ntask, 256, bwd_red_smem<T>(), s>>>(tasks, a);
+      k_bwd_red3<T, ACC><<<ntask, 512, bwd_red_smem<T>(), s>>>(tasks, a);
       break;
     case LS_BWD_DIAG2:
-      k_diag_mv<T, ACC, true><<<dim3(ntask, BW2 / 64), 256, diag_mv_smem<T>(), s>>>(tasks, a);
+      k_diag_mv<T, ACC, true><<<dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s>>>(tasks, a);
       break;
   }
 }

@@ -96,13 +96,17 @@ FKeep::~FKeep() {
   clear_solve_graphs();
 }
 
-int64_t FKeep::nnz_orig() const {
+int64_t AKeep::nnz_val() const {
+  if (nz_val_ >= 0) return nz_val_;
   int64_t mx = 0;
-  for (int64_t s : ak->clean.src) mx = std::max(mx, s + 1);
-  const auto& nl = ak->st.nlist;
+  for (int64_t s : clean.src) mx = std::max(mx, s + 1);
+  const auto& nl = st.nlist;
   for (size_t k = 0; k < nl.size(); k += 2) mx = std::max<int64_t>(mx, nl[k]);
+  nz_val_ = mx;
   return mx;
 }
+
+int64_t FKeep::nnz_orig() const { return ak->nnz_val(); }
 
 namespace {
 // fronts that get the blocked multi-CTA solve
@@ -682,7 +686,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           int bw = std::min(LB2, d.n - c0), c1 = c0 + bw;
           if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
           else
-            for (int r0 = c1; r0 < d.m; r0 += (kind == LS_FWD_UPD2 ? 32 : 64))
+            for (int r0 = c1; r0 < d.m; r0 += 32)
               htasks.push_back({f, c0, bw, r0, 0, 0});
         }
         push(ops, kind, a);
@@ -746,17 +750,73 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
                                         unit, s);
       else launch_solve_bwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc, unit,
                                     s);
+      if (prof) mark(fwd ? 0 : 1, s);
     }
     LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),
                      inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), cnt.as<unsigned>(),
                      inv2.as<T>(), inv2_off.as<int64_t>() + v.f0, inv2t.as<T>()};
-    for (const SOp& op : fwd ? v.fwd : v.bwd)
+    for (const SOp& op : fwd ? v.fwd : v.bwd) {
       launch_lsolve<T, ACC>(op.kind, tasks.as<LTask>() + op.a, (int)(op.b - op.a), a, s);
+      if (prof) mark(2 + op.kind, s);
+    }
   };
   if (fwd)
     for (const Lv& v : lv) level(v);
   else
     for (int l = (int)lv.size() - 1; l >= 0; --l) level(lv[l]);
+}
+
+void SolvePlan::mark(int kind, cudaStream_t s) {
+  cudaEvent_t e;
+  SG_CUDA(cudaEventCreate(&e));
+  SG_CUDA(cudaEventRecord(e, s));
+  prof->push_back({kind, e});
+}
+
+int FKeep::profile_solve(int nrhs, double* ms, long* nl, cudaStream_t s) {
+  for (int k = 0; k < 10; ++k) {
+    ms[k] = 0.0;
+    nl[k] = 0;
+  }
+  if (ldlt || nrhs < 1 || nrhs > 32) return -98;
+  const int n = ak->n;
+  const size_t es = precision == 1 ? sizeof(float) : sizeof(double);
+  xp.ensure(std::max<size_t>((size_t)n * nrhs * es, 1));
+  SG_CUDA(cudaMemsetAsync(xp.p, 0, (size_t)n * nrhs * es, s));
+  scratch.ensure(std::max<int64_t>(scratch_rows * nrhs, 1) * es);
+  splan.ensure_tt(es, scratch_rows * nrhs);
+  std::vector<std::pair<int, cudaEvent_t>> ev;
+  splan.prof = &ev;
+  try {
+    splan.mark(-1, s);
+    for (int dir = 0; dir < 2; ++dir) {
+      if (precision == 1)
+        splan.run<float, float>(dir == 0, arena.as<float>(), dfr.as<FrontDesc>(),
+                                rlist0.as<int>(), xp.as<float>(), n, nrhs, scratch.as<float>(),
+                                dscr.as<int64_t>(), false, s);
+      else
+        splan.run<double, double>(dir == 0, arena.as<double>(), dfr.as<FrontDesc>(),
+                                  rlist0.as<int>(), xp.as<double>(), n, nrhs,
+                                  scratch.as<double>(), dscr.as<int64_t>(), false, s);
+    }
+    SG_CUDA(cudaStreamSynchronize(s));
+  } catch (...) {
+    splan.prof = nullptr;
+    for (auto& e : ev) cudaEventDestroy(e.second);
+    throw;
+  }
+  splan.prof = nullptr;
+  for (size_t q = 1; q < ev.size(); ++q) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[q - 1].second, ev[q].second);
+    const int k = ev[q].first;
+    if (k >= 0 && k < 10) {
+      ms[k] += t;
+      nl[k] += 1;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e.second);
+  return 0;
 }
 
 template void SolvePlan::run<float, float>(bool, const float*, const FrontDesc*, const int*,

@@ -94,6 +94,10 @@ struct AKeep {
   std::vector<int> fcol;
   std::vector<int64_t> fidx;
   void build_full_csr();
+  // entries of the caller's val array the analysis refers to (computed once;
+  // a scan of every map, too slow to repeat per factorization)
+  int64_t nnz_val() const;
+  mutable int64_t nz_val_ = -1;
 };
 
 // One kernel launch of the factor schedule.
@@ -143,6 +147,11 @@ struct SolvePlan {
   template <typename T, typename ACC>
   void run(bool fwd, const T* arena, const FrontDesc* dfr, const int* rlist, ACC* x, int n,
            int nrhs, ACC* scratch, const int64_t* dscr, bool unit, cudaStream_t s);
+  // Profiling (sylver_gb300_profile_solve): when set, run() records an event
+  // after every launch, tagged with its kind (0 small fronts forward, 1 small
+  // fronts backward, 2 + LsKind for the large-front launches).
+  std::vector<std::pair<int, cudaEvent_t>>* prof = nullptr;
+  void mark(int kind, cudaStream_t s);
 };
 
 struct FKeep {
@@ -249,6 +258,8 @@ struct FKeep {
   int solve_raw(int job, int nrhs, double* x_dev, int ldx, cudaStream_t s);
   // Per-kind timing of the factor schedule (see sylver_gb300_profile_factor).
   int profile(const double* val_dev, double* ms, long* launches, double* flops, cudaStream_t s);
+  // Per-kind timing of one forward + backward sweep (see sylver_gb300_profile_solve).
+  int profile_solve(int nrhs, double* ms, long* launches, cudaStream_t s);
 
  public:
   template <typename T> void run_ops(cudaStream_t s);
