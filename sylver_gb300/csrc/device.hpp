@@ -31,6 +31,7 @@ enum : unsigned {
   ST_TIMEOUT = 32u,       // a bounded wait inside a kernel gave up
 };
 
+#if defined(__CUDACC__)
 // Asynchronous global -> shared copy of one element (cp.async, 4/8 bytes):
 // every copy a thread issued lands once it passes cp_async_wait_all(); a
 // __syncthreads() afterwards makes them visible to the whole CTA.  Lets a
@@ -47,6 +48,7 @@ __device__ __forceinline__ void cp_async(T* smem, const T* gmem) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // Task descriptors (one per CTA unless stated).
@@ -91,11 +93,26 @@ constexpr int BLK_W = 256;
 // Panel [c, c + bw) of a front (pend = c + bw); xi indexes the panel's
 // 16 x 16 sub-block inverses (BLK_B * BLK_B floats) in the launch's
 // scratch.  For the panel kernel r0 is the first of the CTA's 64 rows
-// (>= pend).
+// (>= pend), and base >= 0 is the stacked tensor-core panel row of front row
+// pend, where the kernel writes the rows it solves (transposed, hi/lo TF32
+// split) for the trailing update; base < 0: no trailing update.
 struct BlkTask {
   int64_t off;
-  int ld, m, c, bw, pend, r0, xi, pad;
+  int ld, m, c, bw, pend, r0, xi, base;
 };
+
+#if defined(__CUDACC__)
+// FP32 -> hi = rna_tf32(x), lo = rna_tf32(x - hi): the operand split of the
+// 4xTF32 tensor-core update (the tensor core reads only the TF32 bits).
+__device__ __forceinline__ void tf32_split(float v, float& hi, float& lo) {
+  unsigned h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
+  const float fh = __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - fh));
+  hi = fh;
+  lo = __uint_as_float(l);
+}
+#endif
 
 // Extend-add of one child contribution column into its parent; the entry
 // (i, j), i >= j, of the child block lands at (max, min) of the mapped rows
@@ -138,7 +155,7 @@ void prepare_blocked_kernels();
 void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, unsigned* status,
                      cudaStream_t s);
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      cudaStream_t s);
+                      float* hi, float* lo, int pitch, cudaStream_t s);
 
 template <typename T> struct Tiles;
 template <> struct Tiles<double> {
@@ -174,6 +191,8 @@ enum LsKind {
 };
 constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
 constexpr int LSOLVE_BW2 = 256;  // columns per solve step
+constexpr int LSOLVE_UPD_ROWS = 32;  // rows per forward-update CTA
+constexpr int LSOLVE_RED_ROWS = 64;  // rows per backward-reduction CTA
 // Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
 // explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
 // index), tt: two 256 x 32 accumulators per front (backward steps alternate

@@ -12,8 +12,9 @@
 //               L_R L_WW^T = A_R by block forward substitution over the same
 //               16-column sub-blocks (the 16 x 16 inverses come from
 //               k_blk_diag);
-//   k_split_t + k_update_tc: the trailing fully-summed columns are updated
-//               with K = W on the tensor cores.
+//   k_update_tc: the trailing fully-summed columns are updated with K = W
+//               on the tensor cores; its operands (the rows below the panel,
+//               transposed and hi/lo split) are written by k_blk_panel.
 // After the last panel the contribution block gets one update with K = n on
 // the tensor cores as well.
 //
@@ -213,7 +214,9 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
 // columns 4*(tid/64) .. +3 of the sub-block).
 __global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ arena,
                                                            const BlkTask* __restrict__ tasks,
-                                                           const float* __restrict__ xinv) {
+                                                           const float* __restrict__ xinv,
+                                                           float* __restrict__ hi,
+                                                           float* __restrict__ lo, int pitch) {
   extern __shared__ __align__(16) float sm[];
   float* Ar = sm;                // Ar[k*ALD + r] = A(r0 + r, k0 + k), then L
   float* Lrow = Ar + PW * ALD;   // Lrow[jj*(PW+1) + k] = L(k0 + q0 + jj, k0 + k), k < q0
@@ -270,6 +273,19 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ a
       if (r < nr && q0 + j0 + jj < w) a[(int64_t)(k0 + q0 + j0 + jj) * ld + r0 + r] = v[jj];
     }
   }
+  if (t.base >= 0) {
+    // the rows just solved, transposed and split, for the trailing
+    // tensor-core update (k contiguous: coalesced writes)
+    __syncthreads();
+    const int64_t row0 = (int64_t)t.base + (r0 - t.pend);
+    for (int e = tid; e < nr * pitch; e += PTHREADS) {
+      const int rr = e / pitch, k = e % pitch;
+      float h, l;
+      tf32_split(k < w ? Ar[k * ALD + rr] : 0.f, h, l);
+      hi[(row0 + rr) * pitch + k] = h;
+      lo[(row0 + rr) * pitch + k] = l;
+    }
+  }
 }
 
 constexpr size_t diag_smem() {
@@ -295,9 +311,9 @@ void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, uns
 }
 
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      cudaStream_t s) {
+                      float* hi, float* lo, int pitch, cudaStream_t s) {
   if (ntask <= 0) return;
-  k_blk_panel<<<ntask, PTHREADS, panel_smem(), s>>>(arena, t, xinv);
+  k_blk_panel<<<ntask, PTHREADS, panel_smem(), s>>>(arena, t, xinv, hi, lo, pitch);
 }
 
 }  // namespace sylver_gb300

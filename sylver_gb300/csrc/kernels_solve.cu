@@ -431,6 +431,7 @@ __global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
 // or reduction (backward) of the rows below, spread over many small CTAs.
 constexpr int BW2 = LSOLVE_BW2;
 constexpr int DMV_ROWS = 16;  // rows of the diagonal mat-vec per CTA (16 CTAs per block)
+constexpr int BRED_ROWS = LSOLVE_RED_ROWS;  // rows per backward-reduction CTA
 template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
 
 // X = inverse of the 256-column diagonal block (column-major, ld 256, lower):
@@ -727,10 +728,12 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
   }
 }
 
-// rows [r0, r0+32) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw.
-// The 32 x 256 tile of L is staged in shared memory by one wave of
+// rows [r0, r0+BR) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw.
+// The BR x 256 tile of L is staged in shared memory by one wave of
 // asynchronous copies; thread (column k = tid % 256, row half h = tid / 256),
-// 512 threads, the halves reduced through shared memory.
+// 512 threads, the halves reduced through shared memory.  Every CTA of a
+// step adds into the same accumulator, so taller tiles mean fewer atomics
+// per address.
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
@@ -738,9 +741,10 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   extern __shared__ __align__(16) unsigned char dsm[];
+  constexpr int BR = BRED_ROWS;
   T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(BW2+1) + k] = L(r0 + ii, c0 + k)
-  ACC* half = reinterpret_cast<ACC*>(dsm + sizeof(T) * 32 * (BW2 + 1));  // [BW2][RG + 1]
-  __shared__ __align__(16) ACC xt[32][RG];
+  ACC* half = reinterpret_cast<ACC*>(dsm + sizeof(T) * BR * (BW2 + 1));  // [BW2][RG + 1]
+  __shared__ __align__(16) ACC xt[BR][RG];
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
@@ -749,9 +753,9 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
   const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / BW2) & 1)) * BW2 * MAXR;
-  const int nrow = min(32, f.m - t.r0);
-  for (int e = tid; e < 32 * BW2; e += 512) {
-    const int ii = e % 32, kk = e / 32;
+  const int nrow = min(BR, f.m - t.r0);
+  for (int e = tid; e < BR * BW2; e += 512) {
+    const int ii = e % BR, kk = e / BR;
     T* dst = &Lt[ii * (BW2 + 1) + kk];
     if (ii < nrow && kk < bw) cp_async(dst, &L[(int64_t)(c0 + kk) * f.ld + t.r0 + ii]);
     else *dst = T(0);
@@ -761,16 +765,16 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    for (int e = tid; e < 32 * RG; e += blockDim.x) {
-      const int ii = e % 32, r = e / 32, row = t.r0 + ii;
+    for (int e = tid; e < BR * RG; e += blockDim.x) {
+      const int ii = e % BR, r = e / BR, row = t.r0 + ii;
       const ACC* src = (row < f.n) ? ysl : xs;
       xt[ii][r] = (ii < nrow && r < nr) ? src[(int64_t)(rg + r) * f.m + row] : ACC(0);
     }
     cp_async_wait_all();
     __syncthreads();
 #pragma unroll 8
-    for (int i2 = 0; i2 < 16; ++i2) {
-      const int ii = h * 16 + i2;
+    for (int i2 = 0; i2 < BR / 2; ++i2) {
+      const int ii = h * (BR / 2) + i2;
       const ACC l = (ACC)Lt[ii * (BW2 + 1) + k];
       const V* xv = reinterpret_cast<const V*>(&xt[ii][0]);
 #pragma unroll
@@ -809,7 +813,7 @@ template <typename T> constexpr size_t fwd_upd_smem() {
   return sizeof(T) * 32 * BW2 + sizeof(T) * 16 * 32 * (RGn<T>::v + 1);
 }
 template <typename T> constexpr size_t bwd_red_smem() {
-  return sizeof(T) * 32 * (BW2 + 1) + sizeof(T) * BW2 * (RGn<T>::v + 1);
+  return sizeof(T) * BRED_ROWS * (BW2 + 1) + sizeof(T) * BW2 * (RGn<T>::v + 1);
 }
 
 }  // namespace

@@ -410,17 +410,14 @@ __global__ void __launch_bounds__(256) k_split_t(const float* __restrict__ arena
   for (int ii = ty; ii < 32; ii += 8) {
     const int i = i0 + ii;
     if (i >= rows) break;
-    const float v = tile[tx][ii];
-    uint32_t h, l;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-    const float fh = __uint_as_float(h);
-    // the tensor core ignores the low 13 bits of a TF32 operand: round the
-    // remainder to TF32 here so that its error is unbiased instead of a
+    // the tensor core ignores the low 13 bits of a TF32 operand: the
+    // remainder is rounded to TF32 so that its error is unbiased instead of a
     // truncation that accumulates along k
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - fh));
+    float fh, fl;
+    tf32_split(tile[tx][ii], fh, fl);
     const int64_t o = (int64_t)(t.base + i) * pitch + k0 + tx;
     hi[o] = fh;
-    lo[o] = __uint_as_float(l);
+    lo[o] = fl;
   }
 }
 

@@ -266,6 +266,18 @@ void FKeep::plan_cholesky() {
       int maxn = 0;
       for (int s : large) maxn = std::max(maxn, st.ncol[s]);
       for (int k0 = 0; k0 < maxn; k0 += PW) {
+        // fronts whose fully-summed columns continue past this panel: their
+        // rows below the panel are stacked (transposed, hi/lo split) by the
+        // panel kernel for the tensor-core update of the trailing columns
+        const int p = k0 + PW;
+        std::vector<int> base(ns, -1);
+        int64_t rows = 0, mxr = 0;
+        for (int s : large)
+          if (p < st.ncol[s]) {
+            base[s] = (int)rows;
+            mxr = std::max<int64_t>(mxr, st.nrow[s] - p);
+            rows += st.nrow[s] - p;
+          }
         // the panel's diagonal block (one CTA per front), then the rows below
         // it (one CTA per 64 rows)
         const int64_t d0 = (int64_t)blkd.size(), p0 = (int64_t)blkp.size();
@@ -274,32 +286,25 @@ void FKeep::plan_cholesky() {
           if (k0 >= n) continue;
           const int pend = std::min(k0 + PW, n);
           const int xi = (int)((int64_t)blkd.size() - d0);
-          blkd.push_back({off[s], ld[s], m, k0, pend - k0, pend, 0, xi, 0});
+          blkd.push_back({off[s], ld[s], m, k0, pend - k0, pend, 0, xi, -1});
           for (int r0 = pend; r0 < m; r0 += 64)
-            blkp.push_back({off[s], ld[s], m, k0, pend - k0, pend, r0, xi, 0});
+            blkp.push_back({off[s], ld[s], m, k0, pend - k0, pend, r0, xi, base[s]});
         }
         if ((int64_t)blkd.size() > d0) {
           ops.push_back({Op::BDIAG, d0, (int64_t)blkd.size(), 0});
           blkinv_count = std::max(blkinv_count, (int64_t)blkd.size() - d0);
         }
-        if ((int64_t)blkp.size() > p0) ops.push_back({Op::BPANEL, p0, (int64_t)blkp.size(), 0});
-        const int p = k0 + PW;
-        std::vector<int> tf;
-        for (int s : large)
-          if (p < st.ncol[s]) tf.push_back(s);
-        if (tf.empty()) continue;
-        int64_t rows = 0, mxr = 0;
+        if ((int64_t)blkp.size() > p0) ops.push_back({Op::BPANEL, p0, (int64_t)blkp.size(), PW});
+        if (rows == 0) continue;
         double fl = 0.0;
-        const int64_t sp0 = (int64_t)tcs.size(), tk0 = (int64_t)tct.size();
-        for (int s : tf) {
+        const int64_t tk0 = (int64_t)tct.size();
+        for (int s : large) {
+          if (base[s] < 0) continue;
           const int m = st.nrow[s], n = st.ncol[s];
-          tcs.push_back({off[s], ld[s], m, p, PW, (int)rows, k0});
           for (int col0 = p; col0 < n; col0 += 128)
             for (int row0 = col0; row0 < m; row0 += 128)
-              tct.push_back({off[s], ld[s], row0, col0, m, n, (int)rows + row0 - p,
-                             (int)rows + col0 - p, PW / 32});
-          mxr = std::max<int64_t>(mxr, m - p);
-          rows += m - p;
+              tct.push_back({off[s], ld[s], row0, col0, m, n, base[s] + row0 - p,
+                             base[s] + col0 - p, PW / 32});
           // lower-triangle entries of rows [p, m) x cols [p, n), times 2K
           const double cnt = (double)(n - p) * m - (0.5 * n * (n - 1.0) - 0.5 * p * (p - 1.0));
           fl += 2.0 * PW * cnt;
@@ -307,7 +312,6 @@ void FKeep::plan_cholesky() {
         const int lvl = (int)tclev.size();
         tclev.push_back({PW, rows, mxr});
         tc_flops.push_back(fl);
-        ops.push_back({Op::SPLIT, sp0, (int64_t)tcs.size(), lvl});
         ops.push_back({Op::TCUPD, tk0, (int64_t)tct.size(), lvl});
       }
     } else {
@@ -505,7 +509,8 @@ void FKeep::run_ops(cudaStream_t s) {
         break;
       case Op::BPANEL:
         if constexpr (std::is_same<T, float>::value)
-          launch_blk_panel(A, blkpanel.as<BlkTask>() + op.a, (int)cnt, blkinv.as<float>(), s);
+          launch_blk_panel(A, blkpanel.as<BlkTask>() + op.a, (int)cnt, blkinv.as<float>(),
+                           panel_hi.as<float>(), panel_lo.as<float>(), op.aux, s);
         break;
       case Op::TCUPD:
         if constexpr (std::is_same<T, float>::value)
@@ -686,7 +691,8 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           int bw = std::min(LB2, d.n - c0), c1 = c0 + bw;
           if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
           else
-            for (int r0 = c1; r0 < d.m; r0 += 32)
+            for (int r0 = c1; r0 < d.m;
+                 r0 += (kind == LS_FWD_UPD2 ? LSOLVE_UPD_ROWS : LSOLVE_RED_ROWS))
               htasks.push_back({f, c0, bw, r0, 0, 0});
         }
         push(ops, kind, a);
