@@ -261,7 +261,7 @@ int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, 
  * an LDL^T factor or nrhs outside 1..32.  No reference counterpart. */
 int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches);
 
-/* Diagnostic: run the tensor-core (tcgen05, 4xTF32) contribution-block
+/* Diagnostic: run the tensor-core (tcgen05, 3xBF16) contribution-block
  * update on a synthetic rows x k panel and report max|C - C_ref| / max|C_ref|
  * against an FP64 host product.  Returns 0 or a reference flag. */
 int sylver_gb300_tc_selfcheck(int rows, int k, double* max_rel_err);

@@ -4,6 +4,9 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#if defined(__CUDACC__)
+#include <cuda_bf16.h>
+#endif
 #include <cstdint>
 #include <stdexcept>
 #include <string>
@@ -90,27 +93,34 @@ struct UpdTask {
 // most BLK_W columns (a multiple of BLK_B by schedule choice).
 constexpr int BLK_B = 64;
 constexpr int BLK_W = 256;
+// k per pipeline stage of the tensor-core update (BF16 elements); stacked
+// panel pitches are multiples of it
+constexpr int TC_KCHUNK = 64;
 // Panel [c, c + bw) of a front (pend = c + bw); xi indexes the panel's
 // 16 x 16 sub-block inverses (BLK_B * BLK_B floats) in the launch's
 // scratch.  For the panel kernel r0 is the first of the CTA's 64 rows
 // (>= pend), and base >= 0 is the stacked tensor-core panel row of front row
-// pend, where the kernel writes the rows it solves (transposed, hi/lo TF32
-// split) for the trailing update; base < 0: no trailing update.
+// pend, where the kernel writes the rows it solves (transposed, split into
+// three BF16 planes) for the trailing update; base < 0: no trailing update.
 struct BlkTask {
   int64_t off;
   int ld, m, c, bw, pend, r0, xi, base;
 };
 
 #if defined(__CUDACC__)
-// FP32 -> hi = rna_tf32(x), lo = rna_tf32(x - hi): the operand split of the
-// 4xTF32 tensor-core update (the tensor core reads only the TF32 bits).
-__device__ __forceinline__ void tf32_split(float v, float& hi, float& lo) {
-  unsigned h, l;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(v));
-  const float fh = __uint_as_float(h);
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(v - fh));
-  hi = fh;
-  lo = __uint_as_float(l);
+// FP32 -> x0 + x1 + x2, three BF16 parts (round to nearest at each step; both
+// remainders are exact in FP32): the operand split of the 3xBF16
+// tensor-core update.  Returned as raw 16-bit patterns.
+__device__ __forceinline__ void bf16x3_split(float v, uint16_t& b0, uint16_t& b1,
+                                             uint16_t& b2) {
+  const __nv_bfloat16 h0 = __float2bfloat16_rn(v);
+  const float r1 = v - __bfloat162float(h0);
+  const __nv_bfloat16 h1 = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(h1);
+  const __nv_bfloat16 h2 = __float2bfloat16_rn(r2);
+  b0 = __bfloat16_as_ushort(h0);
+  b1 = __bfloat16_as_ushort(h1);
+  b2 = __bfloat16_as_ushort(h2);
 }
 #endif
 
@@ -155,7 +165,7 @@ void prepare_blocked_kernels();
 void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, unsigned* status,
                      cudaStream_t s);
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      float* hi, float* lo, int pitch, cudaStream_t s);
+                      uint16_t* planes, int64_t pstride, int pitch, cudaStream_t s);
 
 template <typename T> struct Tiles;
 template <> struct Tiles<double> {

@@ -14,7 +14,8 @@
 //               k_blk_diag);
 //   k_update_tc: the trailing fully-summed columns are updated with K = W
 //               on the tensor cores; its operands (the rows below the panel,
-//               transposed and hi/lo split) are written by k_blk_panel.
+//               transposed and split into three BF16 parts) are written by
+//               k_blk_panel.
 // After the last panel the contribution block gets one update with K = n on
 // the tensor cores as well.
 //
@@ -215,8 +216,8 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
 __global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ arena,
                                                            const BlkTask* __restrict__ tasks,
                                                            const float* __restrict__ xinv,
-                                                           float* __restrict__ hi,
-                                                           float* __restrict__ lo, int pitch) {
+                                                           uint16_t* __restrict__ planes,
+                                                           int64_t pstride, int pitch) {
   extern __shared__ __align__(16) float sm[];
   float* Ar = sm;                // Ar[k*ALD + r] = A(r0 + r, k0 + k), then L
   float* Lrow = Ar + PW * ALD;   // Lrow[jj*(PW+1) + k] = L(k0 + q0 + jj, k0 + k), k < q0
@@ -274,16 +275,18 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ a
     }
   }
   if (t.base >= 0) {
-    // the rows just solved, transposed and split, for the trailing
-    // tensor-core update (k contiguous: coalesced writes)
+    // the rows just solved, transposed and split into three BF16 planes, for
+    // the trailing tensor-core update (k contiguous: coalesced writes)
     __syncthreads();
     const int64_t row0 = (int64_t)t.base + (r0 - t.pend);
     for (int e = tid; e < nr * pitch; e += PTHREADS) {
       const int rr = e / pitch, k = e % pitch;
-      float h, l;
-      tf32_split(k < w ? Ar[k * ALD + rr] : 0.f, h, l);
-      hi[(row0 + rr) * pitch + k] = h;
-      lo[(row0 + rr) * pitch + k] = l;
+      uint16_t b0, b1, b2;
+      bf16x3_split(k < w ? Ar[k * ALD + rr] : 0.f, b0, b1, b2);
+      const int64_t o = (row0 + rr) * pitch + k;
+      planes[o] = b0;
+      planes[pstride + o] = b1;
+      planes[2 * pstride + o] = b2;
     }
   }
 }
@@ -311,9 +314,9 @@ void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, uns
 }
 
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      float* hi, float* lo, int pitch, cudaStream_t s) {
+                      uint16_t* planes, int64_t pstride, int pitch, cudaStream_t s) {
   if (ntask <= 0) return;
-  k_blk_panel<<<ntask, PTHREADS, panel_smem(), s>>>(arena, t, xinv, hi, lo, pitch);
+  k_blk_panel<<<ntask, PTHREADS, panel_smem(), s>>>(arena, t, xinv, planes, pstride, pitch);
 }
 
 }  // namespace sylver_gb300

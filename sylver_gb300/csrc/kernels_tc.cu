@@ -1,25 +1,31 @@
 // Tensor-core Schur-complement update for FP32 fronts: C -= A B^T on the
-// 5th-generation tensor cores (tcgen05, kind::tf32) with the accumulator in
-// tensor memory and operands staged by TMA.
+// 5th-generation tensor cores (tcgen05, kind::f16 with BF16 operands) with
+// the accumulator in tensor memory and operands staged by TMA.
 //
-// Accuracy: 4xTF32.  Each operand is split into hi = rna_tf32(x) and
-// lo = rna_tf32(x - hi), and C -= Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T +
-// Alo Blo^T: the products are within FP32 rounding of the exact ones.  The
+// Accuracy: 3xBF16 with six products.  Each FP32 operand is split exactly
+// into three BF16 parts x = x0 + x1 + x2 (x1 ~ 2^-8 x, x2 ~ 2^-16 x; the
+// remainder is below 2^-24 x), and C -= A0 B0^T + A0 B1^T + A1 B0^T +
+// A1 B1^T + A0 B2^T + A2 B0^T; the dropped products are below 2^-23 of the
+// exact one, so each product is within FP32 rounding -- closer than a 4xTF32
+// split (hi/lo of 11 bits each, 2^-22) at three quarters of its MMA time,
+// since a BF16 MMA does twice the work of a TF32 one in the same time.  The
 // tensor-core accumulator does not round to nearest, so its error over a long
-// k range grows linearly (measured: 16x an FP32 dot product at k = 4096); the
-// accumulator is therefore drained into FP32 registers after every 32-wide k
-// chunk and the chunks are summed there, which brings the update to FP32
-// accuracy and lets FP64 refinement converge as for SIMT FP32 factors.
+// k range grows linearly (measured with TF32 operands: 16x an FP32 dot product
+// at k = 4096); the accumulator is therefore drained into FP32 registers after
+// every 64-wide k chunk and the chunks are summed there, which brings the
+// update to FP32 accuracy and lets FP64 refinement converge as for SIMT FP32
+// factors.
 //
-// Operand layout: TF32 MMAs read K-major shared-memory tiles, so A and B come
-// from a transposed copy of the contribution rows of L ("panel rows", one row
-// per front row, k contiguous, zero-padded to a multiple of 32) stacked for all
-// fronts of a level in one buffer with a fixed pitch; one 2D tensor map per
-// level covers it.  TMA boxes are 32 (k) x 128 (rows) FP32 with 128-byte
-// swizzle, matching the tcgen05 K-major SWIZZLE_128B canonical layout.
+// Operand layout: the MMAs read K-major shared-memory tiles, so A and B come
+// from a transposed copy of the rows of L below the eliminated columns
+// ("panel rows", one row per front row, k contiguous, zero-padded to a
+// multiple of 64) stacked for all fronts of a launch with a fixed pitch, one
+// plane per BF16 part; one 2D tensor map per plane covers it.  TMA boxes are
+// 64 (k) x 128 (rows) BF16 with 128-byte swizzle, matching the tcgen05
+// K-major SWIZZLE_128B canonical layout.
 //
-// A persistent CTA per SM walks the level's 128 x 128 tiles (10 warps): a TMA
-// producer, an MMA issuer (16 MMAs per 32-wide k chunk; tcgen05.commit
+// A persistent CTA per SM walks the launch's 128 x 128 tiles (10 warps): a TMA
+// producer, an MMA issuer (24 MMAs per 64-wide k chunk; tcgen05.commit
 // releases a stage and signals an accumulator) and eight epilogue warps that
 // tcgen05.ld their 32 TMEM lanes after every chunk and subtract it from the
 // C values they hold in registers while the next chunks' MMAs run in the
@@ -37,10 +43,11 @@ namespace sylver_gb300 {
 
 namespace {
 
-constexpr int TC_M = 128, TC_N = 128, TC_KC = 32;  // tile rows, cols, k per stage
-constexpr int TC_STAGES = 3;
-constexpr int TILE_BYTES = TC_M * TC_KC * 4;        // 16 KiB per operand tile
-constexpr int STAGE_BYTES = 4 * TILE_BYTES;         // Ahi, Alo, Bhi, Blo
+constexpr int TC_M = 128, TC_N = 128, TC_KC = TC_KCHUNK;  // tile rows, cols, k per stage
+constexpr int TC_STAGES = 2;
+constexpr int TC_PLANES = 3;                        // BF16 parts of an operand
+constexpr int TILE_BYTES = TC_M * TC_KC * 2;        // 16 KiB per operand tile
+constexpr int STAGE_BYTES = 2 * TC_PLANES * TILE_BYTES;  // A0 A1 A2 B0 B1 B2
 constexpr long WAIT_LIMIT = 1L << 24;               // try_wait polls before giving up
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -110,18 +117,20 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-// instruction descriptor: D f32, A/B tf32, both K-major, N = 128, M = 128
-__host__ __device__ constexpr uint32_t tf32_idesc() {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+// instruction descriptor (kind::f16): D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9 and 10-12 = 1), both K-major, N >> 3 in bits 17-22, M >> 4 in
+// bits 24-28
+__host__ __device__ constexpr uint32_t bf16_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
          ((uint32_t)(TC_M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t ad, uint64_t bd,
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t ad, uint64_t bd,
                                          uint32_t idesc, uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
       "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate)
       : "memory");
 }
@@ -196,8 +205,9 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* b, uint32_t parity,
 //                   subtracts every chunk, releases the accumulator after
 //                   each, and stores C after the tile's last chunk.
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    k_update_tc(const __grid_constant__ CUtensorMap map_hi,
-                const __grid_constant__ CUtensorMap map_lo, float* __restrict__ arena,
+    k_update_tc(const __grid_constant__ CUtensorMap map0,
+                const __grid_constant__ CUtensorMap map1,
+                const __grid_constant__ CUtensorMap map2, float* __restrict__ arena,
                 const TcTask* __restrict__ tasks, int ntask, unsigned* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1 KiB alignment for the swizzled tiles
@@ -252,10 +262,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           unsigned char* st = smem + s * STAGE_BYTES;
           mbar_expect_tx(&full[s], STAGE_BYTES);
           const int x = kc * TC_KC;
-          tma_load_2d(st + 0 * TILE_BYTES, &map_hi, x, t.a_row, &full[s]);
-          tma_load_2d(st + 1 * TILE_BYTES, &map_lo, x, t.a_row, &full[s]);
-          tma_load_2d(st + 2 * TILE_BYTES, &map_hi, x, t.b_row, &full[s]);
-          tma_load_2d(st + 3 * TILE_BYTES, &map_lo, x, t.b_row, &full[s]);
+          tma_load_2d(st + 0 * TILE_BYTES, &map0, x, t.a_row, &full[s]);
+          tma_load_2d(st + 1 * TILE_BYTES, &map1, x, t.a_row, &full[s]);
+          tma_load_2d(st + 2 * TILE_BYTES, &map2, x, t.a_row, &full[s]);
+          tma_load_2d(st + 3 * TILE_BYTES, &map0, x, t.b_row, &full[s]);
+          tma_load_2d(st + 4 * TILE_BYTES, &map1, x, t.b_row, &full[s]);
+          tma_load_2d(st + 5 * TILE_BYTES, &map2, x, t.b_row, &full[s]);
           issued = g + 1;
         }
         if (!ok) break;
@@ -263,7 +275,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      const uint32_t idesc = tf32_idesc();
+      const uint32_t idesc = bf16_idesc();
       int g = 0, it = 0;  // it counts accumulator uses (one per k chunk)
       bool ok = true;
       for (int ti = blockIdx.x; ti < ntask && ok; ti += gridDim.x) {
@@ -285,19 +297,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t d = tmem + (uint32_t)(a * TC_N);
           unsigned char* st = smem + s * STAGE_BYTES;
-          const uint64_t ahi = sw128_desc(su32(st + 0 * TILE_BYTES));
-          const uint64_t alo = sw128_desc(su32(st + 1 * TILE_BYTES));
-          const uint64_t bhi = sw128_desc(su32(st + 2 * TILE_BYTES));
-          const uint64_t blo = sw128_desc(su32(st + 3 * TILE_BYTES));
+          const uint64_t a0 = sw128_desc(su32(st + 0 * TILE_BYTES));
+          const uint64_t a1 = sw128_desc(su32(st + 1 * TILE_BYTES));
+          const uint64_t a2 = sw128_desc(su32(st + 2 * TILE_BYTES));
+          const uint64_t b0 = sw128_desc(su32(st + 3 * TILE_BYTES));
+          const uint64_t b1 = sw128_desc(su32(st + 4 * TILE_BYTES));
+          const uint64_t b2 = sw128_desc(su32(st + 5 * TILE_BYTES));
 #pragma unroll
-          for (int kk = 0; kk < TC_KC / 8; ++kk) {
-            // 8 tf32 = 32 bytes further along k inside the swizzled row;
+          for (int kk = 0; kk < TC_KC / 16; ++kk) {
+            // 16 bf16 = 32 bytes further along k inside the swizzled row;
             // small products first
             const uint64_t adv = (uint64_t)((kk * 32) >> 4);
-            mma_tf32(d, alo + adv, blo + adv, idesc, kk > 0 ? 1u : 0u);
-            mma_tf32(d, ahi + adv, blo + adv, idesc, 1u);
-            mma_tf32(d, alo + adv, bhi + adv, idesc, 1u);
-            mma_tf32(d, ahi + adv, bhi + adv, idesc, 1u);
+            mma_bf16(d, a2 + adv, b0 + adv, idesc, kk > 0 ? 1u : 0u);
+            mma_bf16(d, a0 + adv, b2 + adv, idesc, 1u);
+            mma_bf16(d, a1 + adv, b1 + adv, idesc, 1u);
+            mma_bf16(d, a1 + adv, b0 + adv, idesc, 1u);
+            mma_bf16(d, a0 + adv, b1 + adv, idesc, 1u);
+            mma_bf16(d, a0 + adv, b0 + adv, idesc, 1u);
           }
           mma_commit(&empty[s]);
           mma_commit(&acc_full[a]);
@@ -386,15 +402,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                  : "memory");
 }
 
-// Transposed, hi/lo-split copy of rows [n, m) x cols [c0, c0 + K) of one
-// front into the stacked panel buffer: out[(base + i - n) * pitch + k];
-// columns [K, pitch) are zero.  A 32 x 32 tile per CTA (32 x 8 threads)
-// goes through shared memory, so both the column reads from the front and
-// the row writes to the panel are coalesced.
+// Transposed, 3xBF16-split copy of rows [n, m) x cols [c0, c0 + K) of one
+// front into the stacked panel planes: plane q at planes + q * pstride,
+// element (base + i - n) * pitch + k; columns [K, pitch) are zero.  A 32 x 32
+// tile per CTA (32 x 8 threads) goes through shared memory, so both the
+// column reads from the front and the row writes to the planes are
+// coalesced.
 __global__ void __launch_bounds__(256) k_split_t(const float* __restrict__ arena,
                                                  const TcSplit* __restrict__ sp,
-                                                 float* __restrict__ hi, float* __restrict__ lo,
-                                                 int pitch) {
+                                                 uint16_t* __restrict__ planes,
+                                                 int64_t pstride, int pitch) {
   __shared__ float tile[32][33];  // tile[k][i]
   const TcSplit t = sp[blockIdx.z];
   const int rows = t.m - t.n;
@@ -410,14 +427,12 @@ __global__ void __launch_bounds__(256) k_split_t(const float* __restrict__ arena
   for (int ii = ty; ii < 32; ii += 8) {
     const int i = i0 + ii;
     if (i >= rows) break;
-    // the tensor core ignores the low 13 bits of a TF32 operand: the
-    // remainder is rounded to TF32 so that its error is unbiased instead of a
-    // truncation that accumulates along k
-    float fh, fl;
-    tf32_split(tile[tx][ii], fh, fl);
+    uint16_t b0, b1, b2;
+    bf16x3_split(tile[tx][ii], b0, b1, b2);
     const int64_t o = (int64_t)(t.base + i) * pitch + k0 + tx;
-    hi[o] = fh;
-    lo[o] = fl;
+    planes[o] = b0;
+    planes[pstride + o] = b1;
+    planes[2 * pstride + o] = b2;
   }
 }
 
@@ -447,32 +462,33 @@ void prepare_tc_kernels() {
   SG_CUDA(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
 }
 
-void make_panel_map(CUtensorMap* map, const float* base, int64_t rows, int pitch) {
-  // 2D: x = k (contiguous, pitch elements), y = stacked panel row
+void make_panel_map(CUtensorMap* map, const uint16_t* base, int64_t rows, int pitch) {
+  // 2D: x = k (contiguous, pitch BF16 elements), y = stacked panel row
   cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)std::max<int64_t>(rows, 1)};
-  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(uint16_t)};
   cuuint32_t box[2] = {(cuuint32_t)TC_KC, (cuuint32_t)TC_M};
   cuuint32_t estr[2] = {1, 1};
-  CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides,
+  CUresult r = encode_fn()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void*)base, dims, strides,
                            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw CudaError("cuTensorMapEncodeTiled failed");
 }
 
 void launch_split_t(const float* arena, const TcSplit* sp, int nsplit, int64_t max_rows,
-                    float* hi, float* lo, int pitch, cudaStream_t s) {
+                    uint16_t* planes, int64_t pstride, int pitch, cudaStream_t s) {
   if (nsplit <= 0 || max_rows <= 0) return;
-  // pitch is a multiple of 32: every k of a tile lies inside the row
+  // pitch is a multiple of 64: every k of a tile lies inside the row
   dim3 grid((unsigned)((max_rows + 31) / 32), (unsigned)(pitch / 32), (unsigned)nsplit);
-  k_split_t<<<grid, 256, 0, s>>>(arena, sp, hi, lo, pitch);
+  k_split_t<<<grid, 256, 0, s>>>(arena, sp, planes, pstride, pitch);
 }
 
-void launch_update_tc(const CUtensorMap& hi, const CUtensorMap& lo, float* arena,
-                      const TcTask* t, int ntask, unsigned* err, cudaStream_t s) {
+void launch_update_tc(const CUtensorMap* maps, float* arena, const TcTask* t, int ntask,
+                      unsigned* err, cudaStream_t s) {
   if (ntask <= 0) return;
   // one persistent CTA per SM (the shared-memory ring admits one per SM)
   const int grid = std::min(ntask, g_num_sms > 0 ? g_num_sms : 148);
-  k_update_tc<<<grid, TC_THREADS, tc_smem_bytes(), s>>>(hi, lo, arena, t, ntask, err);
+  k_update_tc<<<grid, TC_THREADS, tc_smem_bytes(), s>>>(maps[0], maps[1], maps[2], arena, t,
+                                                         ntask, err);
 }
 
 }  // namespace sylver_gb300

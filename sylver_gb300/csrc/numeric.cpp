@@ -267,7 +267,7 @@ void FKeep::plan_cholesky() {
       for (int s : large) maxn = std::max(maxn, st.ncol[s]);
       for (int k0 = 0; k0 < maxn; k0 += PW) {
         // fronts whose fully-summed columns continue past this panel: their
-        // rows below the panel are stacked (transposed, hi/lo split) by the
+        // rows below the panel are stacked (transposed, 3xBF16 split) by the
         // panel kernel for the tensor-core update of the trailing columns
         const int p = k0 + PW;
         std::vector<int> base(ns, -1);
@@ -304,7 +304,7 @@ void FKeep::plan_cholesky() {
           for (int col0 = p; col0 < n; col0 += 128)
             for (int row0 = col0; row0 < m; row0 += 128)
               tct.push_back({off[s], ld[s], row0, col0, m, n, base[s] + row0 - p,
-                             base[s] + col0 - p, PW / 32});
+                             base[s] + col0 - p, PW / TC_KCHUNK});
           // lower-triangle entries of rows [p, m) x cols [p, n), times 2K
           const double cnt = (double)(n - p) * m - (0.5 * n * (n - 1.0) - 0.5 * p * (p - 1.0));
           fl += 2.0 * PW * cnt;
@@ -341,7 +341,7 @@ void FKeep::plan_cholesky() {
       if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
     }
     // contribution blocks: one Schur-complement update with K = n, on the
-    // tensor cores (FP32, 4xTF32) for blocks of at least 64 rows
+    // tensor cores (FP32, 3xBF16) for blocks of at least 64 rows
     int64_t u0 = (int64_t)upds.size();
     std::vector<int> tcf;
     for (int s : large) {
@@ -360,7 +360,7 @@ void FKeep::plan_cholesky() {
     if (!tcf.empty()) {
       int pitch = 0;
       int64_t rows = 0, mx = 0;
-      for (int s : tcf) pitch = std::max(pitch, (st.ncol[s] + 31) / 32 * 32);
+      for (int s : tcf) pitch = std::max(pitch, (st.ncol[s] + TC_KCHUNK - 1) / TC_KCHUNK * TC_KCHUNK);
       int64_t sp0 = (int64_t)tcs.size(), tk0 = (int64_t)tct.size();
       for (int s : tcf) {
         int m = st.nrow[s], n = st.ncol[s];
@@ -368,7 +368,8 @@ void FKeep::plan_cholesky() {
         for (int cj = 0; cj * 128 < m - n; ++cj)
           for (int ri = cj; ri * 128 < m - n; ++ri)
             tct.push_back({off[s], ld[s], n + ri * 128, n + cj * 128, m, m,
-                           (int)rows + ri * 128, (int)rows + cj * 128, (n + 31) / 32});
+                           (int)rows + ri * 128, (int)rows + cj * 128,
+                           (n + TC_KCHUNK - 1) / TC_KCHUNK});
         mx = std::max(mx, (int64_t)(m - n));
         rows += m - n;
       }
@@ -454,14 +455,15 @@ void FKeep::upload_static(cudaStream_t s) {
   if (!tclev.empty()) {
     int64_t cap = 0;
     for (auto& L : tclev) cap = std::max(cap, L.rows * L.pitch);
-    panel_hi.ensure((size_t)cap * sizeof(float));
-    panel_lo.ensure((size_t)cap * sizeof(float));
-    tmap_hi.resize(tclev.size());
-    tmap_lo.resize(tclev.size());
-    for (size_t l = 0; l < tclev.size(); ++l) {
-      make_panel_map(&tmap_hi[l], panel_hi.as<float>(), tclev[l].rows, tclev[l].pitch);
-      make_panel_map(&tmap_lo[l], panel_lo.as<float>(), tclev[l].rows, tclev[l].pitch);
-    }
+    // three BF16 planes of cap elements each (plane stride rounded to 64
+    // elements keeps every plane 128-byte aligned)
+    plane_stride = (std::max<int64_t>(cap, 1) + 63) / 64 * 64;
+    tcplanes.ensure((size_t)3 * plane_stride * sizeof(uint16_t));
+    tmaps.resize(3 * tclev.size());
+    for (size_t l = 0; l < tclev.size(); ++l)
+      for (int q = 0; q < 3; ++q)
+        make_panel_map(&tmaps[3 * l + q], tcplanes.as<uint16_t>() + q * plane_stride,
+                       tclev[l].rows, tclev[l].pitch);
   }
 }
 
@@ -501,7 +503,7 @@ void FKeep::run_ops(cudaStream_t s) {
       case Op::SPLIT:
         if constexpr (std::is_same<T, float>::value)
           launch_split_t(A, tcsplit.as<TcSplit>() + op.a, (int)cnt, tclev[op.aux].max_rows,
-                         panel_hi.as<float>(), panel_lo.as<float>(), tclev[op.aux].pitch, s);
+                         tcplanes.as<uint16_t>(), plane_stride, tclev[op.aux].pitch, s);
         break;
       case Op::BDIAG:
         if constexpr (std::is_same<T, float>::value)
@@ -510,12 +512,12 @@ void FKeep::run_ops(cudaStream_t s) {
       case Op::BPANEL:
         if constexpr (std::is_same<T, float>::value)
           launch_blk_panel(A, blkpanel.as<BlkTask>() + op.a, (int)cnt, blkinv.as<float>(),
-                           panel_hi.as<float>(), panel_lo.as<float>(), op.aux, s);
+                           tcplanes.as<uint16_t>(), plane_stride, op.aux, s);
         break;
       case Op::TCUPD:
         if constexpr (std::is_same<T, float>::value)
-          launch_update_tc(tmap_hi[op.aux], tmap_lo[op.aux], A, tctask.as<TcTask>() + op.a,
-                           (int)cnt, tcerr.as<unsigned>(), s);
+          launch_update_tc(&tmaps[3 * op.aux], A, tctask.as<TcTask>() + op.a, (int)cnt,
+                           tcerr.as<unsigned>(), s);
         break;
     }
   }

@@ -167,15 +167,17 @@ struct FKeep {
   bool action = true;
   std::vector<double> scale;  // user scaling S (empty: none)
 
-  // tensor-core contribution-block updates (FP32 Cholesky)
+  // tensor-core updates (FP32 Cholesky): stacked transposed operands, split
+  // into three BF16 planes
   bool use_tc = true;
   struct TcLevel {
     int pitch;
     int64_t rows, max_rows;  // stacked panel rows; most rows of one split
   };
   std::vector<TcLevel> tclev;
-  std::vector<CUtensorMap> tmap_hi, tmap_lo;
-  DevMem tcsplit, tctask, panel_hi, panel_lo, tcerr;
+  std::vector<CUtensorMap> tmaps;   // three per tensor-core launch (one per BF16 plane)
+  DevMem tcsplit, tctask, tcplanes, tcerr;
+  int64_t plane_stride = 0;        // elements between the BF16 planes
   // blocked large-front path (FP32): diagonal-block and panel tasks, and the
   // 64 x 64 inverses of one diagonal-block launch
   DevMem blkdiag, blkpanel, blkinv;

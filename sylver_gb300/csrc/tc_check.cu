@@ -17,33 +17,34 @@ extern "C" int sylver_gb300_tc_selfcheck(int rows, int k, double* max_rel_err) {
   Runtime& rt = Runtime::get();
   if (!rt.init()) return SYLVER_ERROR_CUDA_UNKNOWN;
   try {
-    const int m = k + rows, ld = (m + 3) / 4 * 4, pitch = (k + 31) / 32 * 32;
+    const int m = k + rows, ld = (m + 3) / 4 * 4,
+              pitch = (k + TC_KCHUNK - 1) / TC_KCHUNK * TC_KCHUNK;
     std::vector<float> h((size_t)ld * m, 0.f);
     std::mt19937 gen(7);
     std::uniform_real_distribution<float> U(-1.f, 1.f);
     for (int c = 0; c < k; ++c)
       for (int r = k; r < m; ++r) h[(size_t)c * ld + r] = U(gen);
-    DevMem arena, hi, lo, sp, tk, err;
+    DevMem arena, planes, sp, tk, err;
     arena.ensure(h.size() * sizeof(float));
     SG_CUDA(cudaMemcpy(arena.p, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
-    hi.ensure((size_t)rows * pitch * sizeof(float));
-    lo.ensure((size_t)rows * pitch * sizeof(float));
+    const int64_t pstride = ((int64_t)rows * pitch + 63) / 64 * 64;
+    planes.ensure((size_t)3 * pstride * sizeof(uint16_t));
     std::vector<TcSplit> hs{{0, ld, m, k, k, 0, 0}};
     std::vector<TcTask> ht;
     for (int cj = 0; cj * 128 < rows; ++cj)
       for (int ri = cj; ri * 128 < rows; ++ri)
         ht.push_back({0, ld, k + ri * 128, k + cj * 128, m, m, ri * 128, cj * 128,
-                      (k + 31) / 32});
+                      (k + TC_KCHUNK - 1) / TC_KCHUNK});
     sp.upload(hs, rt.stream);
     tk.upload(ht, rt.stream);
     err.ensure(sizeof(unsigned));
     SG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(unsigned), rt.stream));
-    CUtensorMap mhi, mlo;
-    make_panel_map(&mhi, hi.as<float>(), rows, pitch);
-    make_panel_map(&mlo, lo.as<float>(), rows, pitch);
-    launch_split_t(arena.as<float>(), sp.as<TcSplit>(), 1, (int64_t)rows, hi.as<float>(),
-                   lo.as<float>(), pitch, rt.stream);
-    launch_update_tc(mhi, mlo, arena.as<float>(), tk.as<TcTask>(), (int)ht.size(),
+    CUtensorMap maps[3];
+    for (int q = 0; q < 3; ++q)
+      make_panel_map(&maps[q], planes.as<uint16_t>() + q * pstride, rows, pitch);
+    launch_split_t(arena.as<float>(), sp.as<TcSplit>(), 1, (int64_t)rows,
+                   planes.as<uint16_t>(), pstride, pitch, rt.stream);
+    launch_update_tc(maps, arena.as<float>(), tk.as<TcTask>(), (int)ht.size(),
                      err.as<unsigned>(), rt.stream);
     unsigned herr = 0;
     SG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, rt.stream));

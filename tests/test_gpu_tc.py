@@ -1,12 +1,13 @@
-"""Tensor-core (tcgen05, 4xTF32) contribution-block update.
+"""Tensor-core (tcgen05, 3xBF16) Schur-complement update.
 
 The self-check runs the same transposed split + TMA + tcgen05 path as the
 factorization on a synthetic panel and compares with an FP64 host product;
-4xTF32 must be close to FP32 accuracy: the bound 1e-5 is two orders of
-magnitude below what a single TF32 product (unit roundoff ~5e-4) gives and
-about what FP32 accumulation over K <= 257 terms gives.  The larger cases
-have more tiles than the GPU has SMs, so persistent CTAs walk several tiles
-and reuse both accumulators and every pipeline stage."""
+3xBF16 with six products and FP32 accumulation of 64-wide k chunks must be
+close to FP32 accuracy: the bound 1e-5 is two orders of magnitude below what
+a single BF16 product (unit roundoff ~4e-3) gives and about what FP32
+accumulation over K <= 257 terms gives.  The larger cases have more tiles
+than the GPU has SMs, so persistent CTAs walk several tiles and reuse every
+accumulator and pipeline stage."""
 import ctypes
 
 import pytest
