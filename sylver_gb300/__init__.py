@@ -303,11 +303,12 @@ class Factor:
                 for i, k in enumerate(self.KINDS)}
 
     SOLVE_KINDS = ("small_fwd", "small_bwd", "gather_fwd", "gather_bwd", "scatter_fwd",
-                   "scatter_bwd", "diag_fwd", "rows_fwd", "rows_bwd", "diag_bwd")
+                   "scatter_bwd", "diag_fwd", "rows_fwd", "rows_bwd", "diag_bwd", "cb_fwd",
+                   "cb_bwd")
 
     def profile_solve(self, nrhs=16):
         """Per-kernel-kind timing of one forward + backward sweep (no graph)."""
-        ms = np.zeros(10); nl = np.zeros(10, dtype=np.int64)
+        ms = np.zeros(12); nl = np.zeros(12, dtype=np.int64)
         rc = load().sylver_gb300_profile_solve(self.fkeep, int(nrhs), _p(ms), _p(nl))
         if rc != 0:
             raise RuntimeError(f"profile_solve failed: {rc}")

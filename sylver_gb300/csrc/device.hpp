@@ -197,12 +197,19 @@ struct LTask {
 };
 enum LsKind {
   LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD,
-  LS_FWD_DIAG2, LS_FWD_UPD2, LS_BWD_RED2, LS_BWD_DIAG2
+  LS_FWD_DIAG2, LS_FWD_UPD2, LS_BWD_RED2, LS_BWD_DIAG2,
+  LS_FWD_CB,   // contribution rows of a front, once after all its blocks (forward)
+  LS_BWD_CB    // contribution rows' share of every block, once before the steps (backward)
 };
 constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
 constexpr int LSOLVE_BW2 = 256;  // columns per solve step
 constexpr int LSOLVE_UPD_ROWS = 32;  // rows per forward-update CTA
 constexpr int LSOLVE_RED_ROWS = 64;  // rows per backward-reduction CTA
+constexpr int LSOLVE_CB_ROWS = 256;  // contribution rows per backward CB CTA
+// Large fronts are swept block by block over their fully-summed rows only;
+// the contribution rows (>= n) are updated once per front after the forward
+// blocks (LS_FWD_CB) and contribute to every backward block once, before the
+// backward blocks (LS_BWD_CB).
 // Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
 // explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
 // index), tt: two 256 x 32 accumulators per front (backward steps alternate
@@ -225,6 +232,9 @@ struct LsArgs {
   const T* inv2;            // 256x256 inverses of the solve-step diagonal blocks
   const int64_t* inv2_off;  // per front of the level
   const T* inv2t;           // the same inverses transposed (row-major)
+  // per 256-column block of every large front: the contribution rows' share
+  // of the backward reduction, 256 x 32 (block index inv2_off[f]/256^2 + c0/256)
+  ACC* tcb;
 };
 // Inverse of each 256-column diagonal block from its 64x64 inverses: task
 // (front f, c0, bw), output at inv2 + inv2_off[f] + (c0/256)*256*256

@@ -356,9 +356,13 @@ __global__ void k_lgather(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, boo
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   if (!fwd && t.r0 == 0) {
-    // both backward accumulators of this front start at zero
+    // both backward accumulators of this front start at zero, and so do its
+    // contribution-row sums
     ACC* tf = a.tt + (int64_t)t.f * 2 * LSOLVE_BW2 * MAXR;
     for (int e = threadIdx.x; e < 2 * LSOLVE_BW2 * MAXR; e += blockDim.x) tf[e] = ACC(0);
+    const int nb = (f.n + LSOLVE_BW2 - 1) / LSOLVE_BW2;
+    ACC* cb = a.tcb + (a.inv2_off[t.f] / ((int64_t)LSOLVE_BW2 * LSOLVE_BW2)) * LSOLVE_BW2 * MAXR;
+    for (int e = threadIdx.x; e < nb * LSOLVE_BW2 * MAXR; e += blockDim.x) cb[e] = ACC(0);
   }
   const int i = t.r0 + threadIdx.x;
   if (i >= f.m) return;
@@ -432,6 +436,7 @@ __global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
 constexpr int BW2 = LSOLVE_BW2;
 constexpr int DMV_ROWS = 16;  // rows of the diagonal mat-vec per CTA (16 CTAs per block)
 constexpr int BRED_ROWS = LSOLVE_RED_ROWS;  // rows per backward-reduction CTA
+constexpr int CB_CHUNK = LSOLVE_CB_ROWS;    // contribution rows per backward CB CTA
 template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
 
 // X = inverse of the 256-column diagonal block (column-major, ld 256, lower):
@@ -569,6 +574,7 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
   ACC* tf = a.tt + (int64_t)t.f * 2 * BW2 * MAXR;
   ACC* tcur = tf + ((c0 / BW2) & 1) * BW2 * MAXR;
   ACC* tnext = tf + (((c0 / BW2) + 1) & 1) * BW2 * MAXR;
+  const ACC* tcbb = a.tcb + (a.inv2_off[t.f] / ((int64_t)BW2 * BW2) + c0 / BW2) * BW2 * MAXR;
   // entries k of v (and columns of the matrix slice) this CTA needs
   const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + DR), nk = khi - klo;
   if (i0 < bw) {
@@ -593,7 +599,7 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
         v[u] = ACC(0);
         if (e < nk * RG && r < nr) {
           v[u] = xs[(int64_t)(rg + r) * m + c0 + k];
-          if (BWD) v[u] -= tcur[k * MAXR + rg + r];
+          if (BWD) v[u] -= tcur[k * MAXR + rg + r] + tcbb[k * MAXR + rg + r];
         }
       }
 #pragma unroll
@@ -645,8 +651,8 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
     for (int e = tid; e < DR * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
 }
 
-// rows [r0, r0+32): xs_i -= L_i,blk y_blk; thread (row, 16-column group g),
-// 512 threads.  The 32 x 256 tile of L is staged in shared memory by one wave
+// rows [r0, r0+32) < n: xs_i -= L_i,blk y_blk; thread (row, 16-column
+// group g), 512 threads.  The 32 x 256 tile of L is staged in shared memory by one wave
 // of asynchronous copies; y is read as 16-byte vectors (one broadcast per
 // warp).
 template <typename T, typename ACC>
@@ -662,52 +668,59 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, rr = tid % 32, g = tid / 32;
+  const int tid = threadIdx.x, rr = tid % 32, g = tid / 32;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  const int nrow = min(32, f.m - t.r0);
-  for (int e = tid; e < BW2 * 32; e += 512) {
-    const int r2 = e & 31, k = e >> 5;
-    if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
-    else Lt[e] = T(0);
-  }
+  // rows [r0, r0+32) below the block, fully summed (< n); the contribution
+  // rows are updated once per front by k_fwd_cb
+  const int nrow = min(32, f.n - t.r0);
+  const int cfirst = t.c0, clast = t.c0 + t.bw;
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
-    {
-      constexpr int NL = BW2 * RG / 512;
-      ACC v[NL];
-#pragma unroll
-      for (int u = 0; u < NL; ++u) {
-        const int e = tid + 512 * u, k = e % BW2, r = e / BW2;
-        v[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
-      }
-#pragma unroll
-      for (int u = 0; u < NL; ++u) {
-        const int e = tid + 512 * u;
-        yb[(e % BW2) * RG + e / BW2] = v[u];
-      }
-    }
-    cp_async_wait_all();
-    __syncthreads();
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-#pragma unroll 8
-    for (int kk = 0; kk < 16; ++kk) {
-      const int k = g * 16 + kk;
-      const ACC l = (ACC)Lt[k * 32 + rr];
-      const V* yv = reinterpret_cast<const V*>(yb + k * RG);
+    for (int c0 = cfirst; c0 < clast; c0 += BW2) {
+      const int bw = min(BW2, clast - c0);
+      __syncthreads();  // the previous block's tiles are no longer read
+      for (int e = tid; e < BW2 * 32; e += 512) {
+        const int r2 = e & 31, k = e >> 5;
+        if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
+        else Lt[e] = T(0);
+      }
+      {
+        constexpr int NL = BW2 * RG / 512;
+        ACC v[NL];
 #pragma unroll
-      for (int q = 0; q < RG / VW; ++q) {
-        const V y4 = yv[q];
-        if constexpr (VW == 4) {
-          acc[4 * q + 0] += l * y4.x;
-          acc[4 * q + 1] += l * y4.y;
-          acc[4 * q + 2] += l * y4.z;
-          acc[4 * q + 3] += l * y4.w;
-        } else {
-          acc[2 * q + 0] += l * y4.x;
-          acc[2 * q + 1] += l * y4.y;
+        for (int u = 0; u < NL; ++u) {
+          const int e = tid + 512 * u, k = e % BW2, r = e / BW2;
+          v[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+        }
+#pragma unroll
+        for (int u = 0; u < NL; ++u) {
+          const int e = tid + 512 * u;
+          yb[(e % BW2) * RG + e / BW2] = v[u];
+        }
+      }
+      cp_async_wait_all();
+      __syncthreads();
+#pragma unroll 8
+      for (int kk = 0; kk < 16; ++kk) {
+        const int k = g * 16 + kk;
+        const ACC l = (ACC)Lt[k * 32 + rr];
+        const V* yv = reinterpret_cast<const V*>(yb + k * RG);
+#pragma unroll
+        for (int q = 0; q < RG / VW; ++q) {
+          const V y4 = yv[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l * y4.x;
+            acc[4 * q + 1] += l * y4.y;
+            acc[4 * q + 2] += l * y4.z;
+            acc[4 * q + 3] += l * y4.w;
+          } else {
+            acc[2 * q + 0] += l * y4.x;
+            acc[2 * q + 1] += l * y4.y;
+          }
         }
       }
     }
@@ -717,7 +730,7 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
     // 32 rows x RG sums, spread over all threads
     for (int e = tid; e < 32 * RG; e += 512) {
       const int r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
-      if (i2 < f.m && q < nr) {
+      if (r2 < nrow && q < nr) {
         ACC sum = ACC(0);
 #pragma unroll
         for (int gg = 0; gg < 16; ++gg) sum += red[(gg * 32 + r2) * (RG + 1) + q];
@@ -753,7 +766,9 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
   const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / BW2) & 1)) * BW2 * MAXR;
-  const int nrow = min(BR, f.m - t.r0);
+  // fully-summed rows [r0, n) only; the contribution rows' share comes from
+  // k_bwd_cb
+  const int nrow = min(BR, f.n - t.r0);
   for (int e = tid; e < BR * BW2; e += 512) {
     const int ii = e % BR, kk = e / BR;
     T* dst = &Lt[ii * (BW2 + 1) + kk];
@@ -803,6 +818,205 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
   }
 }
 
+// Contribution rows of a front, forward: xs(r, :) -= sum over the front's
+// blocks of L(r, blk) y(blk, :) for the 32 rows [r0, r0+32) >= n, all blocks
+// in one CTA.  The next block's L tile and y are fetched (cp.async, register
+// batch) while the current block is multiplied, so the CTA streams L at the
+// rate it can use it.  Thread (row rr, 16-column group g), 512 threads.
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(512) k_fwd_cb(const LTask* __restrict__ tasks,
+                                                LsArgs<T, ACC> a) {
+  constexpr int RG = RGn<ACC>::v;
+  constexpr int NL = BW2 * RG / 512;
+  using V = typename Vec4<ACC>::V;
+  constexpr int VW = Vec4<ACC>::W;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* Lt = reinterpret_cast<T*>(dsm);                            // [2][BW2*32]
+  ACC* yb = reinterpret_cast<ACC*>(dsm + sizeof(T) * 2 * 32 * BW2);  // [2][BW2*RG]
+  ACC* red = yb + 2 * BW2 * RG;                                 // [16][32][RG + 1]
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  const T* L = a.arena + f.off;
+  const int tid = threadIdx.x, rr = tid % 32, g = tid / 32;
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
+  const int nrow = min(32, f.m - t.r0);
+  const int nb = (f.n + BW2 - 1) / BW2;
+  for (int rg = 0; rg < a.nrhs; rg += RG) {
+    const int nr = min(RG, a.nrhs - rg);
+    ACC acc[RG];
+#pragma unroll
+    for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
+    auto issue_l = [&](int b, int buf) {
+      const int c0 = b * BW2, bw = min(BW2, f.n - c0);
+      T* dst = Lt + buf * BW2 * 32;
+      for (int e = tid; e < BW2 * 32; e += 512) {
+        const int r2 = e & 31, k = e >> 5;
+        if (k < bw && r2 < nrow) cp_async(&dst[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
+        else dst[e] = T(0);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    ACC yv[NL];
+    auto load_y = [&](int b) {
+      const int c0 = b * BW2, bw = min(BW2, f.n - c0);
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int e = tid + 512 * u, k = e % BW2, r = e / BW2;
+        yv[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+      }
+    };
+    auto store_y = [&](int buf) {
+#pragma unroll
+      for (int u = 0; u < NL; ++u) {
+        const int e = tid + 512 * u;
+        yb[buf * BW2 * RG + (e % BW2) * RG + e / BW2] = yv[u];
+      }
+    };
+    __syncthreads();
+    issue_l(0, 0);
+    load_y(0);
+    store_y(0);
+    for (int b = 0; b < nb; ++b) {
+      const int buf = b & 1;
+      if (b + 1 < nb) {
+        issue_l(b + 1, buf ^ 1);
+        load_y(b + 1);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+      }
+      __syncthreads();
+      const T* lt = Lt + buf * BW2 * 32;
+      const ACC* ybb = yb + buf * BW2 * RG;
+#pragma unroll 8
+      for (int kk = 0; kk < 16; ++kk) {
+        const int k = g * 16 + kk;
+        const ACC l = (ACC)lt[k * 32 + rr];
+        const V* yp = reinterpret_cast<const V*>(ybb + k * RG);
+#pragma unroll
+        for (int q = 0; q < RG / VW; ++q) {
+          const V y4 = yp[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l * y4.x;
+            acc[4 * q + 1] += l * y4.y;
+            acc[4 * q + 2] += l * y4.z;
+            acc[4 * q + 3] += l * y4.w;
+          } else {
+            acc[2 * q + 0] += l * y4.x;
+            acc[2 * q + 1] += l * y4.y;
+          }
+        }
+      }
+      __syncthreads();  // buffer buf is read; the next issue may overwrite it
+      if (b + 1 < nb) store_y(buf ^ 1);
+    }
+#pragma unroll
+    for (int q = 0; q < RG; ++q) red[(g * 32 + rr) * (RG + 1) + q] = acc[q];
+    __syncthreads();
+    for (int e = tid; e < 32 * RG; e += 512) {
+      const int r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
+      if (r2 < nrow && q < nr) {
+        ACC sum = ACC(0);
+#pragma unroll
+        for (int gg = 0; gg < 16; ++gg) sum += red[(gg * 32 + r2) * (RG + 1) + q];
+        xs[(int64_t)(rg + q) * f.m + i2] -= sum;
+      }
+    }
+  }
+}
+
+// Contribution rows of a front, backward: their share of block c0's
+// reduction, tcb(k, r) += sum_i L(i, c0+k) x(i, r) over the CB_CHUNK rows
+// [r0, r0 + CB_CHUNK) >= n, in 32-row sub-tiles staged with double-buffered
+// cp.async; one set of atomics per CTA.  Thread (column k = tid % 256, row
+// half h = tid / 256), 512 threads.
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(512) k_bwd_cb(const LTask* __restrict__ tasks,
+                                                LsArgs<T, ACC> a) {
+  constexpr int RG = RGn<ACC>::v;
+  constexpr int SR = 32;
+  using V = typename Vec4<ACC>::V;
+  constexpr int VW = Vec4<ACC>::W;
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* Lt = reinterpret_cast<T*>(dsm);  // [2][SR*(BW2+1)]
+  ACC* xt = reinterpret_cast<ACC*>(dsm + sizeof(T) * 2 * SR * (BW2 + 1));  // [2][SR*RG]
+  ACC* half = xt + 2 * SR * RG;       // [BW2][RG + 1]
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  const T* L = a.arena + f.off;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, k = tid % BW2, h = tid / BW2;
+  const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  ACC* tf = a.tcb + (a.inv2_off[t.f] / ((int64_t)BW2 * BW2) + c0 / BW2) * BW2 * MAXR;
+  const int rend = min(t.r0 + CB_CHUNK, f.m);
+  const int nsub = (rend - t.r0 + SR - 1) / SR;
+  for (int rg = 0; rg < a.nrhs; rg += RG) {
+    const int nr = min(RG, a.nrhs - rg);
+    ACC acc[RG];
+#pragma unroll
+    for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
+    auto issue = [&](int sub, int buf) {
+      const int s0 = t.r0 + sub * SR, nrow = min(SR, rend - s0);
+      T* dst = Lt + buf * SR * (BW2 + 1);
+      for (int e = tid; e < SR * BW2; e += 512) {
+        const int ii = e % SR, kk = e / SR;
+        T* d = &dst[ii * (BW2 + 1) + kk];
+        if (ii < nrow && kk < bw) cp_async(d, &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]);
+        else *d = T(0);
+      }
+      ACC* xd = xt + buf * SR * RG;
+      for (int e = tid; e < SR * RG; e += 512) {
+        const int ii = e % SR, r = e / SR;
+        if (ii < nrow && r < nr) cp_async(&xd[ii * RG + r], &xs[(int64_t)(rg + r) * f.m + s0 + ii]);
+        else xd[ii * RG + r] = ACC(0);
+      }
+      asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    __syncthreads();
+    issue(0, 0);
+    for (int sub = 0; sub < nsub; ++sub) {
+      const int buf = sub & 1;
+      if (sub + 1 < nsub) {
+        issue(sub + 1, buf ^ 1);
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+      } else {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+      }
+      __syncthreads();
+      const T* lt = Lt + buf * SR * (BW2 + 1);
+      const ACC* xb = xt + buf * SR * RG;
+#pragma unroll 8
+      for (int i2 = 0; i2 < SR / 2; ++i2) {
+        const int ii = h * (SR / 2) + i2;
+        const ACC l = (ACC)lt[ii * (BW2 + 1) + k];
+        const V* xv = reinterpret_cast<const V*>(&xb[ii * RG]);
+#pragma unroll
+        for (int q = 0; q < RG / VW; ++q) {
+          const V x4 = xv[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l * x4.x;
+            acc[4 * q + 1] += l * x4.y;
+            acc[4 * q + 2] += l * x4.z;
+            acc[4 * q + 3] += l * x4.w;
+          } else {
+            acc[2 * q + 0] += l * x4.x;
+            acc[2 * q + 1] += l * x4.y;
+          }
+        }
+      }
+      __syncthreads();  // buffer buf is read; the next issue may overwrite it
+    }
+    if (h == 1)
+#pragma unroll
+      for (int q = 0; q < RG; ++q) half[k * (RG + 1) + q] = acc[q];
+    __syncthreads();
+    if (h == 0 && k < bw)
+#pragma unroll
+      for (int q = 0; q < RG; ++q)
+        if (q < nr) aadd(&tf[k * MAXR + rg + q], acc[q] + half[k * (RG + 1) + q]);
+  }
+}
+
 inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
 
 // dynamic shared memory of the staged solve-step kernels
@@ -811,6 +1025,12 @@ template <typename T> constexpr size_t diag_mv_smem() {
 }
 template <typename T> constexpr size_t fwd_upd_smem() {
   return sizeof(T) * 32 * BW2 + sizeof(T) * 16 * 32 * (RGn<T>::v + 1);
+}
+template <typename T> constexpr size_t fwd_cb_smem() {
+  return sizeof(T) * 2 * 32 * BW2 + sizeof(T) * (2 * BW2 * RGn<T>::v + 16 * 32 * (RGn<T>::v + 1));
+}
+template <typename T> constexpr size_t bwd_cb_smem() {
+  return sizeof(T) * 2 * 32 * (BW2 + 1) + sizeof(T) * (2 * 32 * RGn<T>::v + BW2 * (RGn<T>::v + 1));
 }
 template <typename T> constexpr size_t bwd_red_smem() {
   return sizeof(T) * BRED_ROWS * (BW2 + 1) + sizeof(T) * BW2 * (RGn<T>::v + 1);
@@ -911,6 +1131,12 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
     case LS_FWD_UPD2:
       k_fwd_upd3<T, ACC><<<ntask, 512, fwd_upd_smem<T>(), s>>>(tasks, a);
       break;
+    case LS_FWD_CB:
+      k_fwd_cb<T, ACC><<<ntask, 512, fwd_cb_smem<T>(), s>>>(tasks, a);
+      break;
+    case LS_BWD_CB:
+      k_bwd_cb<T, ACC><<<ntask, 512, bwd_cb_smem<T>(), s>>>(tasks, a);
+      break;
     case LS_BWD_RED2:
       k_bwd_red3<T, ACC><<<ntask, 512, bwd_red_smem<T>(), s>>>(tasks, a);
       break;
@@ -937,8 +1163,12 @@ void prepare_solve_kernels() {
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
   SG_CUDA(cudaFuncSetAttribute(k_fwd_upd3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)fwd_upd_smem<T>()));
+  SG_CUDA(cudaFuncSetAttribute(k_fwd_cb<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)fwd_cb_smem<T>()));
   SG_CUDA(cudaFuncSetAttribute(k_bwd_red3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)bwd_red_smem<T>()));
+  SG_CUDA(cudaFuncSetAttribute(k_bwd_cb<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)bwd_cb_smem<T>()));
 }
 
 template <typename T>

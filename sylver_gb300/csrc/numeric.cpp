@@ -684,6 +684,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
       int maxb2 = 0;
       for (int f = v.nsmall; f < v.nfront; ++f)
         maxb2 = std::max(maxb2, (hfr[L.f0 + f].n + LB2 - 1) / LB2);
+      // block steps over the fully-summed rows (< n) only
       auto step = [&](std::vector<SOp>& ops, int kind, int b, bool diag) {
         int64_t a = (int64_t)htasks.size();
         for (int f = v.nsmall; f < v.nfront; ++f) {
@@ -693,7 +694,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           int bw = std::min(LB2, d.n - c0), c1 = c0 + bw;
           if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
           else
-            for (int r0 = c1; r0 < d.m;
+            for (int r0 = c1; r0 < d.n;
                  r0 += (kind == LS_FWD_UPD2 ? LSOLVE_UPD_ROWS : LSOLVE_RED_ROWS))
               htasks.push_back({f, c0, bw, r0, 0, 0});
         }
@@ -703,8 +704,28 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
         step(v.fwd, LS_FWD_DIAG2, b, true);
         step(v.fwd, LS_FWD_UPD2, b, false);
       }
+      {
+        // contribution rows: one pass over all blocks of each front
+        int64_t a = (int64_t)htasks.size();
+        for (int f = v.nsmall; f < v.nfront; ++f) {
+          const FrontDesc& d = hfr[L.f0 + f];
+          for (int r0 = d.n; r0 < d.m; r0 += LSOLVE_UPD_ROWS) htasks.push_back({f, 0, 0, r0, 0, 0});
+        }
+        push(v.fwd, LS_FWD_CB, a);
+      }
       rows(v.fwd, LS_SCATTER_FWD);
       rows(v.bwd, LS_GATHER_BWD);
+      {
+        // contribution rows' share of every block, before the block steps
+        int64_t a = (int64_t)htasks.size();
+        for (int f = v.nsmall; f < v.nfront; ++f) {
+          const FrontDesc& d = hfr[L.f0 + f];
+          for (int c0 = 0; c0 < d.n; c0 += LB2)
+            for (int r0 = d.n; r0 < d.m; r0 += LSOLVE_CB_ROWS)
+              htasks.push_back({f, c0, std::min(LB2, d.n - c0), r0, 0, 0});
+        }
+        push(v.bwd, LS_BWD_CB, a);
+      }
       for (int b = maxb2 - 1; b >= 0; --b) {
         step(v.bwd, LS_BWD_RED2, b, false);
         step(v.bwd, LS_BWD_DIAG2, b, true);
@@ -744,6 +765,10 @@ void SolvePlan::ensure_tt(size_t elem, int64_t scratch_elems) {
   // the backward steps leave the accumulators zero; a new buffer starts zero
   if (tt.p != before) SG_CUDA(cudaMemset(tt.p, 0, tt.bytes));
   ys.ensure((size_t)std::max<int64_t>(scratch_elems, 1) * elem);
+  // one 256 x 32 block of contribution-row sums per solve block (the gather
+  // of each backward level clears the blocks it uses)
+  tcb.ensure((size_t)std::max<int64_t>(inv2_elems / (LSOLVE_BW2 * LSOLVE_BW2), 1) * LSOLVE_BW2 *
+             32 * elem);
 }
 
 template <typename T, typename ACC>
@@ -762,7 +787,8 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
     }
     LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),
                      inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), cnt.as<unsigned>(),
-                     inv2.as<T>(), inv2_off.as<int64_t>() + v.f0, inv2t.as<T>()};
+                     inv2.as<T>(), inv2_off.as<int64_t>() + v.f0, inv2t.as<T>(),
+                     tcb.as<ACC>()};
     for (const SOp& op : fwd ? v.fwd : v.bwd) {
       launch_lsolve<T, ACC>(op.kind, tasks.as<LTask>() + op.a, (int)(op.b - op.a), a, s);
       if (prof) mark(2 + op.kind, s);
@@ -782,7 +808,7 @@ void SolvePlan::mark(int kind, cudaStream_t s) {
 }
 
 int FKeep::profile_solve(int nrhs, double* ms, long* nl, cudaStream_t s) {
-  for (int k = 0; k < 10; ++k) {
+  for (int k = 0; k < 12; ++k) {
     ms[k] = 0.0;
     nl[k] = 0;
   }
@@ -818,7 +844,7 @@ int FKeep::profile_solve(int nrhs, double* ms, long* nl, cudaStream_t s) {
     float t = 0.f;
     cudaEventElapsedTime(&t, ev[q - 1].second, ev[q].second);
     const int k = ev[q].first;
-    if (k >= 0 && k < 10) {
+    if (k >= 0 && k < 12) {
       ms[k] += t;
       nl[k] += 1;
     }

@@ -131,7 +131,7 @@ struct SolvePlan {
   std::vector<LTask> hinv2;       // 256-column diagonal blocks (f = level-ordered index)
   std::vector<int64_t> hinv2_off;
   int64_t inv2_elems = 0;
-  DevMem tasks, tt, cnt, ys, inv, invt, inv_off, inv2, inv2t, invt2, inv2_off;
+  DevMem tasks, tt, cnt, ys, inv, invt, inv_off, inv2, inv2t, invt2, inv2_off, tcb;
   int max_large = 0;
   // Invert every diagonal block of the large fronts (after a factorization).
   template <typename T>
