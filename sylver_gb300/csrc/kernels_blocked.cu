@@ -6,8 +6,9 @@
 //               block, held packed in shared memory, in sub-steps of 16
 //               columns: one warp factorises the 16 x 16 diagonal sub-block in
 //               registers and inverts it, all threads solve the rows below it
-//               with that inverse, and the warps update the trailing triangle
-//               of the block in 32 x 32 register tiles;
+//               with that inverse and update the next sub-block column, and
+//               while warp 0 factorises that one the other warps update the
+//               rest of the trailing triangle in 32 x 32 register tiles;
 //   k_blk_panel (one CTA per 64 rows below the panel): those rows solve
 //               L_R L_WW^T = A_R by block forward substitution over the same
 //               16-column sub-blocks (the 16 x 16 inverses come from
@@ -128,22 +129,27 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
   }
   cp_async_wait_all();
   __syncthreads();
-  for (int q0 = 0; q0 < wp; q0 += SB) {
-    // (a) diagonal sub-block by warp 0
-    if (warp == 0) {
-      for (int e = lane; e < SB * SB; e += 32) {
-        const int i = e % SB, k = e / SB;
-        T[k * TLD + i] = (i >= k) ? Lp[pidx(q0 + i, q0 + k)] : 0.f;
-      }
-      __syncwarp();
-      warp_chol16(T, q0, w, Xs, xg + (q0 / SB) * SB * SB, status);
-      __syncwarp();
-      for (int e = lane; e < SB * SB; e += 32) {
-        const int i = e % SB, k = e / SB;
-        if (i >= k) Lp[pidx(q0 + i, q0 + k)] = T[k * TLD + i];
-      }
+  // (a) one warp factorises and inverts the 16 x 16 diagonal sub-block at q
+  auto factor_sub = [&](int q) {
+    for (int e = lane; e < SB * SB; e += 32) {
+      const int i = e % SB, k = e / SB;
+      T[k * TLD + i] = (i >= k) ? Lp[pidx(q + i, q + k)] : 0.f;
     }
-    __syncthreads();
+    __syncwarp();
+    warp_chol16(T, q, w, Xs, xg + (q / SB) * SB * SB, status);
+    __syncwarp();
+    for (int e = lane; e < SB * SB; e += 32) {
+      const int i = e % SB, k = e / SB;
+      if (i >= k) Lp[pidx(q + i, q + k)] = T[k * TLD + i];
+    }
+  };
+  if (warp == 0) factor_sub(0);
+  __syncthreads();
+  // Lookahead: after the rows below sub-block q0 are solved (b), the next
+  // sub-block column is updated first (c1); warp 0 then factorises it while
+  // the other warps update the rest of the trailing triangle (c2), so the
+  // serial pivot chain overlaps the update.
+  for (int q0 = 0; q0 < wp; q0 += SB) {
     const int c1 = q0 + SB;
     if (c1 >= wp) break;
     // (b) rows below: L(r, q0:+16) = A(r, q0:+16) X^T, one thread per row
@@ -160,47 +166,73 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
       }
     }
     __syncthreads();
-    // (c) trailing triangle [c1, wp)^2 -= L(:, q0:+16) L(:, q0:+16)^T in
-    // 32 x 32 tiles, one warp per tile; lane owns rows r0 + (lane&7) + 8u
-    // (u < 4) and columns cc0 + (lane>>3) + 4v (v < 8)
-    const int nt = (wp - c1 + 31) / 32;
-    for (int tile = warp; tile < nt * (nt + 1) / 2; tile += DTHREADS / 32) {
-      int ti = 0;
-      while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
-      const int tj = tile - ti * (ti + 1) / 2;
-      const int r0 = c1 + 32 * ti, cc0 = c1 + 32 * tj;
-      float acc[4][8];
+    // (c1) the next sub-block column: rows [c1, wp) x cols [c1, c1 + 16);
+    // thread (row c1 + tid % 256, eight columns c1 + 8 * (tid / 256) ..)
+    {
+      const int r = c1 + (tid & 255), cbase = c1 + 8 * (tid >> 8);
+      if (r < wp) {
+        float lr[SB];
 #pragma unroll
-      for (int u = 0; u < 4; ++u)
+        for (int k = 0; k < SB; ++k) lr[k] = Lp[pidx(r, q0 + k)];
 #pragma unroll
-        for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
-      const int rl = lane & 7, cl = lane >> 3;
-#pragma unroll 4
-      for (int k = 0; k < SB; ++k) {
-        const float* colk = Lp + pcol(q0 + k) - (q0 + k);
-        float rv[4], cv[8];
+        for (int u = 0; u < 8; ++u) {
+          const int cc = cbase + u;
+          if (cc <= r) {
+            float sacc = 0.f;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int r = r0 + rl + 8 * u;
-          rv[u] = r < wp ? colk[r] : 0.f;
+            for (int k = 0; k < SB; ++k) sacc = fmaf(lr[k], Lp[pidx(cc, q0 + k)], sacc);
+            Lp[pidx(r, cc)] -= sacc;
+          }
         }
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      factor_sub(c1);
+    } else {
+      // (c2) trailing triangle [c2s, wp)^2 -= L(:, q0:+16) L(:, q0:+16)^T in
+      // 32 x 32 tiles, one warp per tile (warps 1..); lane owns rows
+      // r0 + (lane&7) + 8u (u < 4) and columns cc0 + (lane>>3) + 4v (v < 8)
+      const int c2s = c1 + SB;
+      const int nt = (wp - c2s + 31) / 32;
+      for (int tile = warp - 1; tile < nt * (nt + 1) / 2; tile += DTHREADS / 32 - 1) {
+        int ti = 0;
+        while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
+        const int tj = tile - ti * (ti + 1) / 2;
+        const int r0 = c2s + 32 * ti, cc0 = c2s + 32 * tj;
+        float acc[4][8];
 #pragma unroll
-        for (int v = 0; v < 8; ++v) {
-          const int cc = cc0 + cl + 4 * v;
-          cv[v] = cc < wp ? colk[cc] : 0.f;
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+        const int rl = lane & 7, cl = lane >> 3;
+#pragma unroll 4
+        for (int k = 0; k < SB; ++k) {
+          const float* colk = Lp + pcol(q0 + k) - (q0 + k);
+          float rv[4], cv[8];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int r = r0 + rl + 8 * u;
+            rv[u] = r < wp ? colk[r] : 0.f;
+          }
+#pragma unroll
+          for (int v = 0; v < 8; ++v) {
+            const int cc = cc0 + cl + 4 * v;
+            cv[v] = cc < wp ? colk[cc] : 0.f;
+          }
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(rv[u], cv[v], acc[u][v]);
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
-          for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(rv[u], cv[v], acc[u][v]);
+          for (int v = 0; v < 8; ++v) {
+            const int r = r0 + rl + 8 * u, cc = cc0 + cl + 4 * v;
+            if (r < wp && cc <= r) Lp[pidx(r, cc)] -= acc[u][v];
+          }
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int v = 0; v < 8; ++v) {
-          const int r = r0 + rl + 8 * u, cc = cc0 + cl + 4 * v;
-          if (r < wp && cc <= r) Lp[pidx(r, cc)] -= acc[u][v];
-        }
     }
     __syncthreads();
   }
