@@ -65,6 +65,13 @@ struct FrontDesc {
   int pad;
 };
 
+// Zeroing before assembly: columns [j0, j1) of a front, rows j .. m - 1 of
+// column j (the lower triangle; nothing reads the upper one).
+struct ZeroTask {
+  int64_t off;
+  int ld, m, j0, j1;
+};
+
 // Whole small front factorized by one CTA in shared memory.
 struct SmallTask {
   int64_t off;
@@ -143,6 +150,8 @@ struct EaItem {
 template <typename T>
 void prepare_factor_kernels();
 template <typename T>
+void launch_zero_lower(T* arena, const ZeroTask* t, int ntask, cudaStream_t s);
+template <typename T>
 void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
                    int64_t count, bool atomic, cudaStream_t s);
 template <typename T>
@@ -198,7 +207,6 @@ struct LTask {
 enum LsKind {
   LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD,
   LS_FWD_DIAG2, LS_FWD_UPD2, LS_BWD_RED2, LS_BWD_DIAG2,
-  LS_FWD_CB,   // contribution rows of a front, once after all its blocks (forward)
   LS_BWD_CB    // contribution rows' share of every block, once before the steps (backward)
 };
 constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
@@ -206,10 +214,9 @@ constexpr int LSOLVE_BW2 = 256;  // columns per solve step
 constexpr int LSOLVE_UPD_ROWS = 32;  // rows per forward-update CTA
 constexpr int LSOLVE_RED_ROWS = 64;  // rows per backward-reduction CTA
 constexpr int LSOLVE_CB_ROWS = 256;  // contribution rows per backward CB CTA
-// Large fronts are swept block by block over their fully-summed rows only;
-// the contribution rows (>= n) are updated once per front after the forward
-// blocks (LS_FWD_CB) and contribute to every backward block once, before the
-// backward blocks (LS_BWD_CB).
+// Large fronts are swept block by block; the backward steps reduce over the
+// fully-summed rows only, because the contribution rows (>= n) contribute to
+// every backward block once, before the backward blocks (LS_BWD_CB).
 // Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
 // explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
 // index), tt: two 256 x 32 accumulators per front (backward steps alternate

@@ -19,6 +19,19 @@ namespace {
 template <typename T> __device__ __forceinline__ void atomic_add(T* p, T v) { atomicAdd(p, v); }
 
 // ---------------------------------------------------------------------------
+// Lower triangles of the fronts set to zero before assembly, one CTA per task
+// (a range of columns); warps take columns, lanes run down the rows.
+template <typename T>
+__global__ void __launch_bounds__(256) k_zero_lower(T* __restrict__ arena,
+                                                    const ZeroTask* __restrict__ tasks) {
+  const ZeroTask t = tasks[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int j = t.j0 + warp; j < t.j1; j += 8) {
+    T* col = arena + t.off + (int64_t)j * t.ld;
+    for (int i = j + lane; i < t.m; i += 32) col[i] = T(0);
+  }
+}
+
 // arena[dst[k]] (+)= val[src[k]]  -- assembly of original entries.
 template <typename T>
 __global__ void k_init_a(T* __restrict__ arena, const double* __restrict__ val,
@@ -288,6 +301,12 @@ __global__ void __launch_bounds__(256) k_update(T* __restrict__ arena,
 // ---------------------------------------------------------------------------
 
 template <typename T>
+void launch_zero_lower(T* arena, const ZeroTask* t, int ntask, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_zero_lower<T><<<ntask, 256, 0, s>>>(arena, t);
+}
+
+template <typename T>
 void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
                    int64_t count, bool atomic, cudaStream_t s) {
   if (count <= 0) return;
@@ -351,6 +370,7 @@ void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStr
 
 #define SG_INST(T)                                                                          \
   template void prepare_factor_kernels<T>();                                                 \
+  template void launch_zero_lower<T>(T*, const ZeroTask*, int, cudaStream_t);                \
   template void launch_init_a<T>(T*, const double*, const int64_t*, const int64_t*, int64_t, \
                                  bool, cudaStream_t);                                       \
   template void launch_extend_add<T>(T*, const ChildDesc*, const EaItem*, const int*, int,   \

@@ -255,26 +255,39 @@ __global__ void k_permute_out(const ACC* __restrict__ xp, const int* __restrict_
   *d = add ? *d + v : v;
 }
 
-__global__ void k_residual(const int64_t* __restrict__ rowptr, const int* __restrict__ col,
-                           const double* __restrict__ a, int n, const double* __restrict__ x,
-                           int ldx, const double* __restrict__ b, int ldb,
-                           double* __restrict__ res, int nrhs) {
+__global__ void __launch_bounds__(128) k_residual(const int64_t* __restrict__ rowptr,
+                                                  const int* __restrict__ col,
+                                                  const double* __restrict__ a, int n,
+                                                  const double* __restrict__ x, int ldx,
+                                                  const double* __restrict__ b, int ldb,
+                                                  double* __restrict__ res, int nrhs) {
+  // one row per thread, up to 16 right-hand sides per pass; the row's
+  // entries are taken four at a time so that 64 loads of x are in flight
+  constexpr int RR = 16;
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int64_t p0 = rowptr[i], p1 = rowptr[i + 1];
-  for (int r0 = 0; r0 < nrhs; r0 += RC) {
-    double acc[RC];
+  for (int r0 = 0; r0 < nrhs; r0 += RR) {
+    double acc[RR];
 #pragma unroll
-    for (int q = 0; q < RC; ++q) acc[q] = 0.0;
-    for (int64_t p = p0; p < p1; ++p) {
-      double v = a[p];
-      int j = col[p];
+    for (int q = 0; q < RR; ++q) acc[q] = 0.0;
+    for (int64_t p = p0; p < p1; p += 4) {
+      double v[4];
+      int j[4];
 #pragma unroll
-      for (int q = 0; q < RC; ++q)
-        if (r0 + q < nrhs) acc[q] = fma(v, x[(int64_t)(r0 + q) * ldx + j], acc[q]);
+      for (int u = 0; u < 4; ++u) {
+        const bool ok = p + u < p1;
+        v[u] = ok ? a[p + u] : 0.0;
+        j[u] = ok ? col[p + u] : col[p0];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int q = 0; q < RR; ++q)
+          if (r0 + q < nrhs) acc[q] = fma(v[u], x[(int64_t)(r0 + q) * ldx + j[u]], acc[q]);
     }
 #pragma unroll
-    for (int q = 0; q < RC; ++q)
+    for (int q = 0; q < RR; ++q)
       if (r0 + q < nrhs)
         res[(int64_t)(r0 + q) * n + i] = b[(int64_t)(r0 + q) * ldb + i] - acc[q];
   }
@@ -285,9 +298,15 @@ __device__ __forceinline__ void atomic_max_nonneg(double* p, double v) {
   atomicMax(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__double_as_longlong(v));
 }
 
-__global__ void k_maxnorms(const double* __restrict__ res, const double* __restrict__ x,
-                           int ldx, const double* __restrict__ b, int ldb, int n, int nrhs,
-                           double* norms) {
+__global__ void __launch_bounds__(256) k_maxnorms(const double* __restrict__ res,
+                                                  const double* __restrict__ x, int ldx,
+                                                  const double* __restrict__ b, int ldb, int n,
+                                                  int nrhs, double* norms) {
+  // per right-hand side r = blockIdx.y: max |res|, |x|, |b| over a grid-stride
+  // range, reduced in the block before one atomic per value (a few hundred
+  // blocks per right-hand side; per-warp atomics on the same three words were
+  // the bottleneck)
+  __shared__ double red[3][8];
   const int r = blockIdx.y;
   double mr = 0.0, mx = 0.0, mb = 0.0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -300,10 +319,17 @@ __global__ void k_maxnorms(const double* __restrict__ res, const double* __restr
     mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     mb = fmax(mb, __shfl_xor_sync(0xffffffffu, mb, o));
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomic_max_nonneg(&norms[3 * r + 0], mr);
-    atomic_max_nonneg(&norms[3 * r + 1], mx);
-    atomic_max_nonneg(&norms[3 * r + 2], mb);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    red[0][warp] = mr;
+    red[1][warp] = mx;
+    red[2][warp] = mb;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, red[threadIdx.x][w]);
+    atomic_max_nonneg(&norms[3 * r + threadIdx.x], m);
   }
 }
 
@@ -651,8 +677,8 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
     for (int e = tid; e < DR * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
 }
 
-// rows [r0, r0+32) < n: xs_i -= L_i,blk y_blk; thread (row, 16-column
-// group g), 512 threads.  The 32 x 256 tile of L is staged in shared memory by one wave
+// rows [r0, r0+32) below the block: xs_i -= L_i,blk y_blk; thread (row,
+// 16-column group g), 512 threads.  The 32 x 256 tile of L is staged in shared memory by one wave
 // of asynchronous copies; y is read as 16-byte vectors (one broadcast per
 // warp).
 template <typename T, typename ACC>
@@ -671,9 +697,7 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
   const int tid = threadIdx.x, rr = tid % 32, g = tid / 32;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  // rows [r0, r0+32) below the block, fully summed (< n); the contribution
-  // rows are updated once per front by k_fwd_cb
-  const int nrow = min(32, f.n - t.r0);
+  const int nrow = min(32, f.m - t.r0);
   const int cfirst = t.c0, clast = t.c0 + t.bw;
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
@@ -818,114 +842,6 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
   }
 }
 
-// Contribution rows of a front, forward: xs(r, :) -= sum over the front's
-// blocks of L(r, blk) y(blk, :) for the 32 rows [r0, r0+32) >= n, all blocks
-// in one CTA.  The next block's L tile and y are fetched (cp.async, register
-// batch) while the current block is multiplied, so the CTA streams L at the
-// rate it can use it.  Thread (row rr, 16-column group g), 512 threads.
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(512) k_fwd_cb(const LTask* __restrict__ tasks,
-                                                LsArgs<T, ACC> a) {
-  constexpr int RG = RGn<ACC>::v;
-  constexpr int NL = BW2 * RG / 512;
-  using V = typename Vec4<ACC>::V;
-  constexpr int VW = Vec4<ACC>::W;
-  extern __shared__ __align__(16) unsigned char dsm[];
-  T* Lt = reinterpret_cast<T*>(dsm);                            // [2][BW2*32]
-  ACC* yb = reinterpret_cast<ACC*>(dsm + sizeof(T) * 2 * 32 * BW2);  // [2][BW2*RG]
-  ACC* red = yb + 2 * BW2 * RG;                                 // [16][32][RG + 1]
-  const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = a.fr[t.f];
-  const T* L = a.arena + f.off;
-  const int tid = threadIdx.x, rr = tid % 32, g = tid / 32;
-  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
-  const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  const int nrow = min(32, f.m - t.r0);
-  const int nb = (f.n + BW2 - 1) / BW2;
-  for (int rg = 0; rg < a.nrhs; rg += RG) {
-    const int nr = min(RG, a.nrhs - rg);
-    ACC acc[RG];
-#pragma unroll
-    for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    auto issue_l = [&](int b, int buf) {
-      const int c0 = b * BW2, bw = min(BW2, f.n - c0);
-      T* dst = Lt + buf * BW2 * 32;
-      for (int e = tid; e < BW2 * 32; e += 512) {
-        const int r2 = e & 31, k = e >> 5;
-        if (k < bw && r2 < nrow) cp_async(&dst[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
-        else dst[e] = T(0);
-      }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    ACC yv[NL];
-    auto load_y = [&](int b) {
-      const int c0 = b * BW2, bw = min(BW2, f.n - c0);
-#pragma unroll
-      for (int u = 0; u < NL; ++u) {
-        const int e = tid + 512 * u, k = e % BW2, r = e / BW2;
-        yv[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
-      }
-    };
-    auto store_y = [&](int buf) {
-#pragma unroll
-      for (int u = 0; u < NL; ++u) {
-        const int e = tid + 512 * u;
-        yb[buf * BW2 * RG + (e % BW2) * RG + e / BW2] = yv[u];
-      }
-    };
-    __syncthreads();
-    issue_l(0, 0);
-    load_y(0);
-    store_y(0);
-    for (int b = 0; b < nb; ++b) {
-      const int buf = b & 1;
-      if (b + 1 < nb) {
-        issue_l(b + 1, buf ^ 1);
-        load_y(b + 1);
-        asm volatile("cp.async.wait_group 1;" ::: "memory");
-      } else {
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
-      }
-      __syncthreads();
-      const T* lt = Lt + buf * BW2 * 32;
-      const ACC* ybb = yb + buf * BW2 * RG;
-#pragma unroll 8
-      for (int kk = 0; kk < 16; ++kk) {
-        const int k = g * 16 + kk;
-        const ACC l = (ACC)lt[k * 32 + rr];
-        const V* yp = reinterpret_cast<const V*>(ybb + k * RG);
-#pragma unroll
-        for (int q = 0; q < RG / VW; ++q) {
-          const V y4 = yp[q];
-          if constexpr (VW == 4) {
-            acc[4 * q + 0] += l * y4.x;
-            acc[4 * q + 1] += l * y4.y;
-            acc[4 * q + 2] += l * y4.z;
-            acc[4 * q + 3] += l * y4.w;
-          } else {
-            acc[2 * q + 0] += l * y4.x;
-            acc[2 * q + 1] += l * y4.y;
-          }
-        }
-      }
-      __syncthreads();  // buffer buf is read; the next issue may overwrite it
-      if (b + 1 < nb) store_y(buf ^ 1);
-    }
-#pragma unroll
-    for (int q = 0; q < RG; ++q) red[(g * 32 + rr) * (RG + 1) + q] = acc[q];
-    __syncthreads();
-    for (int e = tid; e < 32 * RG; e += 512) {
-      const int r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
-      if (r2 < nrow && q < nr) {
-        ACC sum = ACC(0);
-#pragma unroll
-        for (int gg = 0; gg < 16; ++gg) sum += red[(gg * 32 + r2) * (RG + 1) + q];
-        xs[(int64_t)(rg + q) * f.m + i2] -= sum;
-      }
-    }
-  }
-}
-
 // Contribution rows of a front, backward: their share of block c0's
 // reduction, tcb(k, r) += sum_i L(i, c0+k) x(i, r) over the CB_CHUNK rows
 // [r0, r0 + CB_CHUNK) >= n, in 32-row sub-tiles staged with double-buffered
@@ -1026,9 +942,6 @@ template <typename T> constexpr size_t diag_mv_smem() {
 template <typename T> constexpr size_t fwd_upd_smem() {
   return sizeof(T) * 32 * BW2 + sizeof(T) * 16 * 32 * (RGn<T>::v + 1);
 }
-template <typename T> constexpr size_t fwd_cb_smem() {
-  return sizeof(T) * 2 * 32 * BW2 + sizeof(T) * (2 * BW2 * RGn<T>::v + 16 * 32 * (RGn<T>::v + 1));
-}
 template <typename T> constexpr size_t bwd_cb_smem() {
   return sizeof(T) * 2 * 32 * (BW2 + 1) + sizeof(T) * (2 * 32 * RGn<T>::v + BW2 * (RGn<T>::v + 1));
 }
@@ -1084,7 +997,7 @@ void launch_residual(const int64_t* rowptr, const int* col, const double* aval, 
 void launch_maxnorms(const double* res, const double* x, int ldx, const double* b, int ldb,
                      int n, int nrhs, double* norms, cudaStream_t s) {
   if (n == 0) return;
-  dim3 grid(std::min(nblocks(n, 256), 152 * 4), nrhs);
+  dim3 grid(std::min(nblocks(n, 256), 152), nrhs);
   k_maxnorms<<<grid, 256, 0, s>>>(res, x, ldx, b, ldb, n, nrhs, norms);
 }
 
@@ -1131,9 +1044,6 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
     case LS_FWD_UPD2:
       k_fwd_upd3<T, ACC><<<ntask, 512, fwd_upd_smem<T>(), s>>>(tasks, a);
       break;
-    case LS_FWD_CB:
-      k_fwd_cb<T, ACC><<<ntask, 512, fwd_cb_smem<T>(), s>>>(tasks, a);
-      break;
     case LS_BWD_CB:
       k_bwd_cb<T, ACC><<<ntask, 512, bwd_cb_smem<T>(), s>>>(tasks, a);
       break;
@@ -1163,8 +1073,6 @@ void prepare_solve_kernels() {
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
   SG_CUDA(cudaFuncSetAttribute(k_fwd_upd3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)fwd_upd_smem<T>()));
-  SG_CUDA(cudaFuncSetAttribute(k_fwd_cb<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)fwd_cb_smem<T>()));
   SG_CUDA(cudaFuncSetAttribute(k_bwd_red3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)bwd_red_smem<T>()));
   SG_CUDA(cudaFuncSetAttribute(k_bwd_cb<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -157,6 +157,21 @@ void FKeep::plan_cholesky() {
     cur += round_up64((int64_t)ld[s] * m, 64);
   }
   arena_elems = std::max<int64_t>(cur, 1);
+  // zeroing tasks: each front's lower triangle in column ranges of about 64K
+  // entries
+  std::vector<ZeroTask> zt;
+  for (int k = 0; k < ns; ++k) {
+    const int s = order[k], m = st.nrow[s];
+    int j0 = 0;
+    while (j0 < m) {
+      int64_t acc = 0;
+      int j1 = j0;
+      while (j1 < m && acc < 65536) acc += m - j1++;
+      zt.push_back({off[s], ld[s], m, j0, j1});
+      j0 = j1;
+    }
+  }
+  nzero = (int)zt.size();
 
   // A -> arena map
   std::vector<int64_t> asrc, adst;
@@ -406,6 +421,7 @@ void FKeep::plan_cholesky() {
     op_flops[q] = f;
   }
   cudaStream_t s = Runtime::get().stream;
+  zerot.upload(zt, s);
   amap_src.upload(asrc, s);
   amap_dst.upload(adst, s);
   cdesc.upload(cds, s);
@@ -475,7 +491,7 @@ void FKeep::run_ops(cudaStream_t s) {
     int64_t cnt = op.b - op.a;
     switch (op.kind) {
       case Op::MEMSET:
-        SG_CUDA(cudaMemsetAsync(A, 0, (size_t)arena_elems * sizeof(T), s));
+        launch_zero_lower<T>(A, zerot.as<ZeroTask>(), nzero, s);
         break;
       case Op::INIT:
         launch_init_a<T>(A, val.as<double>(), amap_src.as<int64_t>(), amap_dst.as<int64_t>(),
@@ -563,7 +579,7 @@ int FKeep::factorize(const double* val_dev, cudaStream_t s) {
     else run_ops<double>(s);
   }
   SG_CUDA(cudaEventRecord(e1, s));
-  launches = (long)ops.size() - 1;  // the memset is not a kernel
+  launches = (long)ops.size();
   unsigned st = 0, tce = 0;
   SG_CUDA(cudaMemcpyAsync(&st, status.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   SG_CUDA(cudaMemcpyAsync(&tce, tcerr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
@@ -684,7 +700,8 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
       int maxb2 = 0;
       for (int f = v.nsmall; f < v.nfront; ++f)
         maxb2 = std::max(maxb2, (hfr[L.f0 + f].n + LB2 - 1) / LB2);
-      // block steps over the fully-summed rows (< n) only
+      // block steps: forward, over all rows below the block; backward, over
+      // the fully-summed rows (< n) only
       auto step = [&](std::vector<SOp>& ops, int kind, int b, bool diag) {
         int64_t a = (int64_t)htasks.size();
         for (int f = v.nsmall; f < v.nfront; ++f) {
@@ -693,25 +710,16 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           if (c0 >= d.n) continue;
           int bw = std::min(LB2, d.n - c0), c1 = c0 + bw;
           if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
+          else if (kind == LS_FWD_UPD2)
+            for (int r0 = c1; r0 < d.m; r0 += LSOLVE_UPD_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
           else
-            for (int r0 = c1; r0 < d.n;
-                 r0 += (kind == LS_FWD_UPD2 ? LSOLVE_UPD_ROWS : LSOLVE_RED_ROWS))
-              htasks.push_back({f, c0, bw, r0, 0, 0});
+            for (int r0 = c1; r0 < d.n; r0 += LSOLVE_RED_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
         }
         push(ops, kind, a);
       };
       for (int b = 0; b < maxb2; ++b) {
         step(v.fwd, LS_FWD_DIAG2, b, true);
         step(v.fwd, LS_FWD_UPD2, b, false);
-      }
-      {
-        // contribution rows: one pass over all blocks of each front
-        int64_t a = (int64_t)htasks.size();
-        for (int f = v.nsmall; f < v.nfront; ++f) {
-          const FrontDesc& d = hfr[L.f0 + f];
-          for (int r0 = d.n; r0 < d.m; r0 += LSOLVE_UPD_ROWS) htasks.push_back({f, 0, 0, r0, 0, 0});
-        }
-        push(v.fwd, LS_FWD_CB, a);
       }
       rows(v.fwd, LS_SCATTER_FWD);
       rows(v.bwd, LS_GATHER_BWD);

@@ -199,7 +199,8 @@ struct FKeep {
 
   // device data
   DevMem arena, val, cval, faval, frow, fcol, fidx, srcptr, src, status, anorm;
-  DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, small, panel, upd, diagt;
+  DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, small, panel, upd, diagt, zerot;
+  int nzero = 0;
   DevMem dfr, dscr, rlist0, perm0;
   DevMem xp, scratch, bcopy, resid, norms;
   cudaGraphExec_t graph = nullptr;
