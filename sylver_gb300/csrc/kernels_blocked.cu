@@ -252,8 +252,8 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ a
                                                            int64_t pstride, int pitch) {
   extern __shared__ __align__(16) float sm[];
   float* Ar = sm;                // Ar[k*ALD + r] = A(r0 + r, k0 + k), then L
-  float* Lrow = Ar + PW * ALD;   // Lrow[jj*(PW+1) + k] = L(k0 + q0 + jj, k0 + k), k < q0
-  float* Xs = Lrow + SB * (PW + 1);  // X of the sub-block, Xs[j*16 + i] = X(i, j)
+  float* Lrow = Ar + PW * ALD;   // Lrow[k*16 + jj] = L(k0 + q0 + jj, k0 + k), k < q0
+  float* Xs = Lrow + PW * SB;    // X of the sub-block, Xs[j*16 + i] = X(i, j)
   const BlkTask t = tasks[blockIdx.x];
   float* a = arena + t.off;
   const int64_t ld = t.ld;
@@ -271,33 +271,42 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ a
     // block row q0/16 of L (left of the sub-block) and the sub-block inverse
     for (int e = tid; e < SB * q0; e += PTHREADS) {
       const int jj = e % SB, k = e / SB;
-      if (q0 + jj < w) cp_async(&Lrow[jj * (PW + 1) + k], &a[(int64_t)(k0 + k) * ld + k0 + q0 + jj]);
-      else Lrow[jj * (PW + 1) + k] = 0.f;
+      if (q0 + jj < w) cp_async(&Lrow[e], &a[(int64_t)(k0 + k) * ld + k0 + q0 + jj]);
+      else Lrow[e] = 0.f;
     }
     for (int e = tid; e < SB * SB; e += PTHREADS) cp_async(&Xs[e], &xg[(q0 / SB) * SB * SB + e]);
     cp_async_wait_all();
     __syncthreads();
+    // correction by the earlier sub-blocks: one shared load of A and one
+    // 16-byte load of the block row per four fused multiply-adds
     float v[4];
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) v[jj] = Ar[(q0 + j0 + jj) * ALD + r];
 #pragma unroll 4
     for (int k = 0; k < q0; ++k) {
       const float ar = Ar[k * ALD + r];
-#pragma unroll
-      for (int jj = 0; jj < 4; ++jj) v[jj] = fmaf(-ar, Lrow[(j0 + jj) * (PW + 1) + k], v[jj]);
+      const float4 l4 = *reinterpret_cast<const float4*>(&Lrow[k * SB + j0]);
+      v[0] = fmaf(-ar, l4.x, v[0]);
+      v[1] = fmaf(-ar, l4.y, v[1]);
+      v[2] = fmaf(-ar, l4.z, v[2]);
+      v[3] = fmaf(-ar, l4.w, v[3]);
     }
     __syncthreads();
 #pragma unroll
     for (int jj = 0; jj < 4; ++jj) Ar[(q0 + j0 + jj) * ALD + r] = v[jj];
     __syncthreads();
+    // L(r, q0 + j) = sum_k A'(r, q0 + k) X(j, k) (X lower triangular, zeros
+    // stored above the diagonal)
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-      const int j = j0 + jj;
-      float o = 0.f;
+    for (int jj = 0; jj < 4; ++jj) v[jj] = 0.f;
 #pragma unroll
-      for (int k = 0; k < SB; ++k)
-        if (k <= j) o = fmaf(Ar[(q0 + k) * ALD + r], Xs[k * SB + j], o);
-      v[jj] = o;
+    for (int k = 0; k < SB; ++k) {
+      const float ak = Ar[(q0 + k) * ALD + r];
+      const float4 x4 = *reinterpret_cast<const float4*>(&Xs[k * SB + j0]);
+      v[0] = fmaf(ak, x4.x, v[0]);
+      v[1] = fmaf(ak, x4.y, v[1]);
+      v[2] = fmaf(ak, x4.z, v[2]);
+      v[3] = fmaf(ak, x4.w, v[3]);
     }
     __syncthreads();
 #pragma unroll
@@ -327,7 +336,7 @@ constexpr size_t diag_smem() {
   return sizeof(float) * ((size_t)PW * (PW + 1) / 2 + SB * SB + SB * TLD);
 }
 constexpr size_t panel_smem() {
-  return sizeof(float) * ((size_t)PW * ALD + SB * (PW + 1) + SB * SB);
+  return sizeof(float) * ((size_t)PW * ALD + PW * SB + SB * SB);
 }
 
 }  // namespace
