@@ -36,57 +36,79 @@ constexpr int PW = BLK_W;         // widest panel (256)
 constexpr int SB = 16;            // sub-block width
 constexpr int NSBMAX = PW / SB;   // sub-blocks of the widest panel
 constexpr int XSZ = NSBMAX * SB * SB;  // floats of the sub-block inverses of one panel
-constexpr int TLD = SB + 1;
 constexpr int DTHREADS = 512;
-constexpr int PTHREADS = 256;
-constexpr int ALD = 64 + 1;       // rows of one panel-kernel CTA (+1)
+constexpr int PROWS = 64;         // rows of one panel-kernel CTA
+constexpr int PTHREADS = 2 * PROWS;
+constexpr int ALD = PROWS + 1;
 
 // start of column j of a packed lower triangle with PW rows
 __device__ __forceinline__ int pcol(int j) { return j * PW - (j * (j - 1)) / 2; }
 // (i, j), i >= j, of the packed lower triangle
 __device__ __forceinline__ int pidx(int i, int j) { return pcol(j) + i - j; }
 
-// One warp: Cholesky of the 16 x 16 tile T (T[j*TLD + i] = A(i, j), lower)
-// in registers, lane i < 16 holding row i; writes L back to T and X = L^-1
-// to xs (xs[i*SB + j] = X(i, j)) and xg (global, xg[j*SB + i] = X(i, j)).
-// A non-positive pivot is replaced by one and reported when its column is
-// below bwreal.
-__device__ __noinline__ void warp_chol16(float* __restrict__ T, int q0, int bwreal,
+// One warp: Cholesky of the 16 x 16 diagonal sub-block at (q, q) of the
+// packed triangle Lp, in registers (lane i < 16 holds row i; lanes 16..31
+// repeat lanes 0..15).  With bk != nullptr the sub-block is first updated
+// by the 16 columns left of it: A(q+i, q+k) -= sum_m L(q+i, m) L(q+k, m),
+// bk[m*16 + i] = L(q + i, q - 16 + m).  Writes L back to Lp and X = L^-1 to
+// xs and xg (both xs[k*16 + i] = X(i, k)).  A non-positive pivot is replaced
+// by one and reported when its column is below bwreal.
+__device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwreal,
+                                         const float* __restrict__ bk,
                                          float* __restrict__ xs, float* __restrict__ xg,
                                          unsigned* __restrict__ status) {
   const int lane = threadIdx.x & 31;
   const int li = lane & (SB - 1);
   float a[SB], rinv[SB];
 #pragma unroll
-  for (int k = 0; k < SB; ++k) a[k] = (k <= li) ? T[k * TLD + li] : 0.f;
+  for (int k = 0; k < SB; ++k) a[k] = (k <= li) ? Lp[pidx(q + li, q + k)] : 0.f;
+  if (bk != nullptr) {
+#pragma unroll 4
+    for (int m = 0; m < SB; ++m) {
+      const float own = bk[m * SB + li];
+#pragma unroll
+      for (int k4 = 0; k4 < SB; k4 += 4) {
+        const float4 b4 = *reinterpret_cast<const float4*>(&bk[m * SB + k4]);
+        a[k4] = fmaf(-own, b4.x, a[k4]);
+        a[k4 + 1] = fmaf(-own, b4.y, a[k4 + 1]);
+        a[k4 + 2] = fmaf(-own, b4.z, a[k4 + 2]);
+        a[k4 + 3] = fmaf(-own, b4.w, a[k4 + 3]);
+      }
+    }
+  }
   bool bad = false;
   // The pivot chain is the critical path of the panel: 1/sqrt(d) comes from
   // the hardware estimate refined by one Newton step (about 1 ulp), and
   // both the column scaling and the inverse multiply by it -- IEEE sqrt and
-  // division cost three times as long per 16 columns.
+  // division cost three times as long per 16 columns.  Lane k + 1 forms the
+  // next pivot from its own l(k+1, k), so only one shuffle per column sits
+  // on the chain.
+  float dn = __shfl_sync(0xffffffffu, a[0], 0);
 #pragma unroll
   for (int k = 0; k < SB; ++k) {
-    float d = __shfl_sync(0xffffffffu, a[k], k);
+    float d = dn;
     if (!(d > 0.f)) {
-      if (q0 + k < bwreal) bad = true;
+      if (q + k < bwreal) bad = true;
       d = 1.f;
     }
     float r = rsqrtf(d);
     r = r * fmaf(-0.5f * d * r, r, 1.5f);
     rinv[k] = r;
-    if (li == k) a[k] = d * r;
-    else if (li > k) a[k] = a[k] * r;
+    const float lik = (li == k) ? d * r : a[k] * r;
+    a[k] = lik;
+    if (k + 1 < SB) dn = __shfl_sync(0xffffffffu, fmaf(-lik, lik, a[k + 1]), k + 1);
 #pragma unroll
     for (int j = k + 1; j < SB; ++j) {
-      const float ljk = __shfl_sync(0xffffffffu, a[k], j);
-      if (li >= j) a[j] = fmaf(-a[k], ljk, a[j]);
+      const float ljk = __shfl_sync(0xffffffffu, lik, j);
+      if (li >= j) a[j] = fmaf(-lik, ljk, a[j]);
     }
   }
   if (lane < SB) {
 #pragma unroll
     for (int k = 0; k < SB; ++k)
-      if (k <= li) T[k * TLD + li] = a[k];
+      if (k <= li) Lp[pidx(q + li, q + k)] = a[k];
   }
+  __syncwarp();
   if (lane == 0 && bad) atomicOr(status, ST_NOT_POSDEF);
   // column li of X: X(i, li) = (delta - sum_{k<i} L(i,k) X(k, li)) / L(i, i)
   float x[SB];
@@ -94,14 +116,15 @@ __device__ __noinline__ void warp_chol16(float* __restrict__ T, int q0, int bwre
   for (int i = 0; i < SB; ++i) {
     float v = (i == li) ? 1.f : 0.f;
 #pragma unroll
-    for (int k = 0; k < i; ++k) v = fmaf(-__shfl_sync(0xffffffffu, a[k], i), x[k], v);
+    for (int k = 0; k < i; ++k) v = fmaf(-Lp[pidx(q + i, q + k)], x[k], v);
     x[i] = v * rinv[i];
   }
   if (lane < SB) {
 #pragma unroll
-    for (int i = 0; i < SB; ++i) {
-      xs[i * SB + li] = x[i];
-      xg[li * SB + i] = x[i];
+    for (int i = 0; i < SB; i += 4) {
+      const float4 x4 = make_float4(x[i], x[i + 1], x[i + 2], x[i + 3]);
+      *reinterpret_cast<float4*>(&xs[li * SB + i]) = x4;
+      *reinterpret_cast<float4*>(&xg[li * SB + i]) = x4;
     }
   }
 }
@@ -111,9 +134,9 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
                                                        float* __restrict__ xinv,
                                                        unsigned* __restrict__ status) {
   extern __shared__ __align__(16) float sm[];
-  float* Lp = sm;                      // packed lower triangle, PW rows
-  float* Xs = Lp + PW * (PW + 1) / 2;  // inverse of the current sub-block
-  float* T = Xs + SB * SB;             // 16 x 16 sub-block for the warp
+  float* Xs = sm;                      // inverse of the current sub-block, Xs[k*16 + j] = X(j, k)
+  float* Bk = Xs + SB * SB;            // Bk[m*16 + i] = L(c1 + i, q0 + m), the next sub-block's rows
+  float* Lp = Bk + SB * SB;            // packed lower triangle, PW rows
   const BlkTask t = tasks[blockIdx.x];
   float* a = arena + t.off;
   const int64_t ld = t.ld;
@@ -129,71 +152,69 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
   }
   cp_async_wait_all();
   __syncthreads();
-  // (a) one warp factorises and inverts the 16 x 16 diagonal sub-block at q
-  auto factor_sub = [&](int q) {
-    for (int e = lane; e < SB * SB; e += 32) {
-      const int i = e % SB, k = e / SB;
-      T[k * TLD + i] = (i >= k) ? Lp[pidx(q + i, q + k)] : 0.f;
-    }
-    __syncwarp();
-    warp_chol16(T, q, w, Xs, xg + (q / SB) * SB * SB, status);
-    __syncwarp();
-    for (int e = lane; e < SB * SB; e += 32) {
-      const int i = e % SB, k = e / SB;
-      if (i >= k) Lp[pidx(q + i, q + k)] = T[k * TLD + i];
-    }
-  };
-  if (warp == 0) factor_sub(0);
+  if (warp == 0) warp_chol16(Lp, 0, w, nullptr, Xs, xg, status);
   __syncthreads();
-  // Lookahead: after the rows below sub-block q0 are solved (b), the next
-  // sub-block column is updated first (c1); warp 0 then factorises it while
-  // the other warps update the rest of the trailing triangle (c2), so the
-  // serial pivot chain overlaps the update.
+  // Per 16-column sub-block q0: (b) all threads solve the rows below it with
+  // its inverse; then warp 0 updates the next diagonal sub-block by it and
+  // factorises that (the serial pivot chain) while the other warps update
+  // the next sub-block column below its diagonal block (c1) and the rest of
+  // the trailing triangle (c2).
   for (int q0 = 0; q0 < wp; q0 += SB) {
     const int c1 = q0 + SB;
     if (c1 >= wp) break;
-    // (b) rows below: L(r, q0:+16) = A(r, q0:+16) X^T, one thread per row
-    for (int r = c1 + tid; r < wp; r += DTHREADS) {
-      float v[SB];
+    // (b) L(r, q0 + j) = sum_k A(r, q0 + k) X(j, k) for rows r >= c1; four
+    // lanes per row, lane group g owning columns 4g .. 4g + 3
+    const int nb = (wp - c1) * 4;
+    for (int e0 = 0; e0 < nb; e0 += DTHREADS) {
+      const int e = e0 + tid;
+      const int r = c1 + (e >> 2), g = e & 3;
+      float o[4] = {0.f, 0.f, 0.f, 0.f};
+      if (e < nb) {
 #pragma unroll
-      for (int k = 0; k < SB; ++k) v[k] = Lp[pidx(r, q0 + k)];
-#pragma unroll
-      for (int j = 0; j < SB; ++j) {
-        float o = 0.f;
-#pragma unroll
-        for (int k = 0; k <= j; ++k) o = fmaf(v[k], Xs[j * SB + k], o);
-        Lp[pidx(r, q0 + j)] = o;
+        for (int k = 0; k < SB; ++k) {
+          const float vk = Lp[pidx(r, q0 + k)];
+          const float4 x4 = *reinterpret_cast<const float4*>(&Xs[k * SB + 4 * g]);
+          o[0] = fmaf(vk, x4.x, o[0]);
+          o[1] = fmaf(vk, x4.y, o[1]);
+          o[2] = fmaf(vk, x4.z, o[2]);
+          o[3] = fmaf(vk, x4.w, o[3]);
+        }
       }
-    }
-    __syncthreads();
-    // (c1) the next sub-block column: rows [c1, wp) x cols [c1, c1 + 16);
-    // thread (row c1 + tid % 256, eight columns c1 + 8 * (tid / 256) ..)
-    {
-      const int r = c1 + (tid & 255), cbase = c1 + 8 * (tid >> 8);
-      if (r < wp) {
-        float lr[SB];
+      __syncwarp();
+      if (e < nb) {
 #pragma unroll
-        for (int k = 0; k < SB; ++k) lr[k] = Lp[pidx(r, q0 + k)];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int cc = cbase + u;
-          if (cc <= r) {
-            float sacc = 0.f;
-#pragma unroll
-            for (int k = 0; k < SB; ++k) sacc = fmaf(lr[k], Lp[pidx(cc, q0 + k)], sacc);
-            Lp[pidx(r, cc)] -= sacc;
-          }
+        for (int jj = 0; jj < 4; ++jj) {
+          Lp[pidx(r, q0 + 4 * g + jj)] = o[jj];
+          if (r < c1 + SB) Bk[(4 * g + jj) * SB + (r - c1)] = o[jj];
         }
       }
     }
     __syncthreads();
     if (warp == 0) {
-      factor_sub(c1);
+      warp_chol16(Lp, c1, w, Bk, Xs, xg + (c1 / SB) * SB * SB, status);
     } else {
+      // (c1) rows [c1 + 16, wp) x columns [c1, c1 + 16): lane group g of a
+      // row updates columns c1 + 4g .. + 3
+      const int c2s = c1 + SB;
+      const int nc = (wp - c2s) * 4;
+      for (int e = tid - 32; e < nc; e += DTHREADS - 32) {
+        const int r = c2s + (e >> 2), g = e & 3;
+        float o[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < SB; ++k) {
+          const float lk = Lp[pidx(r, q0 + k)];
+          const float4 b4 = *reinterpret_cast<const float4*>(&Bk[k * SB + 4 * g]);
+          o[0] = fmaf(lk, b4.x, o[0]);
+          o[1] = fmaf(lk, b4.y, o[1]);
+          o[2] = fmaf(lk, b4.z, o[2]);
+          o[3] = fmaf(lk, b4.w, o[3]);
+        }
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) Lp[pidx(r, c1 + 4 * g + jj)] -= o[jj];
+      }
       // (c2) trailing triangle [c2s, wp)^2 -= L(:, q0:+16) L(:, q0:+16)^T in
       // 32 x 32 tiles, one warp per tile (warps 1..); lane owns rows
       // r0 + (lane&7) + 8u (u < 4) and columns cc0 + (lane>>3) + 4v (v < 8)
-      const int c2s = c1 + SB;
       const int nt = (wp - c2s + 31) / 32;
       for (int tile = warp - 1; tile < nt * (nt + 1) / 2; tile += DTHREADS / 32 - 1) {
         int ti = 0;
@@ -242,78 +263,107 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
   }
 }
 
+// Floats of the staged block rows of L_WW: block row q >= 1 (columns k < 16q
+// of rows 16q .. 16q + 15) starts at lw_off(q), 16 values per k.
+__host__ __device__ constexpr int lw_off(int q) { return 128 * q * (q - 1); }
+
 // Rows [r0, r0 + 64) below the panel [k0, k0 + w): L_R L_WW^T = A_R by block
-// forward substitution over 16-column sub-blocks.  Thread (row tid % 64,
-// columns 4*(tid/64) .. +3 of the sub-block).
-__global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ arena,
-                                                           const BlkTask* __restrict__ tasks,
-                                                           const float* __restrict__ xinv,
-                                                           uint16_t* __restrict__ planes,
-                                                           int64_t pstride, int pitch) {
+// forward substitution over 16-column sub-blocks.  Each row is solved by two
+// lanes of one warp (lane & 15 picks the row, lane >> 4 the half of the
+// sub-block's columns); rows never depend on one another, so after the block
+// rows of L_WW and the sub-block inverses are staged once, the sub-steps need
+// no block-wide barrier.
+__global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ arena,
+                                                        const BlkTask* __restrict__ tasks,
+                                                        const float* __restrict__ xinv,
+                                                        uint16_t* __restrict__ planes,
+                                                        int64_t pstride, int pitch) {
   extern __shared__ __align__(16) float sm[];
-  float* Ar = sm;                // Ar[k*ALD + r] = A(r0 + r, k0 + k), then L
-  float* Lrow = Ar + PW * ALD;   // Lrow[k*16 + jj] = L(k0 + q0 + jj, k0 + k), k < q0
-  float* Xs = Lrow + PW * SB;    // X of the sub-block, Xs[j*16 + i] = X(i, j)
+  float* Ar = sm;                          // Ar[k*ALD + r] = A(r0 + r, k0 + k), then L
+  float* Lw = Ar + pitch * ALD;            // block rows of L_WW (lw_off layout)
+  float* Xs = Lw + lw_off(pitch / SB);     // Xs[q*256 + k*16 + j] = X_q(j, k)
   const BlkTask t = tasks[blockIdx.x];
   float* a = arena + t.off;
   const int64_t ld = t.ld;
   const int k0 = t.c, w = t.bw, r0 = t.r0, tid = threadIdx.x;
-  const int nr = min(64, t.m - r0);
-  const int wp = (w + SB - 1) / SB * SB;
+  const int nr = min(PROWS, t.m - r0);
+  const int nsb = (w + SB - 1) / SB, wp = nsb * SB;
   const float* xg = xinv + (int64_t)t.xi * XSZ;
-  for (int e = tid; e < 64 * wp; e += PTHREADS) {
-    const int r = e % 64, k = e / 64;
+  for (int e = tid; e < PROWS * wp; e += PTHREADS) {
+    const int r = e % PROWS, k = e / PROWS;
     if (r < nr && k < w) cp_async(&Ar[k * ALD + r], &a[(int64_t)(k0 + k) * ld + r0 + r]);
     else Ar[k * ALD + r] = 0.f;
   }
-  const int r = tid & 63, j0 = 4 * (tid >> 6);
-  for (int q0 = 0; q0 < wp; q0 += SB) {
-    // block row q0/16 of L (left of the sub-block) and the sub-block inverse
+  for (int q = 1; q < nsb; ++q) {
+    float* dst = Lw + lw_off(q);
+    const int q0 = q * SB;
     for (int e = tid; e < SB * q0; e += PTHREADS) {
       const int jj = e % SB, k = e / SB;
-      if (q0 + jj < w) cp_async(&Lrow[e], &a[(int64_t)(k0 + k) * ld + k0 + q0 + jj]);
-      else Lrow[e] = 0.f;
+      if (q0 + jj < w) cp_async(&dst[e], &a[(int64_t)(k0 + k) * ld + k0 + q0 + jj]);
+      else dst[e] = 0.f;
     }
-    for (int e = tid; e < SB * SB; e += PTHREADS) cp_async(&Xs[e], &xg[(q0 / SB) * SB * SB + e]);
-    cp_async_wait_all();
-    __syncthreads();
-    // correction by the earlier sub-blocks: one shared load of A and one
-    // 16-byte load of the block row per four fused multiply-adds
-    float v[4];
+  }
+  for (int e = tid; e < nsb * SB * SB; e += PTHREADS) cp_async(&Xs[e], &xg[e]);
+  cp_async_wait_all();
+  __syncthreads();
+  const int lane = tid & 31, h = lane >> 4;
+  const int r = (tid >> 5) * 16 + (lane & 15);
+  for (int q = 0; q < nsb; ++q) {
+    const int q0 = q * SB, c0 = q0 + 8 * h;  // this lane's eight columns
+    // correction by the earlier sub-blocks: one shared load of the row and
+    // two 16-byte loads of the block row per eight fused multiply-adds
+    float v[8];
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) v[jj] = Ar[(q0 + j0 + jj) * ALD + r];
+    for (int jj = 0; jj < 8; ++jj) v[jj] = Ar[(c0 + jj) * ALD + r];
+    const float* lq = Lw + lw_off(q) + 8 * h;
 #pragma unroll 4
     for (int k = 0; k < q0; ++k) {
       const float ar = Ar[k * ALD + r];
-      const float4 l4 = *reinterpret_cast<const float4*>(&Lrow[k * SB + j0]);
-      v[0] = fmaf(-ar, l4.x, v[0]);
-      v[1] = fmaf(-ar, l4.y, v[1]);
-      v[2] = fmaf(-ar, l4.z, v[2]);
-      v[3] = fmaf(-ar, l4.w, v[3]);
+      const float4 la = *reinterpret_cast<const float4*>(lq + k * SB);
+      const float4 lb = *reinterpret_cast<const float4*>(lq + k * SB + 4);
+      v[0] = fmaf(-ar, la.x, v[0]);
+      v[1] = fmaf(-ar, la.y, v[1]);
+      v[2] = fmaf(-ar, la.z, v[2]);
+      v[3] = fmaf(-ar, la.w, v[3]);
+      v[4] = fmaf(-ar, lb.x, v[4]);
+      v[5] = fmaf(-ar, lb.y, v[5]);
+      v[6] = fmaf(-ar, lb.z, v[6]);
+      v[7] = fmaf(-ar, lb.w, v[7]);
     }
-    __syncthreads();
+    // the whole corrected row of the sub-block from the partner lane
+    float lo[8], hi[8];
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) Ar[(q0 + j0 + jj) * ALD + r] = v[jj];
-    __syncthreads();
-    // L(r, q0 + j) = sum_k A'(r, q0 + k) X(j, k) (X lower triangular, zeros
-    // stored above the diagonal)
+    for (int jj = 0; jj < 8; ++jj) {
+      const float o = __shfl_xor_sync(0xffffffffu, v[jj], 16);
+      lo[jj] = h ? o : v[jj];
+      hi[jj] = h ? v[jj] : o;
+    }
+    // L(r, c0 + jj) = sum_k A'(r, q0 + k) X_q(8h + jj, k); X_q is lower
+    // triangular with zeros stored above the diagonal
+    const float* xq = Xs + q * SB * SB + 8 * h;
+    float o[8];
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) v[jj] = 0.f;
+    for (int jj = 0; jj < 8; ++jj) o[jj] = 0.f;
 #pragma unroll
     for (int k = 0; k < SB; ++k) {
-      const float ak = Ar[(q0 + k) * ALD + r];
-      const float4 x4 = *reinterpret_cast<const float4*>(&Xs[k * SB + j0]);
-      v[0] = fmaf(ak, x4.x, v[0]);
-      v[1] = fmaf(ak, x4.y, v[1]);
-      v[2] = fmaf(ak, x4.z, v[2]);
-      v[3] = fmaf(ak, x4.w, v[3]);
+      const float vk = k < 8 ? lo[k] : hi[k - 8];
+      const float4 xa = *reinterpret_cast<const float4*>(xq + k * SB);
+      const float4 xb = *reinterpret_cast<const float4*>(xq + k * SB + 4);
+      o[0] = fmaf(vk, xa.x, o[0]);
+      o[1] = fmaf(vk, xa.y, o[1]);
+      o[2] = fmaf(vk, xa.z, o[2]);
+      o[3] = fmaf(vk, xa.w, o[3]);
+      o[4] = fmaf(vk, xb.x, o[4]);
+      o[5] = fmaf(vk, xb.y, o[5]);
+      o[6] = fmaf(vk, xb.z, o[6]);
+      o[7] = fmaf(vk, xb.w, o[7]);
     }
-    __syncthreads();
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-      Ar[(q0 + j0 + jj) * ALD + r] = v[jj];
-      if (r < nr && q0 + j0 + jj < w) a[(int64_t)(k0 + q0 + j0 + jj) * ld + r0 + r] = v[jj];
+    for (int jj = 0; jj < 8; ++jj) {
+      Ar[(c0 + jj) * ALD + r] = o[jj];
+      if (r < nr && c0 + jj < w) a[(int64_t)(k0 + c0 + jj) * ld + r0 + r] = o[jj];
     }
+    __syncwarp();
   }
   if (t.base >= 0) {
     // the rows just solved, transposed and split into three BF16 planes, for
@@ -333,10 +383,10 @@ __global__ void __launch_bounds__(PTHREADS, 2) k_blk_panel(float* __restrict__ a
 }
 
 constexpr size_t diag_smem() {
-  return sizeof(float) * ((size_t)PW * (PW + 1) / 2 + SB * SB + SB * TLD);
+  return sizeof(float) * ((size_t)PW * (PW + 1) / 2 + 2 * SB * SB);
 }
-constexpr size_t panel_smem() {
-  return sizeof(float) * ((size_t)PW * ALD + PW * SB + SB * SB);
+constexpr size_t panel_smem(int pitch) {
+  return sizeof(float) * ((size_t)pitch * ALD + lw_off(pitch / SB) + (size_t)pitch * SB);
 }
 
 }  // namespace
@@ -345,7 +395,7 @@ void prepare_blocked_kernels() {
   SG_CUDA(cudaFuncSetAttribute(k_blk_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)diag_smem()));
   SG_CUDA(cudaFuncSetAttribute(k_blk_panel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)panel_smem()));
+                               (int)panel_smem(PW)));
 }
 
 void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, unsigned* status,
@@ -357,7 +407,7 @@ void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, uns
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
                       uint16_t* planes, int64_t pstride, int pitch, cudaStream_t s) {
   if (ntask <= 0) return;
-  k_blk_panel<<<ntask, PTHREADS, panel_smem(), s>>>(arena, t, xinv, planes, pstride, pitch);
+  k_blk_panel<<<ntask, PTHREADS, panel_smem(pitch), s>>>(arena, t, xinv, planes, pstride, pitch);
 }
 
 }  // namespace sylver_gb300
