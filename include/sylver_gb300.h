@@ -307,6 +307,10 @@ typedef struct {
                             (default 128); the trailing fully-summed update after each panel
                             runs on the tensor cores.  Negative: 64-column steps with SIMT
                             updates throughout */
+  int fs_panel_group;    /* FP32 Cholesky: outer panels per trailing fully-summed update, 1 to 8
+                            (default 2).  Within a group each panel but the last updates only
+                            the group's remaining columns; the columns past the group get one
+                            tensor-core update with K = group x panel width */
 } sylver_gb300_schedule_t;
 
 /* Set the schedule used by factorizations planned afterwards (a new fkeep);

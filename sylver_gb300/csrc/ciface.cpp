@@ -574,6 +574,7 @@ void sylver_gb300_set_schedule(sylver_gb300_schedule_t const* s) {
   c.solve_large_cols = s->solve_large_cols;
   c.ldlt_tpp_cols = s->ldlt_tpp_cols;
   c.fs_panel_cols = s->fs_panel_cols;
+  c.fs_panel_group = s->fs_panel_group;
 }
 
 void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
@@ -584,6 +585,7 @@ void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
   s->solve_large_cols = c.solve_large_cols;
   s->ldlt_tpp_cols = c.ldlt_tpp_cols;
   s->fs_panel_cols = c.fs_panel_cols;
+  s->fs_panel_group = c.fs_panel_group;
 }
 
 }  // extern "C"

@@ -108,7 +108,9 @@ constexpr int TC_KCHUNK = 64;
 // scratch.  For the panel kernel r0 is the first of the CTA's 64 rows
 // (>= pend), and base >= 0 is the stacked tensor-core panel row of front row
 // pend, where the kernel writes the rows it solves (transposed, split into
-// three BF16 planes) for the trailing update; base < 0: no trailing update.
+// three BF16 planes) for the later tensor-core updates, at K columns
+// [c mod pitch, + panel width) of planes with pitch K columns; base < 0: no
+// later update reads the panel.
 struct BlkTask {
   int64_t off;
   int ld, m, c, bw, pend, r0, xi, base;
@@ -173,8 +175,9 @@ void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStr
 void prepare_blocked_kernels();
 void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, unsigned* status,
                      cudaStream_t s);
+// pw: the panel width (shared-memory layout), pitch: K columns of the planes.
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      uint16_t* planes, int64_t pstride, int pitch, cudaStream_t s);
+                      uint16_t* planes, int64_t pstride, int pw, int pitch, cudaStream_t s);
 
 template <typename T> struct Tiles;
 template <> struct Tiles<double> {

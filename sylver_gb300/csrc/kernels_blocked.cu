@@ -277,11 +277,11 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
                                                         const BlkTask* __restrict__ tasks,
                                                         const float* __restrict__ xinv,
                                                         uint16_t* __restrict__ planes,
-                                                        int64_t pstride, int pitch) {
+                                                        int64_t pstride, int pw, int pitch) {
   extern __shared__ __align__(16) float sm[];
   float* Ar = sm;                          // Ar[k*ALD + r] = A(r0 + r, k0 + k), then L
-  float* Lw = Ar + pitch * ALD;            // block rows of L_WW (lw_off layout)
-  float* Xs = Lw + lw_off(pitch / SB);     // Xs[q*256 + k*16 + j] = X_q(j, k)
+  float* Lw = Ar + pw * ALD;               // block rows of L_WW (lw_off layout)
+  float* Xs = Lw + lw_off(pw / SB);        // Xs[q*256 + k*16 + j] = X_q(j, k)
   const BlkTask t = tasks[blockIdx.x];
   float* a = arena + t.off;
   const int64_t ld = t.ld;
@@ -370,11 +370,12 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
     // the trailing tensor-core update (k contiguous: coalesced writes)
     __syncthreads();
     const int64_t row0 = (int64_t)t.base + (r0 - t.pend);
-    for (int e = tid; e < nr * pitch; e += PTHREADS) {
-      const int rr = e / pitch, k = e % pitch;
+    const int koff = k0 % pitch;
+    for (int e = tid; e < nr * pw; e += PTHREADS) {
+      const int rr = e / pw, k = e % pw;
       uint16_t b0, b1, b2;
       bf16x3_split(k < w ? Ar[k * ALD + rr] : 0.f, b0, b1, b2);
-      const int64_t o = (row0 + rr) * pitch + k;
+      const int64_t o = (row0 + rr) * pitch + koff + k;
       planes[o] = b0;
       planes[pstride + o] = b1;
       planes[2 * pstride + o] = b2;
@@ -405,9 +406,10 @@ void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, uns
 }
 
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      uint16_t* planes, int64_t pstride, int pitch, cudaStream_t s) {
+                      uint16_t* planes, int64_t pstride, int pw, int pitch, cudaStream_t s) {
   if (ntask <= 0) return;
-  k_blk_panel<<<ntask, PTHREADS, panel_smem(pitch), s>>>(arena, t, xinv, planes, pstride, pitch);
+  k_blk_panel<<<ntask, PTHREADS, panel_smem(pw), s>>>(arena, t, xinv, planes, pstride, pw,
+                                                       pitch);
 }
 
 }  // namespace sylver_gb300

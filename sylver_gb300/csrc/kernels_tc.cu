@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           }
           unsigned char* st = smem + s * STAGE_BYTES;
           mbar_expect_tx(&full[s], STAGE_BYTES);
-          const int x = kc * TC_KC;
+          const int x = (t.kc0 + kc) * TC_KC;
           tma_load_2d(st + 0 * TILE_BYTES, &map0, x, t.a_row, &full[s]);
           tma_load_2d(st + 1 * TILE_BYTES, &map1, x, t.a_row, &full[s]);
           tma_load_2d(st + 2 * TILE_BYTES, &map2, x, t.a_row, &full[s]);

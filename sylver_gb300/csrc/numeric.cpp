@@ -227,10 +227,12 @@ void FKeep::plan_cholesky() {
   std::vector<TcSplit> tcs;
   std::vector<TcTask> tct;
   std::vector<double> tc_flops;
+  std::vector<std::pair<size_t, double>> tcop_flops;  // (op index, flops) of grouped updates
   std::vector<BlkTask> blkd, blkp;
   tclev.clear();
   blkinv_count = 0;
   const int PW = (f32 && use_tc) ? sched.panel_cols() : 0;
+  blk_pw = PW;
   std::vector<int> pos(st.n, -1);
   ops.clear();
   ops.push_back({Op::MEMSET, 0, 0, 0});
@@ -276,58 +278,85 @@ void FKeep::plan_cholesky() {
     // large fronts: panel steps over the fully-summed columns, batched
     int maxsteps = 0;
     if (PW > 0) {
-      // blocked path: outer panels of PW columns; the trailing fully-summed
-      // columns are updated once per panel on the tensor cores
+      // blocked path: outer panels of PW columns in groups of G.  After
+      // each panel but the group's last, the group's remaining columns get
+      // that panel's update on the tensor cores (K = PW); after the group
+      // the trailing fully-summed columns get the whole group's (K = G PW),
+      // which reads and writes the trailing columns once per group.
+      const int G = sched.panel_group();
+      const int GW = G * PW;
       int maxn = 0;
       for (int s : large) maxn = std::max(maxn, st.ncol[s]);
-      for (int k0 = 0; k0 < maxn; k0 += PW) {
-        // fronts whose fully-summed columns continue past this panel: their
-        // rows below the panel are stacked (transposed, 3xBF16 split) by the
-        // panel kernel for the tensor-core update of the trailing columns
-        const int p = k0 + PW;
+      for (int g0 = 0; g0 < maxn; g0 += GW) {
+        // rows [g0 + PW, m) of fronts with fully-summed columns past the
+        // group's first panel are stacked (transposed, 3xBF16 split, K
+        // columns [g PW, (g + 1) PW) written by the group's panel g)
+        const int q = g0 + PW;
         std::vector<int> base(ns, -1);
         int64_t rows = 0, mxr = 0;
         for (int s : large)
-          if (p < st.ncol[s]) {
+          if (q < st.ncol[s]) {
             base[s] = (int)rows;
-            mxr = std::max<int64_t>(mxr, st.nrow[s] - p);
-            rows += st.nrow[s] - p;
+            mxr = std::max<int64_t>(mxr, st.nrow[s] - q);
+            rows += st.nrow[s] - q;
           }
-        // the panel's diagonal block (one CTA per front), then the rows below
-        // it (one CTA per 64 rows)
-        const int64_t d0 = (int64_t)blkd.size(), p0 = (int64_t)blkp.size();
-        for (int s : large) {
-          const int m = st.nrow[s], n = st.ncol[s];
-          if (k0 >= n) continue;
-          const int pend = std::min(k0 + PW, n);
-          const int xi = (int)((int64_t)blkd.size() - d0);
-          blkd.push_back({off[s], ld[s], m, k0, pend - k0, pend, 0, xi, -1});
-          for (int r0 = pend; r0 < m; r0 += 64)
-            blkp.push_back({off[s], ld[s], m, k0, pend - k0, pend, r0, xi, base[s]});
+        const int lvl = rows > 0 ? (int)tclev.size() : -1;
+        if (rows > 0) {
+          tclev.push_back({GW, rows, mxr});
+          tc_flops.push_back(0.0);  // per-op figures in tcop_flops
         }
-        if ((int64_t)blkd.size() > d0) {
-          ops.push_back({Op::BDIAG, d0, (int64_t)blkd.size(), 0});
-          blkinv_count = std::max(blkinv_count, (int64_t)blkd.size() - d0);
+        // update of columns [c, ce) x rows [c, m) of every front with
+        // c < min(ce, n), by K columns [kc0, kc0 + nk) chunks of the group
+        auto tc_update = [&](int coff, int cend_off, int kc0, int nk) {
+          double fl = 0.0;
+          const int64_t tk0 = (int64_t)tct.size();
+          for (int s : large) {
+            if (base[s] < 0) continue;
+            const int m = st.nrow[s], n = st.ncol[s];
+            const int c = g0 + coff, ce = std::min(n, cend_off < 0 ? n : g0 + cend_off);
+            if (c >= ce) continue;
+            for (int col0 = c; col0 < ce; col0 += 128)
+              for (int row0 = col0; row0 < m; row0 += 128)
+                tct.push_back({off[s], ld[s], row0, col0, m, ce, base[s] + row0 - q,
+                               base[s] + col0 - q, nk, kc0});
+            // lower-triangle entries of rows [c, m) x cols [c, ce), times 2K
+            const double cnt = (double)(ce - c) * m - (0.5 * ce * (ce - 1.0) - 0.5 * c * (c - 1.0));
+            fl += 2.0 * nk * TC_KCHUNK * cnt;
+          }
+          if ((int64_t)tct.size() > tk0) {
+            tcop_flops.push_back({ops.size(), fl});
+            ops.push_back({Op::TCUPD, tk0, (int64_t)tct.size(), lvl});
+          }
+        };
+        for (int g = 0; g < G; ++g) {
+          const int k0 = g0 + g * PW;
+          if (k0 >= maxn) break;
+          // the panel's diagonal block (one CTA per front), then the rows
+          // below it (one CTA per 64 rows)
+          const int64_t d0 = (int64_t)blkd.size(), p0 = (int64_t)blkp.size();
+          for (int s : large) {
+            const int m = st.nrow[s], n = st.ncol[s];
+            if (k0 >= n) continue;
+            const int pend = std::min(k0 + PW, n);
+            const int xi = (int)((int64_t)blkd.size() - d0);
+            // stacked row of row pend: only when a later update of this
+            // group reads the panel (columns remain past it)
+            const int pb = (pend < n) ? base[s] + (pend - q) : -1;
+            blkd.push_back({off[s], ld[s], m, k0, pend - k0, pend, 0, xi, -1});
+            for (int r0 = pend; r0 < m; r0 += 64)
+              blkp.push_back({off[s], ld[s], m, k0, pend - k0, pend, r0, xi, pb});
+          }
+          if ((int64_t)blkd.size() > d0) {
+            ops.push_back({Op::BDIAG, d0, (int64_t)blkd.size(), 0});
+            blkinv_count = std::max(blkinv_count, (int64_t)blkd.size() - d0);
+          }
+          if ((int64_t)blkp.size() > p0) ops.push_back({Op::BPANEL, p0, (int64_t)blkp.size(), GW});
+          if (lvl < 0) continue;
+          // the group's next panels, by this one
+          if (g + 1 < G) tc_update((g + 1) * PW, GW, g * (PW / TC_KCHUNK), PW / TC_KCHUNK);
         }
-        if ((int64_t)blkp.size() > p0) ops.push_back({Op::BPANEL, p0, (int64_t)blkp.size(), PW});
-        if (rows == 0) continue;
-        double fl = 0.0;
-        const int64_t tk0 = (int64_t)tct.size();
-        for (int s : large) {
-          if (base[s] < 0) continue;
-          const int m = st.nrow[s], n = st.ncol[s];
-          for (int col0 = p; col0 < n; col0 += 128)
-            for (int row0 = col0; row0 < m; row0 += 128)
-              tct.push_back({off[s], ld[s], row0, col0, m, n, base[s] + row0 - p,
-                             base[s] + col0 - p, PW / TC_KCHUNK});
-          // lower-triangle entries of rows [p, m) x cols [p, n), times 2K
-          const double cnt = (double)(n - p) * m - (0.5 * n * (n - 1.0) - 0.5 * p * (p - 1.0));
-          fl += 2.0 * PW * cnt;
-        }
-        const int lvl = (int)tclev.size();
-        tclev.push_back({PW, rows, mxr});
-        tc_flops.push_back(fl);
-        ops.push_back({Op::TCUPD, tk0, (int64_t)tct.size(), lvl});
+        // the trailing fully-summed columns, by the whole group
+        if (lvl >= 0) tc_update(GW, -1, 0, GW / TC_KCHUNK);
       }
     } else {
       for (int s : large) maxsteps = std::max(maxsteps, (st.ncol[s] + NB - 1) / NB);
@@ -404,9 +433,10 @@ void FKeep::plan_cholesky() {
   ops.push_back({Op::INV, 0, 0, 0});
   // algorithmic flops of update launches: lower-triangle entries x 2K
   op_flops.assign(ops.size(), 0.0);
+  for (const auto& tf : tcop_flops) op_flops[tf.first] = tf.second;
   for (size_t q = 0; q < ops.size(); ++q) {
     if (ops[q].kind == Op::TCUPD) {
-      op_flops[q] = tc_flops[ops[q].aux];
+      if (op_flops[q] == 0.0) op_flops[q] = tc_flops[ops[q].aux];
       continue;
     }
     if (ops[q].kind != Op::UPD) continue;
@@ -528,7 +558,7 @@ void FKeep::run_ops(cudaStream_t s) {
       case Op::BPANEL:
         if constexpr (std::is_same<T, float>::value)
           launch_blk_panel(A, blkpanel.as<BlkTask>() + op.a, (int)cnt, blkinv.as<float>(),
-                           tcplanes.as<uint16_t>(), plane_stride, op.aux, s);
+                           tcplanes.as<uint16_t>(), plane_stride, blk_pw, op.aux, s);
         break;
       case Op::TCUPD:
         if constexpr (std::is_same<T, float>::value)

@@ -57,6 +57,7 @@ struct Schedule {
   int ldlt_tpp_cols = 0;     // LDL^T: fronts with <= fully-summed columns use TPP only
   int fs_panel_cols = 0;     // FP32 Cholesky: outer panel width of the blocked large-front
                              // path (multiple of 64, <= 256; <0: 64-column SIMT steps)
+  int fs_panel_group = 0;    // FP32 Cholesky: outer panels per trailing fully-summed update
   static Schedule& current();
   int small_rows(int compiled_max) const {
     return small_front_rows > 0 ? std::min(small_front_rows, compiled_max) : compiled_max;
@@ -69,6 +70,7 @@ struct Schedule {
     if (fs_panel_cols == 0) return 128;
     return std::max(BLK_B, std::min(BLK_W, fs_panel_cols / BLK_B * BLK_B));
   }
+  int panel_group() const { return fs_panel_group > 0 ? std::min(fs_panel_group, 8) : 2; }
 };
 
 // Process-wide device context: device 0, one non-blocking stream.
@@ -182,6 +184,7 @@ struct FKeep {
   // 64 x 64 inverses of one diagonal-block launch
   DevMem blkdiag, blkpanel, blkinv;
   int64_t blkinv_count = 0;
+  int blk_pw = 0;                  // outer panel width of the blocked path (0: unused)
 
   // host plan
   std::vector<int> order;            // level-ordered front indices

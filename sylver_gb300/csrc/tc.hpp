@@ -10,10 +10,12 @@ namespace sylver_gb300 {
 // One 128 x 128 tile of C -= P_a P_b^T for a contribution block:
 // C(i, j) = arena[c_off + j*ldc + i] for i in [row0, row0+128) < rowEnd,
 // j in [col0, col0+128) < colEnd, only i >= j written.  A rows start at
-// stacked panel row a_row, B rows at b_row; nk chunks of TC_KCHUNK along k.
+// stacked panel row a_row, B rows at b_row; nk chunks of TC_KCHUNK along k
+// starting at chunk kc0.
 struct TcTask {
   int64_t c_off;
   int ldc, row0, col0, rowEnd, colEnd, a_row, b_row, nk;
+  int kc0;
 };
 
 // Transposed 3xBF16 copy of front rows [n, m) x columns [c0, c0 + K) into

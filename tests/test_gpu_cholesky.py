@@ -153,14 +153,15 @@ def _dense_spd(n, seed):
     return w.SymMatrix.from_scipy(sp.csc_matrix(a)), a
 
 
-@pytest.mark.parametrize("width", [64, 128, 192, 256, -1])
-def test_fp32_panel_widths(sylver, orc, gpu, width):
-    """Blocked FP32 large-front path: every outer panel width (and the
-    64-column SIMT path, width < 0) gives FP32-accurate factors, and FP64
-    refinement reaches the 1e-14 backward error.  One dense 700 x 700 front
-    (11 diagonal blocks, the last one ragged) and a 3D grid whose separators
-    exceed one panel."""
-    sylver.set_schedule(fs_panel_cols=width)
+@pytest.mark.parametrize("width,group", [(64, 2), (128, 2), (192, 2), (256, 2), (-1, 0),
+                                         (128, 1), (128, 3), (64, 4), (192, 3)])
+def test_fp32_panel_widths(sylver, orc, gpu, width, group):
+    """Blocked FP32 large-front path: every outer panel width and number of
+    panels per trailing update (and the 64-column SIMT path, width < 0)
+    gives FP32-accurate factors, and FP64 refinement reaches the 1e-14
+    backward error.  One dense 700 x 700 front (the last panel and the last
+    group ragged) and a 3D grid whose separators exceed one panel."""
+    sylver.set_schedule(fs_panel_cols=width, fs_panel_group=group)
     try:
         a, dense = _dense_spd(700, 3)
         rng = np.random.default_rng(4)
