@@ -304,11 +304,11 @@ typedef struct {
                             (default 0: none) */
   int fs_panel_cols;     /* FP32 Cholesky: width of the outer panels in which the fully-summed
                             columns of large fronts are eliminated, a multiple of 64 up to 256
-                            (default 128); the trailing fully-summed update after each panel
+                            (default 64); the trailing fully-summed update after each panel
                             runs on the tensor cores.  Negative: 64-column steps with SIMT
                             updates throughout */
   int fs_panel_group;    /* FP32 Cholesky: outer panels per trailing fully-summed update, 1 to 8
-                            (default 2).  Within a group each panel but the last updates only
+                            (default 4).  Within a group each panel but the last updates only
                             the group's remaining columns; the columns past the group get one
                             tensor-core update with K = group x panel width */
 } sylver_gb300_schedule_t;

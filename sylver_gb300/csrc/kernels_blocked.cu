@@ -54,7 +54,7 @@ __device__ __forceinline__ int pidx(int i, int j) { return pcol(j) + i - j; }
 // xs and xg (both xs[k*16 + i] = X(i, k)).  A non-positive pivot is replaced
 // by one and reported when its column is below bwreal.
 __device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwreal,
-                                         const float* __restrict__ bk,
+                                         const float* __restrict__ bk, float* __restrict__ tt,
                                          float* __restrict__ xs, float* __restrict__ xg,
                                          unsigned* __restrict__ status) {
   const int lane = threadIdx.x & 31;
@@ -103,10 +103,15 @@ __device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwre
       if (li >= j) a[j] = fmaf(-lik, ljk, a[j]);
     }
   }
+  // L to the packed triangle and to the dense tile tt (tt[k*17 + i] =
+  // L(i, k)), which the inverse reads without packed-index arithmetic
   if (lane < SB) {
 #pragma unroll
     for (int k = 0; k < SB; ++k)
-      if (k <= li) Lp[pidx(q + li, q + k)] = a[k];
+      if (k <= li) {
+        Lp[pidx(q + li, q + k)] = a[k];
+        tt[k * (SB + 1) + li] = a[k];
+      }
   }
   __syncwarp();
   if (lane == 0 && bad) atomicOr(status, ST_NOT_POSDEF);
@@ -116,7 +121,7 @@ __device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwre
   for (int i = 0; i < SB; ++i) {
     float v = (i == li) ? 1.f : 0.f;
 #pragma unroll
-    for (int k = 0; k < i; ++k) v = fmaf(-Lp[pidx(q + i, q + k)], x[k], v);
+    for (int k = 0; k < i; ++k) v = fmaf(-tt[k * (SB + 1) + i], x[k], v);
     x[i] = v * rinv[i];
   }
   if (lane < SB) {
@@ -136,7 +141,8 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
   extern __shared__ __align__(16) float sm[];
   float* Xs = sm;                      // inverse of the current sub-block, Xs[k*16 + j] = X(j, k)
   float* Bk = Xs + SB * SB;            // Bk[m*16 + i] = L(c1 + i, q0 + m), the next sub-block's rows
-  float* Lp = Bk + SB * SB;            // packed lower triangle, PW rows
+  float* Tt = Bk + SB * SB;            // dense copy of the factorised sub-block (warp 0)
+  float* Lp = Tt + SB * (SB + 1);      // packed lower triangle, PW rows
   const BlkTask t = tasks[blockIdx.x];
   float* a = arena + t.off;
   const int64_t ld = t.ld;
@@ -152,13 +158,15 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
   }
   cp_async_wait_all();
   __syncthreads();
-  if (warp == 0) warp_chol16(Lp, 0, w, nullptr, Xs, xg, status);
+  if (warp == 0) warp_chol16(Lp, 0, w, nullptr, Tt, Xs, xg, status);
   __syncthreads();
   // Per 16-column sub-block q0: (b) all threads solve the rows below it with
   // its inverse; then warp 0 updates the next diagonal sub-block by it and
-  // factorises that (the serial pivot chain) while the other warps update
-  // the next sub-block column below its diagonal block (c1) and the rest of
-  // the trailing triangle (c2).
+  // factorises that (the serial pivot chain) while the warps of the other
+  // three schedulers update the next sub-block column below its diagonal
+  // block (c1) and the rest of the trailing triangle (c2); the warps that
+  // share warp 0's scheduler (warp % 4 == 0) wait, so the pivot chain
+  // issues without competition.
   for (int q0 = 0; q0 < wp; q0 += SB) {
     const int c1 = q0 + SB;
     if (c1 >= wp) break;
@@ -191,13 +199,16 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
     }
     __syncthreads();
     if (warp == 0) {
-      warp_chol16(Lp, c1, w, Bk, Xs, xg + (c1 / SB) * SB * SB, status);
-    } else {
+      warp_chol16(Lp, c1, w, Bk, Tt, Xs, xg + (c1 / SB) * SB * SB, status);
+    } else if (warp & 3) {
+      // the 12 update warps, numbered 0..11
+      const int uw = warp - 1 - (warp >> 2), utid = uw * 32 + lane;
+      constexpr int UTHREADS = DTHREADS / 32 * 3 / 4 * 32;
       // (c1) rows [c1 + 16, wp) x columns [c1, c1 + 16): lane group g of a
       // row updates columns c1 + 4g .. + 3
       const int c2s = c1 + SB;
       const int nc = (wp - c2s) * 4;
-      for (int e = tid - 32; e < nc; e += DTHREADS - 32) {
+      for (int e = utid; e < nc; e += UTHREADS) {
         const int r = c2s + (e >> 2), g = e & 3;
         float o[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
@@ -213,45 +224,39 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
         for (int jj = 0; jj < 4; ++jj) Lp[pidx(r, c1 + 4 * g + jj)] -= o[jj];
       }
       // (c2) trailing triangle [c2s, wp)^2 -= L(:, q0:+16) L(:, q0:+16)^T in
-      // 32 x 32 tiles, one warp per tile (warps 1..); lane owns rows
-      // r0 + (lane&7) + 8u (u < 4) and columns cc0 + (lane>>3) + 4v (v < 8)
-      const int nt = (wp - c2s + 31) / 32;
-      for (int tile = warp - 1; tile < nt * (nt + 1) / 2; tile += DTHREADS / 32 - 1) {
+      // 16 x 16 tiles, one update warp per tile; lane owns rows
+      // r0 + (lane&7) + 8u (u < 2) and columns cc0 + (lane>>3) + 4v (v < 4)
+      const int nt = (wp - c2s + 15) / 16;
+      for (int tile = uw; tile < nt * (nt + 1) / 2; tile += UTHREADS / 32) {
         int ti = 0;
         while ((ti + 1) * (ti + 2) / 2 <= tile) ++ti;
         const int tj = tile - ti * (ti + 1) / 2;
-        const int r0 = c2s + 32 * ti, cc0 = c2s + 32 * tj;
-        float acc[4][8];
+        const int r0 = c2s + 16 * ti, cc0 = c2s + 16 * tj;
+        float acc[2][4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < 2; ++u)
 #pragma unroll
-          for (int v = 0; v < 8; ++v) acc[u][v] = 0.f;
+          for (int v = 0; v < 4; ++v) acc[u][v] = 0.f;
         const int rl = lane & 7, cl = lane >> 3;
 #pragma unroll 4
         for (int k = 0; k < SB; ++k) {
           const float* colk = Lp + pcol(q0 + k) - (q0 + k);
-          float rv[4], cv[8];
+          float rv[2], cv[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int r = r0 + rl + 8 * u;
-            rv[u] = r < wp ? colk[r] : 0.f;
-          }
+          for (int u = 0; u < 2; ++u) rv[u] = colk[r0 + rl + 8 * u];
 #pragma unroll
-          for (int v = 0; v < 8; ++v) {
-            const int cc = cc0 + cl + 4 * v;
-            cv[v] = cc < wp ? colk[cc] : 0.f;
-          }
+          for (int v = 0; v < 4; ++v) cv[v] = colk[cc0 + cl + 4 * v];
 #pragma unroll
-          for (int u = 0; u < 4; ++u)
+          for (int u = 0; u < 2; ++u)
 #pragma unroll
-            for (int v = 0; v < 8; ++v) acc[u][v] = fmaf(rv[u], cv[v], acc[u][v]);
+            for (int v = 0; v < 4; ++v) acc[u][v] = fmaf(rv[u], cv[v], acc[u][v]);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
+        for (int u = 0; u < 2; ++u)
 #pragma unroll
-          for (int v = 0; v < 8; ++v) {
+          for (int v = 0; v < 4; ++v) {
             const int r = r0 + rl + 8 * u, cc = cc0 + cl + 4 * v;
-            if (r < wp && cc <= r) Lp[pidx(r, cc)] -= acc[u][v];
+            if (cc <= r) Lp[pidx(r, cc)] -= acc[u][v];
           }
       }
     }
@@ -384,7 +389,7 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
 }
 
 constexpr size_t diag_smem() {
-  return sizeof(float) * ((size_t)PW * (PW + 1) / 2 + 2 * SB * SB);
+  return sizeof(float) * ((size_t)PW * (PW + 1) / 2 + 2 * SB * SB + SB * (SB + 1));
 }
 constexpr size_t panel_smem(int pitch) {
   return sizeof(float) * ((size_t)pitch * ALD + lw_off(pitch / SB) + (size_t)pitch * SB);

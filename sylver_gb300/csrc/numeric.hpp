@@ -67,10 +67,10 @@ struct Schedule {
   // 0: legacy SIMT panel steps, else the outer panel width
   int panel_cols() const {
     if (fs_panel_cols < 0) return 0;
-    if (fs_panel_cols == 0) return 128;
+    if (fs_panel_cols == 0) return 64;
     return std::max(BLK_B, std::min(BLK_W, fs_panel_cols / BLK_B * BLK_B));
   }
-  int panel_group() const { return fs_panel_group > 0 ? std::min(fs_panel_group, 8) : 2; }
+  int panel_group() const { return fs_panel_group > 0 ? std::min(fs_panel_group, 8) : 4; }
 };
 
 // Process-wide device context: device 0, one non-blocking stream.
