@@ -257,8 +257,8 @@ int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, 
  * 0 small fronts forward, 1 small fronts backward, 2 + k for the large-front
  * launches (k: 0/1 gather forward/backward, 2/3 scatter forward/backward,
  * 4 diagonal block forward, 5 rows below forward, 6 rows below backward,
- * 7 diagonal block backward, 8 contribution rows backward).  Arrays hold 12
- * entries.  Returns 0, or -98 for
+ * 7 diagonal block backward, 8 contribution rows backward, 9 rows below
+ * forward, one row per thread).  Arrays hold 12 entries.  Returns 0, or -98 for
  * an LDL^T factor or nrhs outside 1..32.  No reference counterpart. */
 int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches);
 

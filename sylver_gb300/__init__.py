@@ -304,7 +304,7 @@ class Factor:
 
     SOLVE_KINDS = ("small_fwd", "small_bwd", "gather_fwd", "gather_bwd", "scatter_fwd",
                    "scatter_bwd", "diag_fwd", "rows_fwd", "rows_bwd", "diag_bwd", "cb_bwd",
-                   "unused")
+                   "rows_fwd_thread")
 
     def profile_solve(self, nrhs=16):
         """Per-kernel-kind timing of one forward + backward sweep (no graph)."""

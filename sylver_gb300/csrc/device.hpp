@@ -199,6 +199,13 @@ template <typename T, typename ACC>
 void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
                       ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
                       bool unit_diag, cudaStream_t s);
+// Fronts of at most maxm rows with their right-hand-side rows on chip
+// (forward or backward); false, launching nothing, when maxm x nrhs rows do
+// not fit.
+template <typename T, typename ACC>
+bool launch_solve_small(bool fwd, const T* arena, const FrontDesc* fr, int nfronts,
+                        const int* rlist, ACC* x, int n, int nrhs, int maxm, bool unit_diag,
+                        cudaStream_t s);
 
 // Large-front blocked sweeps (block width 64).  Task f indexes the level's
 // FrontDesc array; c0/bw give the diagonal block, r0 the first row of a tile.
@@ -210,13 +217,15 @@ struct LTask {
 enum LsKind {
   LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD,
   LS_FWD_DIAG2, LS_FWD_UPD2, LS_BWD_RED2, LS_BWD_DIAG2,
-  LS_BWD_CB    // contribution rows' share of every block, once before the steps (backward)
+  LS_BWD_CB,   // contribution rows' share of every block, once before the steps (backward)
+  LS_FWD_ROWS  // forward update with one row per thread (steps with many rows)
 };
 constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
 constexpr int LSOLVE_BW2 = 256;  // columns per solve step
 constexpr int LSOLVE_UPD_ROWS = 32;  // rows per forward-update CTA
 constexpr int LSOLVE_RED_ROWS = 64;  // rows per backward-reduction CTA
 constexpr int LSOLVE_CB_ROWS = 256;  // contribution rows per backward CB CTA
+constexpr int LSOLVE_ROWS_T = 128;   // rows per one-row-per-thread forward-update CTA
 // Large fronts are swept block by block; the backward steps reduce over the
 // fully-summed rows only, because the contribution rows (>= n) contribute to
 // every backward block once, before the backward blocks (LS_BWD_CB).

@@ -22,6 +22,9 @@ constexpr int SB = 32;      // column block
 constexpr int MAXR = 32;    // right-hand sides per launch
 constexpr int RC = 8;       // right-hand sides per register chunk
 constexpr int GB = 8;       // gather/scatter elements in flight per thread
+// dynamic shared memory of the on-chip small-front kernels (right-hand-side
+// rows and their destinations)
+constexpr size_t SMALL_SOLVE_SMEM = 160 * 1024;
 
 template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
 
@@ -231,6 +234,204 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
     for (int u = 0; u < GB; ++u) {
       const int idx = base + tid + 256 * u;
       if (dsti[u] >= 0) x[(int64_t)(idx / m) * n + dsti[u]] = v[u];
+    }
+  }
+}
+
+// Small fronts whose right-hand-side rows fit in shared memory: the rows
+// (ys[r*m + i], r < nrhs) and their destinations stay on chip from the gather
+// to the scatter, so the column blocks touch global memory only for L.
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_solve_fwd_s(const T* __restrict__ arena,
+                                                     const FrontDesc* __restrict__ fr,
+                                                     const int* __restrict__ rlist,
+                                                     ACC* __restrict__ x, int n, int nrhs,
+                                                     bool unit) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
+  __shared__ ACC rdg[SB];         // 1 / L(c0 + k, c0 + k)
+  const FrontDesc f = fr[blockIdx.x];
+  const T* L = arena + f.off;
+  const int ld = f.ld, m = f.m, nc = f.n, mr = m * nrhs;
+  ACC* ys = reinterpret_cast<ACC*>(dsm);
+  int* rls = reinterpret_cast<int*>(ys + mr);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < m; i += 256) rls[i] = rlist[f.rl + i];
+  __syncthreads();
+  // the pivot rows are gathered; the rows below start at zero and collect
+  // this front's contribution, which the scatter adds to the ancestors'
+  // rows (sibling fronts of the launch add to the same rows)
+  for (int base = 0; base < mr; base += GB * 256) {
+    ACC v[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u, i = idx % m;
+      v[u] = (idx < mr && i < nc) ? x[(int64_t)(idx / m) * n + rls[i]] : ACC(0);
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u;
+      if (idx < mr) ys[idx] = v[u];
+    }
+  }
+  __syncthreads();
+  for (int c0 = 0; c0 < nc; c0 += SB) {
+    const int bw = min(SB, nc - c0), c1 = c0 + bw;
+    {
+      ACC lv[SB * SB / 256];
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u, i = e % SB, k = e / SB;
+        lv[u] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+      }
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u;
+        Ld[e / SB][e % SB] = lv[u];
+        if (e % SB == e / SB) rdg[e % SB] = (e % SB < bw && !unit) ? ACC(1) / lv[u] : ACC(1);
+      }
+    }
+    __syncthreads();
+    // diagonal block: one right-hand side per warp at a time
+    for (int r = warp; r < nrhs; r += 8) {
+      ACC v = (lane < bw) ? ys[r * m + c0 + lane] : ACC(0);
+      for (int kk = 0; kk < bw; ++kk) {
+        const ACC vk = __shfl_sync(0xffffffffu, v, kk) * rdg[kk];
+        if (lane == kk) v = vk;
+        if (lane > kk && lane < bw) v -= Ld[kk][lane] * vk;
+      }
+      if (lane < bw) ys[r * m + c0 + lane] = v;
+    }
+    __syncthreads();
+    // rows below the block: one row per thread, sixteen right-hand sides
+    // per pass, eight columns of L in flight
+    constexpr int RF = 16, KF = 8;
+    for (int i = c1 + tid; i < m; i += 256) {
+      for (int r0 = 0; r0 < nrhs; r0 += RF) {
+        ACC acc[RF];
+#pragma unroll
+        for (int q = 0; q < RF; ++q) acc[q] = ACC(0);
+        for (int kb = 0; kb < bw; kb += KF) {
+          ACC lv[KF];
+#pragma unroll
+          for (int kk = 0; kk < KF; ++kk)
+            lv[kk] = (kb + kk < bw) ? (ACC)L[(int64_t)(c0 + kb + kk) * ld + i] : ACC(0);
+#pragma unroll
+          for (int kk = 0; kk < KF; ++kk) {
+            const int row = c0 + min(kb + kk, bw - 1);
+#pragma unroll
+            for (int q = 0; q < RF; ++q) acc[q] += lv[kk] * ys[min(r0 + q, nrhs - 1) * m + row];
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < RF; ++q)
+          if (r0 + q < nrhs) ys[(r0 + q) * m + i] -= acc[q];
+      }
+    }
+    __syncthreads();
+  }
+  for (int base = 0; base < mr; base += GB * 256) {
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u;
+      if (idx >= mr) break;
+      const int i = idx % m;
+      ACC* dst = x + (int64_t)(idx / m) * n + rls[i];
+      if (i < nc) *dst = ys[idx];
+      else aadd(dst, ys[idx]);
+    }
+  }
+}
+
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(256) k_solve_bwd_s(const T* __restrict__ arena,
+                                                     const FrontDesc* __restrict__ fr,
+                                                     const int* __restrict__ rlist,
+                                                     ACC* __restrict__ x, int n, int nrhs,
+                                                     bool unit) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ ACC tt[SB][MAXR];
+  __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
+  __shared__ ACC rdg[SB];
+  const FrontDesc f = fr[blockIdx.x];
+  const T* L = arena + f.off;
+  const int ld = f.ld, m = f.m, nc = f.n, mr = m * nrhs;
+  ACC* ys = reinterpret_cast<ACC*>(dsm);
+  int* rls = reinterpret_cast<int*>(ys + mr);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  for (int i = tid; i < m; i += 256) rls[i] = rlist[f.rl + i];
+  __syncthreads();
+  for (int base = 0; base < mr; base += GB * 256) {
+    ACC v[GB];
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u;
+      v[u] = idx < mr ? x[(int64_t)(idx / m) * n + rls[idx % m]] : ACC(0);
+    }
+#pragma unroll
+    for (int u = 0; u < GB; ++u) {
+      const int idx = base + tid + 256 * u;
+      if (idx < mr) ys[idx] = v[u];
+    }
+  }
+  __syncthreads();
+  constexpr int RB = 16;  // right-hand sides per pass of a column
+  const int nblk = (nc + SB - 1) / SB;
+  for (int b = nblk - 1; b >= 0; --b) {
+    const int c0 = b * SB, bw = min(SB, nc - c0), c1 = c0 + bw;
+    // tt[kk][r] = sum_{i >= c1} L(i, c0 + kk) x(i, r): one column per warp
+    for (int kk = warp; kk < bw; kk += 8) {
+      const T* col = L + (int64_t)(c0 + kk) * ld;
+      for (int r0 = 0; r0 < nrhs; r0 += RB) {
+        ACC acc[RB];
+#pragma unroll
+        for (int q = 0; q < RB; ++q) acc[q] = ACC(0);
+#pragma unroll 2
+        for (int i = c1 + lane; i < m; i += 32) {
+          const ACC l = (ACC)col[i];
+#pragma unroll
+          for (int q = 0; q < RB; ++q) acc[q] += l * ys[min(r0 + q, nrhs - 1) * m + i];
+        }
+#pragma unroll
+        for (int q = 0; q < RB; ++q) {
+          ACC sv = acc[q];
+          for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
+          if (lane == 0 && r0 + q < nrhs) tt[kk][r0 + q] = sv;
+        }
+      }
+    }
+    {
+      ACC lv[SB * SB / 256];
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u, i = e % SB, k = e / SB;
+        lv[u] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
+      }
+#pragma unroll
+      for (int u = 0; u < SB * SB / 256; ++u) {
+        const int e = tid + 256 * u;
+        Ld[e / SB][e % SB] = lv[u];
+        if (e % SB == e / SB) rdg[e % SB] = (e % SB < bw && !unit) ? ACC(1) / lv[u] : ACC(1);
+      }
+    }
+    __syncthreads();
+    // diagonal block (transposed): one right-hand side per warp at a time
+    for (int r = warp; r < nrhs; r += 8) {
+      ACC v = (lane < bw) ? ys[r * m + c0 + lane] - tt[lane][r] : ACC(0);
+      for (int kk = bw - 1; kk >= 0; --kk) {
+        if (lane == kk) v = v * rdg[kk];
+        const ACC zk = __shfl_sync(0xffffffffu, v, kk);
+        if (lane < kk) v -= Ld[lane][kk] * zk;
+      }
+      if (lane < bw) ys[r * m + c0 + lane] = v;
+    }
+    __syncthreads();
+  }
+  for (int base = 0; base < nc * nrhs; base += 256) {
+    const int idx = base + tid;
+    if (idx < nc * nrhs) {
+      const int i = idx % nc, r = idx / nc;
+      x[(int64_t)r * n + rls[i]] = ys[r * m + i];
     }
   }
 }
@@ -575,6 +776,65 @@ template <> struct Vec4<double> {
   using V = double2;
   static constexpr int W = 2;
 };
+
+// Forward update of rows [r0, r0 + 128) below the block [c0, c0 + bw) of a
+// large front, one row per thread: x(i, :) -= L(i, c0:c0+bw) y(c0:c0+bw, :)
+// with sixteen right-hand sides per pass in registers and the block's solved
+// rows in shared memory.  For steps with many rows (the lower levels, many
+// fronts with narrow blocks), where the k-split update's per-CTA staging and
+// reduction cost more than the product.
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(LSOLVE_ROWS_T) k_fwd_rows(const LTask* __restrict__ tasks,
+                                                            LsArgs<T, ACC> a) {
+  using V = typename Vec4<ACC>::V;
+  constexpr int VW = Vec4<ACC>::W, RP = 16, KU = 16;
+  __shared__ __align__(16) ACC yb[BW2 * RP];  // yb[k*16 + q] = y(c0 + k, rg + q)
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
+  const int tid = threadIdx.x, i = t.r0 + tid, bw = t.bw;
+  const T* Li = a.arena + f.off + (int64_t)t.c0 * f.ld + i;
+  for (int rg = 0; rg < a.nrhs; rg += RP) {
+    const int nr = min(RP, a.nrhs - rg);
+    __syncthreads();  // the previous pass's block is no longer read
+    for (int e = tid; e < bw * RP; e += LSOLVE_ROWS_T) {
+      const int k = e % bw, q = e / bw;
+      yb[k * RP + q] = q < nr ? ysl[(int64_t)(rg + q) * f.m + t.c0 + k] : ACC(0);
+    }
+    __syncthreads();
+    if (i >= f.m) continue;
+    ACC acc[RP];
+#pragma unroll
+    for (int q = 0; q < RP; ++q) acc[q] = ACC(0);
+    for (int k0 = 0; k0 < bw; k0 += KU) {
+      ACC l[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u)
+        l[u] = (k0 + u < bw) ? (ACC)Li[(int64_t)(k0 + u) * f.ld] : ACC(0);
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        const V* yv = reinterpret_cast<const V*>(yb + min(k0 + u, bw - 1) * RP);
+#pragma unroll
+        for (int q = 0; q < RP / VW; ++q) {
+          const V y4 = yv[q];
+          if constexpr (VW == 4) {
+            acc[4 * q + 0] += l[u] * y4.x;
+            acc[4 * q + 1] += l[u] * y4.y;
+            acc[4 * q + 2] += l[u] * y4.z;
+            acc[4 * q + 3] += l[u] * y4.w;
+          } else {
+            acc[2 * q + 0] += l[u] * y4.x;
+            acc[2 * q + 1] += l[u] * y4.y;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RP; ++q)
+      if (q < nr) xs[(int64_t)(rg + q) * f.m + i] -= acc[q];
+  }
+}
 
 template <typename T, typename ACC, bool BWD>
 __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks,
@@ -961,6 +1221,25 @@ void launch_solve_fwd(const T* arena, const FrontDesc* fr, int nfronts, const in
                                               unit_diag);
 }
 
+template <typename ACC>
+size_t small_solve_smem(int maxm, int nrhs) {
+  return (size_t)maxm * nrhs * sizeof(ACC) + (size_t)maxm * sizeof(int);
+}
+
+template <typename T, typename ACC>
+bool launch_solve_small(bool fwd, const T* arena, const FrontDesc* fr, int nfronts,
+                        const int* rlist, ACC* x, int n, int nrhs, int maxm, bool unit_diag,
+                        cudaStream_t s) {
+  const size_t sm = small_solve_smem<ACC>(maxm, nrhs);
+  if (sm > SMALL_SOLVE_SMEM || nrhs > MAXR) return false;
+  if (nfronts <= 0) return true;
+  if (fwd)
+    k_solve_fwd_s<T, ACC><<<nfronts, 256, sm, s>>>(arena, fr, rlist, x, n, nrhs, unit_diag);
+  else
+    k_solve_bwd_s<T, ACC><<<nfronts, 256, sm, s>>>(arena, fr, rlist, x, n, nrhs, unit_diag);
+  return true;
+}
+
 template <typename T, typename ACC>
 void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
                       ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
@@ -1047,6 +1326,9 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
     case LS_BWD_CB:
       k_bwd_cb<T, ACC><<<ntask, 512, bwd_cb_smem<T>(), s>>>(tasks, a);
       break;
+    case LS_FWD_ROWS:
+      k_fwd_rows<T, ACC><<<ntask, LSOLVE_ROWS_T, 0, s>>>(tasks, a);
+      break;
     case LS_BWD_RED2:
       k_bwd_red3<T, ACC><<<ntask, 512, bwd_red_smem<T>(), s>>>(tasks, a);
       break;
@@ -1071,6 +1353,10 @@ void prepare_solve_kernels() {
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
   SG_CUDA(cudaFuncSetAttribute(k_diag_mv<T, T, true>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
+  SG_CUDA(cudaFuncSetAttribute(k_solve_fwd_s<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)SMALL_SOLVE_SMEM));
+  SG_CUDA(cudaFuncSetAttribute(k_solve_bwd_s<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)SMALL_SOLVE_SMEM));
   SG_CUDA(cudaFuncSetAttribute(k_fwd_upd3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)fwd_upd_smem<T>()));
   SG_CUDA(cudaFuncSetAttribute(k_bwd_red3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1116,6 +1402,12 @@ template void launch_solve_fwd<double, double>(const double*, const FrontDesc*, 
 template void launch_solve_bwd<double, double>(const double*, const FrontDesc*, int,
                                                const int*, double*, int, int, double*,
                                                const int64_t*, bool, cudaStream_t);
+template bool launch_solve_small<float, float>(bool, const float*, const FrontDesc*, int,
+                                               const int*, float*, int, int, int, bool,
+                                               cudaStream_t);
+template bool launch_solve_small<double, double>(bool, const double*, const FrontDesc*, int,
+                                                 const int*, double*, int, int, int, bool,
+                                                 cudaStream_t);
 template void launch_permute_in<float>(const double*, int, float*, const int*, int, int,
                                        cudaStream_t);
 template void launch_permute_in<double>(const double*, int, double*, const int*, int, int,

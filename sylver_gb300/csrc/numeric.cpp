@@ -696,6 +696,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
     v.nfront = L.f1 - L.f0;
     v.nsmall = 0;
     while (v.nsmall < v.nfront && !is_large(hfr[L.f0 + v.nsmall])) v.nsmall++;
+    for (int f = 0; f < v.nsmall; ++f) v.small_maxm = std::max(v.small_maxm, hfr[L.f0 + f].m);
     max_large = std::max(max_large, v.nfront);
     auto push = [&](std::vector<SOp>& ops, int kind, int64_t a) {
       int64_t b = (int64_t)htasks.size();
@@ -734,6 +735,17 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
       // the fully-summed rows (< n) only
       auto step = [&](std::vector<SOp>& ops, int kind, int b, bool diag) {
         int64_t a = (int64_t)htasks.size();
+        if (kind == LS_FWD_UPD2) {
+          // steps with rows for at least two one-row-per-thread CTAs per SM
+          // use that update; the k-split update keeps the top levels busy
+          int64_t rows = 0;
+          for (int f = v.nsmall; f < v.nfront; ++f) {
+            const FrontDesc& d = hfr[L.f0 + f];
+            const int c1 = std::min(d.n, (b + 1) * LB2);
+            if (b * LB2 < d.n) rows += d.m - c1;
+          }
+          if (rows >= (int64_t)2 * 152 * LSOLVE_ROWS_T) kind = LS_FWD_ROWS;
+        }
         for (int f = v.nsmall; f < v.nfront; ++f) {
           const FrontDesc& d = hfr[L.f0 + f];
           int c0 = b * LB2;
@@ -742,6 +754,8 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
           else if (kind == LS_FWD_UPD2)
             for (int r0 = c1; r0 < d.m; r0 += LSOLVE_UPD_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
+          else if (kind == LS_FWD_ROWS)
+            for (int r0 = c1; r0 < d.m; r0 += LSOLVE_ROWS_T) htasks.push_back({f, c0, bw, r0, 0, 0});
           else
             for (int r0 = c1; r0 < d.n; r0 += LSOLVE_RED_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
         }
@@ -817,10 +831,13 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
     const FrontDesc* fr = dfr + v.f0;
     const int64_t* sc = dscr + v.f0;
     if (v.nsmall > 0) {
-      if (fwd) launch_solve_fwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc,
-                                        unit, s);
-      else launch_solve_bwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc, unit,
-                                    s);
+      if (!launch_solve_small<T, ACC>(fwd, arena, fr, v.nsmall, rlist, x, n, nrhs, v.small_maxm,
+                                      unit, s)) {
+        if (fwd) launch_solve_fwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc,
+                                          unit, s);
+        else launch_solve_bwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc, unit,
+                                      s);
+      }
       if (prof) mark(fwd ? 0 : 1, s);
     }
     LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),

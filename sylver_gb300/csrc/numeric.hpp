@@ -123,6 +123,7 @@ struct SolvePlan {
   };
   struct Lv {
     int f0 = 0, nsmall = 0, nfront = 0;
+    int small_maxm = 0;  // most rows of the level's small fronts
     std::vector<SOp> fwd, bwd;
   };
   std::vector<Lv> lv;
