@@ -237,15 +237,22 @@ def run_ours(args, rank, ws):
     full = a.to_scipy_full()
     be_host = float(w.backward_error(full, np.asfortranarray(x_h), prob.rhs).max())
 
-    # e2e through the reference C-ABI with host buffers
-    x_host = np.empty((n, nrhs), order="F")
+    # e2e through the reference C-ABI with host buffers in pinned memory: the
+    # values and the right-hand sides go host -> device and the solution
+    # device -> host inside every step
+    val_host = torch.empty(a.val.shape, dtype=torch.float64, pin_memory=True).numpy()
+    val_host[:] = a.val
+    rhs_t = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
+    rhs_t.numpy().T[:] = prob.rhs
+    x_t = torch.empty((nrhs, n), dtype=torch.float64, pin_memory=True)
+    x_host = x_t.numpy().T  # n x nrhs, column-major, ldx = n
     f2 = ctypes.c_void_p()
 
     def step_e2e():
-        lib.spldlt_factorize_mixed(True, None, None, a.val.ctypes.data_as(P), None, an.akeep,
+        lib.spldlt_factorize_mixed(True, None, None, val_host.ctypes.data_as(P), None, an.akeep,
                                    ctypes.byref(f2), ctypes.byref(opts), ctypes.byref(inf),
                                    prec, args.tol, maxit)
-        x_host[:] = prob.rhs
+        x_t.copy_(rhs_t)  # the in-place solve overwrites x: restore the right-hand sides
         sinf = sg.Inform()
         lib.spldlt_solve(0, nrhs, x_host.ctypes.data_as(P), n, an.akeep, f2, ctypes.byref(opts),
                          ctypes.byref(sinf))

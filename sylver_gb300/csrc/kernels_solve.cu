@@ -303,28 +303,24 @@ __global__ void __launch_bounds__(256) k_solve_fwd_s(const T* __restrict__ arena
       if (lane < bw) ys[r * m + c0 + lane] = v;
     }
     __syncthreads();
-    // rows below the block: one row per thread, sixteen right-hand sides
-    // per pass, eight columns of L in flight
-    constexpr int RF = 16, KF = 8;
+    // rows below the block: one row per thread, its block row of L loaded
+    // at once, eight right-hand sides per pass
     for (int i = c1 + tid; i < m; i += 256) {
-      for (int r0 = 0; r0 < nrhs; r0 += RF) {
-        ACC acc[RF];
+      ACC lv[SB];
 #pragma unroll
-        for (int q = 0; q < RF; ++q) acc[q] = ACC(0);
-        for (int kb = 0; kb < bw; kb += KF) {
-          ACC lv[KF];
+      for (int kk = 0; kk < SB; ++kk) lv[kk] = (kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * ld + i] : ACC(0);
+      for (int r0 = 0; r0 < nrhs; r0 += RC) {
+        ACC acc[RC];
 #pragma unroll
-          for (int kk = 0; kk < KF; ++kk)
-            lv[kk] = (kb + kk < bw) ? (ACC)L[(int64_t)(c0 + kb + kk) * ld + i] : ACC(0);
+        for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
 #pragma unroll
-          for (int kk = 0; kk < KF; ++kk) {
-            const int row = c0 + min(kb + kk, bw - 1);
+        for (int kk = 0; kk < SB; ++kk) {
+          const int row = c0 + min(kk, bw - 1);
 #pragma unroll
-            for (int q = 0; q < RF; ++q) acc[q] += lv[kk] * ys[min(r0 + q, nrhs - 1) * m + row];
-          }
+          for (int q = 0; q < RC; ++q) acc[q] += lv[kk] * ys[min(r0 + q, nrhs - 1) * m + row];
         }
 #pragma unroll
-        for (int q = 0; q < RF; ++q)
+        for (int q = 0; q < RC; ++q)
           if (r0 + q < nrhs) ys[(r0 + q) * m + i] -= acc[q];
       }
     }
