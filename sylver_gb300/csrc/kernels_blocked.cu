@@ -50,9 +50,10 @@ __device__ __forceinline__ int pidx(int i, int j) { return pcol(j) + i - j; }
 // packed triangle Lp, in registers (lane i < 16 holds row i; lanes 16..31
 // repeat lanes 0..15).  With bk != nullptr the sub-block is first updated
 // by the 16 columns left of it: A(q+i, q+k) -= sum_m L(q+i, m) L(q+k, m),
-// bk[m*16 + i] = L(q + i, q - 16 + m).  Writes L back to Lp and X = L^-1 to
-// xs and xg (both xs[k*16 + i] = X(i, k)).  A non-positive pivot is replaced
-// by one and reported when its column is below bwreal.
+// bk[m*16 + i] = L(q + i, q - 16 + m).  Writes L back to Lp and to tt
+// (tt[k*16 + i] = L(i, k), 16-byte aligned) and X = L^-1 to xs and xg (both
+// xs[k*16 + i] = X(i, k)).  A non-positive pivot is replaced by one and
+// reported when its column is below bwreal.
 __device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwreal,
                                          const float* __restrict__ bk, float* __restrict__ tt,
                                          float* __restrict__ xs, float* __restrict__ xg,
@@ -82,7 +83,8 @@ __device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwre
   // both the column scaling and the inverse multiply by it -- IEEE sqrt and
   // division cost three times as long per 16 columns.  Lane k + 1 forms the
   // next pivot from its own l(k+1, k), so only one shuffle per column sits
-  // on the chain.
+  // on the chain; the column itself reaches the other lanes through tt
+  // (16-byte loads).
   float dn = __shfl_sync(0xffffffffu, a[0], 0);
 #pragma unroll
   for (int k = 0; k < SB; ++k) {
@@ -97,21 +99,24 @@ __device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwre
     const float lik = (li == k) ? d * r : a[k] * r;
     a[k] = lik;
     if (k + 1 < SB) dn = __shfl_sync(0xffffffffu, fmaf(-lik, lik, a[k + 1]), k + 1);
+    if (lane < SB) tt[k * SB + li] = lik;
+    __syncwarp();
 #pragma unroll
-    for (int j = k + 1; j < SB; ++j) {
-      const float ljk = __shfl_sync(0xffffffffu, lik, j);
-      if (li >= j) a[j] = fmaf(-lik, ljk, a[j]);
+    for (int j4 = ((k + 1) & ~3); j4 < SB; j4 += 4) {
+      const float4 c4 = *reinterpret_cast<const float4*>(&tt[k * SB + j4]);
+      const float cj[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int j = j4 + u;
+        if (j > k && li >= j) a[j] = fmaf(-lik, cj[u], a[j]);
+      }
     }
   }
-  // L to the packed triangle and to the dense tile tt (tt[k*17 + i] =
-  // L(i, k)), which the inverse reads without packed-index arithmetic
+  // L to the packed triangle (tt holds it densely for the inverse)
   if (lane < SB) {
 #pragma unroll
     for (int k = 0; k < SB; ++k)
-      if (k <= li) {
-        Lp[pidx(q + li, q + k)] = a[k];
-        tt[k * (SB + 1) + li] = a[k];
-      }
+      if (k <= li) Lp[pidx(q + li, q + k)] = a[k];
   }
   __syncwarp();
   if (lane == 0 && bad) atomicOr(status, ST_NOT_POSDEF);
@@ -121,7 +126,7 @@ __device__ __noinline__ void warp_chol16(float* __restrict__ Lp, int q, int bwre
   for (int i = 0; i < SB; ++i) {
     float v = (i == li) ? 1.f : 0.f;
 #pragma unroll
-    for (int k = 0; k < i; ++k) v = fmaf(-tt[k * (SB + 1) + i], x[k], v);
+    for (int k = 0; k < i; ++k) v = fmaf(-tt[k * SB + i], x[k], v);
     x[i] = v * rinv[i];
   }
   if (lane < SB) {
@@ -142,7 +147,7 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
   float* Xs = sm;                      // inverse of the current sub-block, Xs[k*16 + j] = X(j, k)
   float* Bk = Xs + SB * SB;            // Bk[m*16 + i] = L(c1 + i, q0 + m), the next sub-block's rows
   float* Tt = Bk + SB * SB;            // dense copy of the factorised sub-block (warp 0)
-  float* Lp = Tt + SB * (SB + 1);      // packed lower triangle, PW rows
+  float* Lp = Tt + SB * SB;            // packed lower triangle, PW rows
   const BlkTask t = tasks[blockIdx.x];
   float* a = arena + t.off;
   const int64_t ld = t.ld;
@@ -389,7 +394,7 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
 }
 
 constexpr size_t diag_smem() {
-  return sizeof(float) * ((size_t)PW * (PW + 1) / 2 + 2 * SB * SB + SB * (SB + 1));
+  return sizeof(float) * ((size_t)PW * (PW + 1) / 2 + 3 * SB * SB);
 }
 constexpr size_t panel_smem(int pitch) {
   return sizeof(float) * ((size_t)pitch * ALD + lw_off(pitch / SB) + (size_t)pitch * SB);
