@@ -28,6 +28,17 @@ constexpr size_t SMALL_SOLVE_SMEM = 160 * 1024;
 
 template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
 
+// Programmatic dependent launch of the large-front solve steps: a step lets
+// the next one launch at once (its CTAs then stage the factor data they
+// need, which no step writes), and waits for the previous step's grid to
+// finish before it reads right-hand-side data.  Every CTA passes the wait
+// before its first dependent access, so a grid completes only after its
+// predecessor did.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
                                                    const FrontDesc* __restrict__ fr,
@@ -859,6 +870,7 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
   const ACC* tcbb = a.tcb + (a.inv2_off[t.f] / ((int64_t)BW2 * BW2) + c0 / BW2) * BW2 * MAXR;
   // entries k of v (and columns of the matrix slice) this CTA needs
   const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + DR), nk = khi - klo;
+  pdl_trigger();
   if (i0 < bw) {
     // the CTA's slice of the inverse, one wave of asynchronous copies
     for (int e = tid; e < nk * DR; e += 256) {
@@ -866,6 +878,7 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
       cp_async(&Ms[e], &M[(int64_t)k * BW2 + i0 + rr]);
     }
   }
+  pdl_wait();
   // rows beyond the block: nothing to compute (uniform per CTA)
   for (int rg = 0; rg < (i0 < bw ? a.nrhs : 0); rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
@@ -955,6 +968,7 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   const int nrow = min(32, f.m - t.r0);
   const int cfirst = t.c0, clast = t.c0 + t.bw;
+  pdl_trigger();
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     ACC acc[RG];
@@ -968,6 +982,7 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
         if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
         else Lt[e] = T(0);
       }
+      pdl_wait();
       {
         constexpr int NL = BW2 * RG / 512;
         ACC v[NL];
@@ -1049,12 +1064,14 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
   // fully-summed rows [r0, n) only; the contribution rows' share comes from
   // k_bwd_cb
   const int nrow = min(BR, f.n - t.r0);
+  pdl_trigger();
   for (int e = tid; e < BR * BW2; e += 512) {
     const int ii = e % BR, kk = e / BR;
     T* dst = &Lt[ii * (BW2 + 1) + kk];
     if (ii < nrow && kk < bw) cp_async(dst, &L[(int64_t)(c0 + kk) * f.ld + t.r0 + ii]);
     else *dst = T(0);
   }
+  pdl_wait();
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     ACC acc[RG];
@@ -1300,6 +1317,24 @@ void launch_axpy_inplace(double* x, int ldx, const double* d, int n, int nrhs, c
   k_axpy<<<nblocks(c, 256), 256, 0, s>>>(x, ldx, d, n, nrhs);
 }
 
+// Launch with programmatic stream serialization (the kernel calls
+// pdl_wait before reading what earlier launches wrote).
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  SG_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+}
+
 template <typename T, typename ACC>
 void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cudaStream_t s) {
   if (ntask <= 0) return;
@@ -1314,10 +1349,11 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
       k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
     case LS_FWD_DIAG2:
-      k_diag_mv<T, ACC, false><<<dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s>>>(tasks, a);
+      launch_pdl(k_diag_mv<T, ACC, false>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s,
+                 tasks, a);
       break;
     case LS_FWD_UPD2:
-      k_fwd_upd3<T, ACC><<<ntask, 512, fwd_upd_smem<T>(), s>>>(tasks, a);
+      launch_pdl(k_fwd_upd3<T, ACC>, dim3(ntask), 512, fwd_upd_smem<T>(), s, tasks, a);
       break;
     case LS_BWD_CB:
       k_bwd_cb<T, ACC><<<ntask, 512, bwd_cb_smem<T>(), s>>>(tasks, a);
@@ -1326,10 +1362,11 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
       k_fwd_rows<T, ACC><<<ntask, LSOLVE_ROWS_T, 0, s>>>(tasks, a);
       break;
     case LS_BWD_RED2:
-      k_bwd_red3<T, ACC><<<ntask, 512, bwd_red_smem<T>(), s>>>(tasks, a);
+      launch_pdl(k_bwd_red3<T, ACC>, dim3(ntask), 512, bwd_red_smem<T>(), s, tasks, a);
       break;
     case LS_BWD_DIAG2:
-      k_diag_mv<T, ACC, true><<<dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s>>>(tasks, a);
+      launch_pdl(k_diag_mv<T, ACC, true>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s,
+                 tasks, a);
       break;
   }
 }
