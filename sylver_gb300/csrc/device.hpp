@@ -110,10 +110,14 @@ constexpr int TC_KCHUNK = 64;
 // pend, where the kernel writes the rows it solves (transposed, split into
 // three BF16 planes) for the later tensor-core updates, at K columns
 // [c mod pitch, + panel width) of planes with pitch K columns; base < 0: no
-// later update reads the panel.
+// later update reads the panel.  cbbase >= 0: the front's contribution
+// rows (>= n) are also written, at K columns [c, c + panel width) clipped to
+// n rounded up to 64, to the contribution-block operand planes (pitch
+// cbpitch), stacked row cbbase for front row n.
 struct BlkTask {
   int64_t off;
   int ld, m, c, bw, pend, r0, xi, base;
+  int n, cbbase, cbpitch;
 };
 
 #if defined(__CUDACC__)
@@ -175,9 +179,11 @@ void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStr
 void prepare_blocked_kernels();
 void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, unsigned* status,
                      cudaStream_t s);
-// pw: the panel width (shared-memory layout), pitch: K columns of the planes.
+// pw: the panel width (shared-memory layout), pitch: K columns of the planes;
+// cbplanes / cbpstride: the contribution-block operand planes.
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      uint16_t* planes, int64_t pstride, int pw, int pitch, cudaStream_t s);
+                      uint16_t* planes, int64_t pstride, int pw, int pitch, uint16_t* cbplanes,
+                      int64_t cbpstride, cudaStream_t s);
 
 template <typename T> struct Tiles;
 template <> struct Tiles<double> {

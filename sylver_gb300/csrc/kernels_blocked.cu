@@ -287,7 +287,9 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
                                                         const BlkTask* __restrict__ tasks,
                                                         const float* __restrict__ xinv,
                                                         uint16_t* __restrict__ planes,
-                                                        int64_t pstride, int pw, int pitch) {
+                                                        int64_t pstride, int pw, int pitch,
+                                                        uint16_t* __restrict__ cbplanes,
+                                                        int64_t cbpstride) {
   extern __shared__ __align__(16) float sm[];
   float* Ar = sm;                          // Ar[k*ALD + r] = A(r0 + r, k0 + k), then L
   float* Lw = Ar + pw * ALD;               // block rows of L_WW (lw_off layout)
@@ -375,10 +377,26 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
     }
     __syncwarp();
   }
+  if (t.base >= 0 || t.cbbase >= 0) __syncthreads();
+  if (t.cbbase >= 0) {
+    // contribution rows: their K columns of the contribution-block update's
+    // operand planes (zeros past the panel up to n rounded to 64)
+    const int rf = max(0, t.n - r0);
+    const int kend = min(pw, (t.n + TC_KCHUNK - 1) / TC_KCHUNK * TC_KCHUNK - k0);
+    if (kend > 0)
+      for (int e = tid; e < (nr - rf) * kend; e += PTHREADS) {
+        const int rr = rf + e / kend, k = e % kend;
+        uint16_t b0, b1, b2;
+        bf16x3_split(k < w ? Ar[k * ALD + rr] : 0.f, b0, b1, b2);
+        const int64_t o = ((int64_t)t.cbbase + (r0 + rr - t.n)) * t.cbpitch + k0 + k;
+        cbplanes[o] = b0;
+        cbplanes[cbpstride + o] = b1;
+        cbplanes[2 * cbpstride + o] = b2;
+      }
+  }
   if (t.base >= 0) {
     // the rows just solved, transposed and split into three BF16 planes, for
     // the trailing tensor-core update (k contiguous: coalesced writes)
-    __syncthreads();
     const int64_t row0 = (int64_t)t.base + (r0 - t.pend);
     const int koff = k0 % pitch;
     for (int e = tid; e < nr * pw; e += PTHREADS) {
@@ -416,10 +434,11 @@ void launch_blk_diag(float* arena, const BlkTask* t, int ntask, float* xinv, uns
 }
 
 void launch_blk_panel(float* arena, const BlkTask* t, int ntask, const float* xinv,
-                      uint16_t* planes, int64_t pstride, int pw, int pitch, cudaStream_t s) {
+                      uint16_t* planes, int64_t pstride, int pw, int pitch, uint16_t* cbplanes,
+                      int64_t cbpstride, cudaStream_t s) {
   if (ntask <= 0) return;
   k_blk_panel<<<ntask, PTHREADS, panel_smem(pw), s>>>(arena, t, xinv, planes, pstride, pw,
-                                                       pitch);
+                                                       pitch, cbplanes, cbpstride);
 }
 
 }  // namespace sylver_gb300

@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
 // (ys[r*m + i], r < nrhs) and their destinations stay on chip from the gather
 // to the scatter, so the column blocks touch global memory only for L.
 template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_solve_fwd_s(const T* __restrict__ arena,
+__global__ void __launch_bounds__(256, sizeof(ACC) == 4 ? 3 : 2) k_solve_fwd_s(const T* __restrict__ arena,
                                                      const FrontDesc* __restrict__ fr,
                                                      const int* __restrict__ rlist,
                                                      ACC* __restrict__ x, int n, int nrhs,

@@ -275,6 +275,24 @@ void FKeep::plan_cholesky() {
       }
     }
     if ((int64_t)smalls.size() > s0) ops.push_back({Op::SMALL, s0, (int64_t)smalls.size(), maxm});
+    // contribution blocks updated on the tensor cores (FP32, 3xBF16, blocks
+    // of at least TC_ROWS rows): their rows are stacked in the operand
+    // planes (pitch: n rounded up to 64, the most of the level), row cbb[s]
+    // for front row n; the blocked path's panel kernel writes them
+    std::vector<int> tcf;
+    std::vector<int> cbb(ns, -1);
+    int cb_pitch = 0;
+    int64_t cb_rows = 0, cb_mx = 0;
+    for (int s : large) {
+      const int m = st.nrow[s], n = st.ncol[s];
+      if (m > n && f32 && use_tc && TC_ROWS > 0 && m - n >= TC_ROWS) {
+        tcf.push_back(s);
+        cbb[s] = (int)cb_rows;
+        cb_rows += m - n;
+        cb_mx = std::max<int64_t>(cb_mx, m - n);
+        cb_pitch = std::max(cb_pitch, (n + TC_KCHUNK - 1) / TC_KCHUNK * TC_KCHUNK);
+      }
+    }
     // large fronts: panel steps over the fully-summed columns, batched
     int maxsteps = 0;
     if (PW > 0) {
@@ -342,9 +360,10 @@ void FKeep::plan_cholesky() {
             // stacked row of row pend: only when a later update of this
             // group reads the panel (columns remain past it)
             const int pb = (pend < n) ? base[s] + (pend - q) : -1;
-            blkd.push_back({off[s], ld[s], m, k0, pend - k0, pend, 0, xi, -1});
+            blkd.push_back({off[s], ld[s], m, k0, pend - k0, pend, 0, xi, -1, n, -1, 0});
             for (int r0 = pend; r0 < m; r0 += 64)
-              blkp.push_back({off[s], ld[s], m, k0, pend - k0, pend, r0, xi, pb});
+              blkp.push_back({off[s], ld[s], m, k0, pend - k0, pend, r0, xi, pb, n,
+                              r0 + 64 > n ? cbb[s] : -1, cb_pitch});
           }
           if ((int64_t)blkd.size() > d0) {
             ops.push_back({Op::BDIAG, d0, (int64_t)blkd.size(), 0});
@@ -387,14 +406,9 @@ void FKeep::plan_cholesky() {
     // contribution blocks: one Schur-complement update with K = n, on the
     // tensor cores (FP32, 3xBF16) for blocks of at least 64 rows
     int64_t u0 = (int64_t)upds.size();
-    std::vector<int> tcf;
     for (int s : large) {
       int m = st.nrow[s], n = st.ncol[s];
-      if (m <= n) continue;
-      if (f32 && use_tc && TC_ROWS > 0 && m - n >= TC_ROWS) {
-        tcf.push_back(s);
-        continue;
-      }
+      if (m <= n || cbb[s] >= 0) continue;
       for (int cj = 0; n + cj * TM < m; ++cj)
         for (int ri = cj; n + ri * TM < m; ++ri)
           upds.push_back({off[s], off[s], off[s], ld[s], ld[s], ld[s], n + ri * TM,
@@ -402,30 +416,29 @@ void FKeep::plan_cholesky() {
     }
     if ((int64_t)upds.size() > u0) ops.push_back({Op::UPD, u0, (int64_t)upds.size(), 0});
     if (!tcf.empty()) {
-      int pitch = 0;
-      int64_t rows = 0, mx = 0;
-      for (int s : tcf) pitch = std::max(pitch, (st.ncol[s] + TC_KCHUNK - 1) / TC_KCHUNK * TC_KCHUNK);
+      const int pitch = cb_pitch;
+      int64_t rows = 0, mx = cb_mx;
       int64_t sp0 = (int64_t)tcs.size(), tk0 = (int64_t)tct.size();
       for (int s : tcf) {
         int m = st.nrow[s], n = st.ncol[s];
-        tcs.push_back({off[s], ld[s], m, n, n, (int)rows, 0});
+        // without the blocked path a transposed split copy makes the operands
+        if (PW == 0) tcs.push_back({off[s], ld[s], m, n, n, (int)rows, 0});
         for (int cj = 0; cj * 128 < m - n; ++cj)
           for (int ri = cj; ri * 128 < m - n; ++ri)
             tct.push_back({off[s], ld[s], n + ri * 128, n + cj * 128, m, m,
                            (int)rows + ri * 128, (int)rows + cj * 128,
                            (n + TC_KCHUNK - 1) / TC_KCHUNK});
-        mx = std::max(mx, (int64_t)(m - n));
         rows += m - n;
       }
       int lvl = (int)tclev.size();
-      tclev.push_back({pitch, rows, mx});
+      tclev.push_back({pitch, rows, mx, PW > 0});
       double fl = 0.0;  // lower triangle (diagonal included) x 2K
       for (int s : tcf) {
         double mc = st.nrow[s] - st.ncol[s];
         fl += mc * (mc + 1.0) * st.ncol[s];
       }
       tc_flops.push_back(fl);
-      ops.push_back({Op::SPLIT, sp0, (int64_t)tcs.size(), lvl});
+      if (PW == 0) ops.push_back({Op::SPLIT, sp0, (int64_t)tcs.size(), lvl});
       ops.push_back({Op::TCUPD, tk0, (int64_t)tct.size(), lvl});
     }
   }
@@ -499,17 +512,21 @@ void FKeep::upload_static(cudaStream_t s) {
   tcerr.ensure(sizeof(unsigned));
   if (blkinv_count > 0) blkinv.ensure((size_t)blkinv_count * BLK_B * BLK_B * sizeof(float));
   if (!tclev.empty()) {
-    int64_t cap = 0;
-    for (auto& L : tclev) cap = std::max(cap, L.rows * L.pitch);
+    int64_t cap = 0, cbcap = 0;
+    for (auto& L : tclev) (L.cb ? cbcap : cap) = std::max(L.cb ? cbcap : cap, L.rows * L.pitch);
     // three BF16 planes of cap elements each (plane stride rounded to 64
     // elements keeps every plane 128-byte aligned)
     plane_stride = (std::max<int64_t>(cap, 1) + 63) / 64 * 64;
     tcplanes.ensure((size_t)3 * plane_stride * sizeof(uint16_t));
+    cb_stride = (std::max<int64_t>(cbcap, 1) + 63) / 64 * 64;
+    cbplanes.ensure((size_t)3 * cb_stride * sizeof(uint16_t));
     tmaps.resize(3 * tclev.size());
     for (size_t l = 0; l < tclev.size(); ++l)
-      for (int q = 0; q < 3; ++q)
-        make_panel_map(&tmaps[3 * l + q], tcplanes.as<uint16_t>() + q * plane_stride,
-                       tclev[l].rows, tclev[l].pitch);
+      for (int q = 0; q < 3; ++q) {
+        const uint16_t* pl = tclev[l].cb ? cbplanes.as<uint16_t>() + q * cb_stride
+                                         : tcplanes.as<uint16_t>() + q * plane_stride;
+        make_panel_map(&tmaps[3 * l + q], pl, tclev[l].rows, tclev[l].pitch);
+      }
   }
 }
 
@@ -558,7 +575,8 @@ void FKeep::run_ops(cudaStream_t s) {
       case Op::BPANEL:
         if constexpr (std::is_same<T, float>::value)
           launch_blk_panel(A, blkpanel.as<BlkTask>() + op.a, (int)cnt, blkinv.as<float>(),
-                           tcplanes.as<uint16_t>(), plane_stride, blk_pw, op.aux, s);
+                           tcplanes.as<uint16_t>(), plane_stride, blk_pw, op.aux,
+                           cbplanes.as<uint16_t>(), cb_stride, s);
         break;
       case Op::TCUPD:
         if constexpr (std::is_same<T, float>::value)

@@ -176,11 +176,14 @@ struct FKeep {
   struct TcLevel {
     int pitch;
     int64_t rows, max_rows;  // stacked panel rows; most rows of one split
+    bool cb = false;         // operands in the contribution-block planes
   };
   std::vector<TcLevel> tclev;
   std::vector<CUtensorMap> tmaps;   // three per tensor-core launch (one per BF16 plane)
   DevMem tcsplit, tctask, tcplanes, tcerr;
   int64_t plane_stride = 0;        // elements between the BF16 planes
+  DevMem cbplanes;                 // contribution-block operands written by the panel kernel
+  int64_t cb_stride = 0;
   // blocked large-front path (FP32): diagonal-block and panel tasks, and the
   // 64 x 64 inverses of one diagonal-block launch
   DevMem blkdiag, blkpanel, blkinv;
