@@ -273,6 +273,25 @@ __global__ void __launch_bounds__(DTHREADS) k_blk_diag(float* __restrict__ arena
   }
 }
 
+// K columns k .. k + 3 (k a multiple of 4) of local row rr of the panel
+// kernel's tile, split into the three BF16 planes and stored as 8-byte
+// vectors at element offset o (a multiple of 4) of each plane; columns >= w
+// are zero.
+__device__ __forceinline__ void put_split4(const float* __restrict__ Ar, int rr, int k, int w,
+                                           uint16_t* __restrict__ pl, int64_t ps, int64_t o) {
+  uint32_t lo[3], hi[3];
+  uint16_t b[3][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+    bf16x3_split(k + u < w ? Ar[(k + u) * ALD + rr] : 0.f, b[0][u], b[1][u], b[2][u]);
+#pragma unroll
+  for (int q = 0; q < 3; ++q) {
+    lo[q] = (uint32_t)b[q][0] | ((uint32_t)b[q][1] << 16);
+    hi[q] = (uint32_t)b[q][2] | ((uint32_t)b[q][3] << 16);
+    *reinterpret_cast<uint2*>(pl + q * ps + o) = make_uint2(lo[q], hi[q]);
+  }
+}
+
 // Floats of the staged block rows of L_WW: block row q >= 1 (columns k < 16q
 // of rows 16q .. 16q + 15) starts at lw_off(q), 16 values per k.
 __host__ __device__ constexpr int lw_off(int q) { return 128 * q * (q - 1); }
@@ -383,15 +402,12 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
     // operand planes (zeros past the panel up to n rounded to 64)
     const int rf = max(0, t.n - r0);
     const int kend = min(pw, (t.n + TC_KCHUNK - 1) / TC_KCHUNK * TC_KCHUNK - k0);
+    const int k4 = kend / 4;
     if (kend > 0)
-      for (int e = tid; e < (nr - rf) * kend; e += PTHREADS) {
-        const int rr = rf + e / kend, k = e % kend;
-        uint16_t b0, b1, b2;
-        bf16x3_split(k < w ? Ar[k * ALD + rr] : 0.f, b0, b1, b2);
-        const int64_t o = ((int64_t)t.cbbase + (r0 + rr - t.n)) * t.cbpitch + k0 + k;
-        cbplanes[o] = b0;
-        cbplanes[cbpstride + o] = b1;
-        cbplanes[2 * cbpstride + o] = b2;
+      for (int e = tid; e < (nr - rf) * k4; e += PTHREADS) {
+        const int rr = rf + e / k4, k = 4 * (e % k4);
+        put_split4(Ar, rr, k, w, cbplanes, cbpstride,
+                   ((int64_t)t.cbbase + (r0 + rr - t.n)) * t.cbpitch + k0 + k);
       }
   }
   if (t.base >= 0) {
@@ -399,14 +415,10 @@ __global__ void __launch_bounds__(PTHREADS) k_blk_panel(float* __restrict__ aren
     // the trailing tensor-core update (k contiguous: coalesced writes)
     const int64_t row0 = (int64_t)t.base + (r0 - t.pend);
     const int koff = k0 % pitch;
-    for (int e = tid; e < nr * pw; e += PTHREADS) {
-      const int rr = e / pw, k = e % pw;
-      uint16_t b0, b1, b2;
-      bf16x3_split(k < w ? Ar[k * ALD + rr] : 0.f, b0, b1, b2);
-      const int64_t o = (row0 + rr) * pitch + koff + k;
-      planes[o] = b0;
-      planes[pstride + o] = b1;
-      planes[2 * pstride + o] = b2;
+    const int k4 = pw / 4;
+    for (int e = tid; e < nr * k4; e += PTHREADS) {
+      const int rr = e / k4, k = 4 * (e % k4);
+      put_split4(Ar, rr, k, w, planes, pstride, (row0 + rr) * pitch + koff + k);
     }
   }
 }
