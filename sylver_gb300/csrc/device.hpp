@@ -51,7 +51,34 @@ __device__ __forceinline__ void cp_async(T* smem, const T* gmem) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
+// Programmatic dependent launch (kernels launched with launch_pdl): the
+// trigger lets the next launch of the stream start at once; the wait blocks
+// until the previous grid has completed and its writes are visible.  Every
+// kernel launched with launch_pdl waits in each CTA before its first read of
+// data an earlier launch wrote, so a grid completes only after its
+// predecessor did.
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 #endif
+
+// Launch with programmatic stream serialization (see pdl_wait).
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  SG_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
+}
 
 // ---------------------------------------------------------------------------
 // Task descriptors (one per CTA unless stated).

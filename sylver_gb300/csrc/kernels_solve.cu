@@ -28,16 +28,10 @@ constexpr size_t SMALL_SOLVE_SMEM = 160 * 1024;
 
 template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
 
-// Programmatic dependent launch of the large-front solve steps: a step lets
-// the next one launch at once (its CTAs then stage the factor data they
-// need, which no step writes), and waits for the previous step's grid to
-// finish before it reads right-hand-side data.  Every CTA passes the wait
-// before its first dependent access, so a grid completes only after its
-// predecessor did.
-__device__ __forceinline__ void pdl_trigger() {
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// The large-front solve steps use programmatic dependent launch
+// (pdl_trigger / pdl_wait): a step lets the next one launch at once, and
+// its CTAs stage the factor data they need (which no step writes) before
+// they wait for the previous step's grid.
 
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
@@ -1315,24 +1309,6 @@ void launch_axpy_inplace(double* x, int ldx, const double* d, int n, int nrhs, c
   int64_t c = (int64_t)n * nrhs;
   if (c == 0) return;
   k_axpy<<<nblocks(c, 256), 256, 0, s>>>(x, ldx, d, n, nrhs);
-}
-
-// Launch with programmatic stream serialization (the kernel calls
-// pdl_wait before reading what earlier launches wrote).
-template <typename... KArgs, typename... Args>
-void launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
-                Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  SG_CUDA(cudaLaunchKernelEx(&cfg, kern, args...));
 }
 
 template <typename T, typename ACC>
