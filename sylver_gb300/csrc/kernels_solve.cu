@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
 // step is one parallel mat-vec on the diagonal block plus one update (forward)
 // or reduction (backward) of the rows below, spread over many small CTAs.
 constexpr int BW2 = LSOLVE_BW2;
-constexpr int DMV_ROWS = 16;  // rows of the diagonal mat-vec per CTA (16 CTAs per block)
+constexpr int DMV_ROWS = 8;   // rows of the diagonal mat-vec per CTA (32 CTAs per block)
 constexpr int BRED_ROWS = LSOLVE_RED_ROWS;  // rows per backward-reduction CTA
 constexpr int CB_CHUNK = LSOLVE_CB_ROWS;    // contribution rows per backward CB CTA
 template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
