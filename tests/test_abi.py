@@ -59,3 +59,16 @@ def test_call_sequence_errors(sylver):
     lib.spldlt_factorize(True, None, None, x.ctypes.data_as(ctypes.c_void_p), None, None,
                          ctypes.byref(fk), ctypes.byref(o), ctypes.byref(inf))
     assert inf.flag == -1
+
+
+def test_schedule_round_trip(sylver):
+    """Every field of sylver_gb300_schedule_t reaches the library and comes
+    back; no arguments restore the defaults (zeros)."""
+    vals = dict(small_front_rows=96, tc_min_cb_rows=128, solve_large_cols=64, ldlt_tpp_cols=8,
+                fs_panel_cols=128, fs_panel_group=3)
+    try:
+        sylver.set_schedule(**vals)
+        assert sylver.get_schedule() == vals
+    finally:
+        sylver.set_schedule()
+    assert all(v == 0 for v in sylver.get_schedule().values())
