@@ -82,8 +82,12 @@ enum {
   SYLVER_ERROR_VAL = -9,
   SYLVER_ERROR_X_SIZE = -10,
   SYLVER_ERROR_JOB_OOR = -11,
+  SYLVER_ERROR_NOT_LLT = -13,
+  SYLVER_ERROR_NOT_LDLT = -14,
+  SYLVER_ERROR_NO_SAVED_SCALING = -15,
   SYLVER_ERROR_ALLOCATION = -50,
   SYLVER_ERROR_CUDA_UNKNOWN = -51,
+  SYLVER_ERROR_CUBLAS_UNKNOWN = -52,
   SYLVER_ERROR_UNIMPLEMENTED = -98,
   SYLVER_ERROR_UNKNOWN = -99,
   SYLVER_WARNING_IDX_OOR = 1,
@@ -91,7 +95,14 @@ enum {
   SYLVER_WARNING_DUP_AND_OOR = 3,
   SYLVER_WARNING_MISSING_DIAGONAL = 4,
   SYLVER_WARNING_MISS_DIAG_OORDUP = 5,
-  SYLVER_WARNING_FACT_SINGULAR = 7
+  SYLVER_WARNING_ANAL_SINGULAR = 6,
+  SYLVER_WARNING_FACT_SINGULAR = 7,
+  SYLVER_WARNING_MATCH_ORD_NO_SCALE = 8,
+  /* No reference counterpart: iterative refinement (FP32 factors, or FP64
+   * with ir_max_iter > 0) stopped at ir_max_iter corrections with the scaled
+   * backward error still above ir_tol; x holds the last iterate and
+   * sylver_gb300_solve_stats the error reached. */
+  SYLVER_GB300_WARNING_IR_NOT_CONVERGED = 9
 };
 
 /* Solve job values: src/sylver_datatypes_mod.F90:46-51. */
@@ -118,7 +129,13 @@ void sylver_default_options(sylver_options_t* options);
 void spldlt_analyse(int n, int* order, long const* ptr, int const* row, double const* val,
                     void** akeep, bool check, sylver_options_t const* options,
                     sylver_inform_t* inform);
-/* Replaces spldlt_c_factorize (sylver_ciface.F90:530-631), FP64 factors. */
+/* Replaces spldlt_c_factorize (sylver_ciface.F90:530-631), FP64 factors.
+ * With options->scaling <= 0 and a non-null `scale` (length n, user order)
+ * the factorization is of S A S, S = diag(scale)
+ * (src/spldlt_factorize_mod.F90:727-733); spldlt_solve then applies S on the
+ * way in for jobs 0 and 1 and on the way out for jobs 0, 3 and 4, as the
+ * reference's solve does (src/spldlt_factorize_mod.F90:945-1050), so that job
+ * 0 solves A x = b.  Refinement (FP32 factors) uses the residual of A. */
 void spldlt_factorize(bool posdef, long const* ptr, int const* row, double const* val,
                       double* scale, void* akeep, void** fkeep,
                       sylver_options_t const* options, sylver_inform_t* inform);
@@ -169,15 +186,22 @@ void* spldlt_create_symbolic_tree(void* akeep, int n, int nnodes, int const* spt
 void spldlt_destroy_symbolic_tree(void* symbolic_tree);
 
 /* Replace spldlt_create_numeric_tree_dbl (src/NumericTree.cxx:27-45) and
- * spldlt_create_numeric_tree_posdef_dbl (src/NumericTreePosdef.cxx:19-35).
- * aval is host memory (values in the order nlist refers to). */
+ * spldlt_create_numeric_tree_posdef_dbl (src/NumericTreePosdef.cxx:19-35),
+ * same argument order as the Fortran bind(C) interfaces
+ * (src/spldlt_factorize_mod.F90:72-83).  aval is host memory (values in the
+ * order nlist refers to).  scaling (null: none) is indexed by the tree's
+ * variables (the rlist values, 1-based there): entry (r, c) of a front is
+ * initialised to scaling[r] * a * scaling[c] as init_a_block does
+ * (src/kernels/assemble.hxx:162-180).  The tree solves then work on the
+ * scaled system; applying the scaling to x around them is the caller's job,
+ * as in the reference's Fortran solve (src/spldlt_factorize_mod.F90:945-1050). */
 void* spldlt_create_numeric_tree_dbl(bool posdef, void* fkeep, void* symbolic_tree,
                                      double* aval, const double* scaling,
                                      void** child_contrib, sylver_options_c* options,
                                      sylver_inform_c* inform);
 void* spldlt_create_numeric_tree_posdef_dbl(void* fkeep, void* symbolic_tree, double* aval,
-                                            void** child_contrib, sylver_options_c* options,
-                                            sylver_inform_c* inform);
+                                            const double* scaling, void** child_contrib,
+                                            sylver_options_c* options, sylver_inform_c* inform);
 void spldlt_destroy_numeric_tree_dbl(bool posdef, void* tree);
 void spldlt_destroy_numeric_tree_posdef_dbl(void* tree);
 

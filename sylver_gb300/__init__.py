@@ -27,8 +27,12 @@ FLAGS = {
     -11: "ERROR_JOB_OOR", -50: "ERROR_ALLOCATION", -51: "ERROR_CUDA_UNKNOWN",
     -98: "ERROR_UNIMPLEMENTED", -99: "ERROR_UNKNOWN", 1: "WARNING_IDX_OOR",
     2: "WARNING_DUP_IDX", 3: "WARNING_DUP_AND_OOR", 4: "WARNING_MISSING_DIAGONAL",
-    5: "WARNING_MISS_DIAG_OORDUP", 7: "WARNING_FACT_SINGULAR",
+    5: "WARNING_MISS_DIAG_OORDUP", 6: "WARNING_ANAL_SINGULAR", 7: "WARNING_FACT_SINGULAR",
+    8: "WARNING_MATCH_ORD_NO_SCALE", 9: "GB300_WARNING_IR_NOT_CONVERGED",
+    -13: "ERROR_NOT_LLT", -14: "ERROR_NOT_LDLT", -15: "ERROR_NO_SAVED_SCALING",
+    -52: "ERROR_CUBLAS_UNKNOWN",
 }
+WARNING_IR_NOT_CONVERGED = 9
 
 
 class Inform(ctypes.Structure):
@@ -60,6 +64,26 @@ class Options(ctypes.Structure):
                 ("action", ctypes.c_bool), ("use_gpu", ctypes.c_bool),
                 ("gpu_perf_coeff", ctypes.c_double), ("failed_pivot_method", ctypes.c_int),
                 ("scheduler", ctypes.c_int)]
+
+
+class OptionsC(ctypes.Structure):
+    """sylver_options_c, the seam's options_c (src/sylver_ciface.hxx:39-51)."""
+    _fields_ = [("print_level", ctypes.c_int), ("action", ctypes.c_bool),
+                ("small", ctypes.c_double), ("u", ctypes.c_double),
+                ("multiplier", ctypes.c_double), ("small_subtree_threshold", ctypes.c_long),
+                ("nb", ctypes.c_int), ("pivot_method", ctypes.c_int),
+                ("failed_pivot_method", ctypes.c_int), ("cpu_topology", ctypes.c_int)]
+
+
+class InformC(ctypes.Structure):
+    """sylver_inform_c, the seam's inform_c (src/sylver_ciface.hxx:74-87)."""
+    _fields_ = [("flag", ctypes.c_int), ("num_delay", ctypes.c_int),
+                ("num_neg", ctypes.c_int), ("num_two", ctypes.c_int),
+                ("num_zero", ctypes.c_int), ("maxfront", ctypes.c_int),
+                ("not_first_pass", ctypes.c_int), ("not_second_pass", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Schedule(ctypes.Structure):
@@ -162,8 +186,14 @@ def load(path: str | None = None):
         "sylver_gb300_mlp_train": (I, [P, P, P, I, I, ctypes.c_float, P]),
         "spldlt_create_symbolic_tree": (P, [P, I, I, P, P, P, P, P, P, I, P, P, P, P]),
         "spldlt_destroy_symbolic_tree": (None, [P]),
-        "spldlt_create_numeric_tree_dbl": (P, [B, P, P, P, P, P, P, P]),
+        "spldlt_create_numeric_tree_dbl": (P, [B, P, P, P, P, P, ctypes.POINTER(OptionsC),
+                                               ctypes.POINTER(InformC)]),
+        "spldlt_create_numeric_tree_posdef_dbl": (P, [P, P, P, P, P, ctypes.POINTER(OptionsC),
+                                                      ctypes.POINTER(InformC)]),
         "spldlt_destroy_numeric_tree_dbl": (None, [B, P]),
+        "spldlt_destroy_numeric_tree_posdef_dbl": (None, [P]),
+        "spldlt_tree_solve_fwd_posdef_dbl": (I, [P, I, P, I]),
+        "spldlt_tree_solve_bwd_posdef_dbl": (I, [P, I, P, I]),
         "spldlt_tree_solve_fwd_dbl": (I, [B, P, I, P, I]),
         "spldlt_tree_solve_bwd_dbl": (I, [B, P, I, P, I]),
         "spldlt_tree_solve_diag_dbl": (I, [B, P, I, P, I]),
@@ -323,3 +353,64 @@ class Factor:
     def __del__(self):
         if getattr(self, "fkeep", None) and _lib is not None and self.fkeep:
             _lib.spldlt_free_fkeep(ctypes.byref(self.fkeep))
+
+
+class SeamTree:
+    """The reference's internal C++ seam, driven as the Fortran factor_core
+    and solve drive it (src/spldlt_factorize_mod.F90:542-550, :901-1060):
+    spldlt_create_symbolic_tree from SPRAL-layout arrays (1-based, pivot
+    order), spldlt_create_numeric_tree[_posdef]_dbl with an optional scaling
+    vector indexed by the tree's variables, and spldlt_tree_solve_*_dbl on x in
+    pivot order."""
+
+    def __init__(self, sym, posdef, aval, scaling=None, u=0.01, small=1e-20, action=True):
+        lib = load()
+        self.posdef = bool(posdef)
+        self._arr = {k: np.ascontiguousarray(sym[k]) for k in
+                     ("sptr", "sparent", "rptr", "rlist", "nptr", "nlist")}
+        a = self._arr
+        self.n, nn = int(sym["n"]), int(sym["nnodes"])
+        self.st = lib.spldlt_create_symbolic_tree(
+            None, self.n, nn, _p(a["sptr"].astype(np.int32)), _p(a["sparent"].astype(np.int32)),
+            _p(a["rptr"].astype(np.int64)), _p(a["rlist"].astype(np.int32)),
+            _p(a["nptr"].astype(np.int64)), _p(a["nlist"].astype(np.int64)), 0, None, None,
+            None, None)
+        self._aval = np.ascontiguousarray(aval, dtype=np.float64)
+        self._scaling = None if scaling is None else np.ascontiguousarray(scaling, np.float64)
+        o = OptionsC(print_level=0, action=bool(action), small=float(small), u=float(u),
+                     multiplier=1.1, small_subtree_threshold=4000000, nb=256, pivot_method=2,
+                     failed_pivot_method=1, cpu_topology=1)
+        self.inform = InformC()
+        sc = _p(self._scaling) if self._scaling is not None else None
+        if self.posdef:
+            self.tree = lib.spldlt_create_numeric_tree_posdef_dbl(
+                None, self.st, _p(self._aval), sc, None, ctypes.byref(o),
+                ctypes.byref(self.inform))
+        else:
+            self.tree = lib.spldlt_create_numeric_tree_dbl(
+                False, None, self.st, _p(self._aval), sc, None, ctypes.byref(o),
+                ctypes.byref(self.inform))
+
+    def solve(self, job, x):
+        """Tree solve `job` ("fwd", "diag", "bwd", "diag_bwd") in place on x
+        (n x nrhs, pivot order); returns the reference flag."""
+        lib = load()
+        assert x.flags.f_contiguous and x.dtype == np.float64
+        nrhs = x.shape[1] if x.ndim == 2 else 1
+        if self.posdef and job in ("fwd", "bwd"):
+            fn = getattr(lib, f"spldlt_tree_solve_{job}_posdef_dbl")
+            return fn(self.tree, nrhs, _p(x), x.shape[0])
+        fn = getattr(lib, f"spldlt_tree_solve_{job}_dbl")
+        return fn(self.posdef, self.tree, nrhs, _p(x), x.shape[0])
+
+    def close(self):
+        lib = load()
+        if getattr(self, "tree", None):
+            if self.posdef:
+                lib.spldlt_destroy_numeric_tree_posdef_dbl(self.tree)
+            else:
+                lib.spldlt_destroy_numeric_tree_dbl(False, self.tree)
+            self.tree = None
+        if getattr(self, "st", None):
+            lib.spldlt_destroy_symbolic_tree(self.st)
+            self.st = None

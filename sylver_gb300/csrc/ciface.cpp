@@ -97,25 +97,12 @@ void factorize_common(bool posdef, const double* val_host, const double* val_dev
     }
     const int64_t nz = ak->nnz_val();
     const double* vdev = val_dev;
+    // user scaling S A S (src/spldlt_factorize_mod.F90:727-733), applied on
+    // the device after the unscaled values are kept for the residual
+    fk->set_scale((scale && (!opt || opt->scaling <= 0)) ? scale : nullptr, rt.stream);
     if (val_host) {
-      std::vector<double> scaled;
-      const double* v = val_host;
-      if (scale && opt && opt->scaling <= 0) {
-        // user scaling S A S (src/spldlt_factorize_mod.F90:727-733)
-        scaled.assign(val_host, val_host + nz);
-        for (int c = 0; c < ak->n; ++c)
-          for (int64_t k = ak->clean.cptr[c]; k < ak->clean.cptr[c + 1]; ++k) {
-            int r = ak->clean.crow[k];
-            for (int64_t q = ak->clean.srcptr[k]; q < ak->clean.srcptr[k + 1]; ++q)
-              scaled[ak->clean.src[q]] *= scale[r] * scale[c];
-          }
-        v = scaled.data();
-        fk->scale.assign(scale, scale + ak->n);
-      } else {
-        fk->scale.clear();
-      }
       fk->val.ensure(std::max<int64_t>(nz, 1) * sizeof(double));
-      if (nz) SG_CUDA(cudaMemcpyAsync(fk->val.p, v, nz * sizeof(double),
+      if (nz) SG_CUDA(cudaMemcpyAsync(fk->val.p, val_host, nz * sizeof(double),
                                       cudaMemcpyHostToDevice, rt.stream));
       vdev = fk->val.as<double>();
     }
@@ -177,6 +164,7 @@ void solve_common(int job, int nrhs, double* x, bool x_on_device, int ldx, void*
     }
     SG_CUDA(cudaStreamSynchronize(rt.stream));
     if (rc < 0) inform->flag = rc;
+    else if (rc > 0) inform->flag = std::max(inform->flag, rc);
   } catch (const std::bad_alloc&) {
     inform->flag = SYLVER_ERROR_ALLOCATION;
   } catch (const CudaError& e) {
@@ -303,20 +291,7 @@ void spldlt_factorize_device(bool posdef, double const* val_dev, void* akeep, vo
 
 void spldlt_solve(int job, int nrhs, double* x, int ldx, void* akeep, void* fkeep,
                   sylver_options_t const* options, sylver_inform_t* inform) {
-  FKeep* fk = static_cast<FKeep*>(fkeep);
-  if (fk && !fk->scale.empty() && job == 0) {
-    // scaled system (S A S) y = S b, x = S y
-    AKeep* ak = static_cast<AKeep*>(akeep);
-    int n = ak ? ak->n : 0;
-    if (ak && ldx >= n && nrhs >= 1)
-      for (int r = 0; r < nrhs; ++r)
-        for (int i = 0; i < n; ++i) x[(size_t)r * ldx + i] *= fk->scale[i];
-    solve_common(job, nrhs, x, false, ldx, akeep, fkeep, options, inform);
-    if (ak && ldx >= n && nrhs >= 1)
-      for (int r = 0; r < nrhs; ++r)
-        for (int i = 0; i < n; ++i) x[(size_t)r * ldx + i] *= fk->scale[i];
-    return;
-  }
+  // a scaling given at factorize time is applied by the device solve
   solve_common(job, nrhs, x, false, ldx, akeep, fkeep, options, inform);
 }
 
@@ -467,7 +442,6 @@ void* spldlt_create_numeric_tree_dbl(bool posdef, void* fkeep, void* symbolic_tr
                                      sylver_options_c* options, sylver_inform_c* inform) {
   (void)fkeep;
   (void)child_contrib;
-  (void)scaling;
   sylver_options_t o;
   sylver_default_options(&o);
   if (options) {
@@ -485,8 +459,10 @@ void* spldlt_create_numeric_tree_dbl(bool posdef, void* fkeep, void* symbolic_tr
   ak->clean.src.resize(nz);
   for (int64_t k = 0; k < nz; ++k) ak->clean.src[k] = k;
   ak->clean.srcptr.assign(1, 0);
-  factorize_common(posdef, aval, nullptr, nullptr, ak, &fk, &o, &inf, SYLVER_GB300_FP64, 1e-14,
-                   0);
+  // scaling is indexed by the tree's variables, which are this handle's user
+  // order (identity permutation at this seam)
+  factorize_common(posdef, aval, nullptr, const_cast<double*>(scaling), ak, &fk, &o, &inf,
+                   SYLVER_GB300_FP64, 1e-14, 0);
   if (inform) {
     std::memset(inform, 0, sizeof(*inform));
     inform->flag = inf.flag;
@@ -504,9 +480,9 @@ void* spldlt_create_numeric_tree_dbl(bool posdef, void* fkeep, void* symbolic_tr
 }
 
 void* spldlt_create_numeric_tree_posdef_dbl(void* fkeep, void* symbolic_tree, double* aval,
-                                            void** child_contrib, sylver_options_c* options,
-                                            sylver_inform_c* inform) {
-  return spldlt_create_numeric_tree_dbl(true, fkeep, symbolic_tree, aval, nullptr,
+                                            const double* scaling, void** child_contrib,
+                                            sylver_options_c* options, sylver_inform_c* inform) {
+  return spldlt_create_numeric_tree_dbl(true, fkeep, symbolic_tree, aval, scaling,
                                         child_contrib, options, inform);
 }
 

@@ -305,12 +305,17 @@ template <typename T>
 void launch_inv_diag(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
                      T* inv, const int64_t* inv_off, bool unit, cudaStream_t s);
 
+// xp[perm[i]] = x[i] * scale[i] (scale null: 1), per right-hand side.
 template <typename ACC>
-void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, int n, int nrhs,
-                       cudaStream_t s);
+void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, const double* scale,
+                       int n, int nrhs, cudaStream_t s);
+// x[i] (+)= xp[perm[i]] * scale[i] (scale null: 1), per right-hand side.
 template <typename ACC>
-void launch_permute_out_add(const ACC* xp, const int* perm, double* x, int ldx, int n,
-                            int nrhs, bool add, cudaStream_t s);
+void launch_permute_out_add(const ACC* xp, const int* perm, const double* scale, double* x,
+                            int ldx, int n, int nrhs, bool add, cudaStream_t s);
+// val[k] = (scale[row[k]] * val[k]) * scale[col[k]] for entries with row >= 0.
+void launch_scale_vals(double* val, const int* row, const int* col, const double* scale,
+                       int64_t count, cudaStream_t s);
 
 // r = b - A x for a full CSR matrix (user order), FP64.
 void launch_residual(const int64_t* rowptr, const int* col, const double* aval, int n,

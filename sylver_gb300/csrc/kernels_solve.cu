@@ -439,22 +439,37 @@ __global__ void __launch_bounds__(256) k_solve_bwd_s(const T* __restrict__ arena
 
 template <typename ACC>
 __global__ void k_permute_in(const double* __restrict__ x, int ldx, ACC* __restrict__ xp,
-                             const int* __restrict__ perm, int n, int nrhs) {
+                             const int* __restrict__ perm, const double* __restrict__ scale,
+                             int n, int nrhs) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (int64_t)n * nrhs) return;
   int i = (int)(idx % n), r = (int)(idx / n);
-  xp[(int64_t)r * n + perm[i]] = (ACC)x[(int64_t)r * ldx + i];
+  double v = x[(int64_t)r * ldx + i];
+  if (scale) v *= scale[i];
+  xp[(int64_t)r * n + perm[i]] = (ACC)v;
 }
 
 template <typename ACC>
 __global__ void k_permute_out(const ACC* __restrict__ xp, const int* __restrict__ perm,
-                              double* __restrict__ x, int ldx, int n, int nrhs, bool add) {
+                              const double* __restrict__ scale, double* __restrict__ x, int ldx,
+                              int n, int nrhs, bool add) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (int64_t)n * nrhs) return;
   int i = (int)(idx % n), r = (int)(idx / n);
   double v = (double)xp[(int64_t)r * n + perm[i]];
+  if (scale) v *= scale[i];
   double* d = x + (int64_t)r * ldx + i;
   *d = add ? *d + v : v;
+}
+
+__global__ void k_scale_vals(double* __restrict__ val, const int* __restrict__ row,
+                             const int* __restrict__ col, const double* __restrict__ scale,
+                             int64_t count) {
+  int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const int r = row[k];
+  if (r < 0) return;
+  val[k] = (scale[r] * val[k]) * scale[col[k]];
 }
 
 __global__ void __launch_bounds__(128) k_residual(const int64_t* __restrict__ rowptr,
@@ -1258,19 +1273,25 @@ void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const in
 }
 
 template <typename ACC>
-void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, int n, int nrhs,
-                       cudaStream_t s) {
+void launch_permute_in(const double* x, int ldx, ACC* xp, const int* perm, const double* scale,
+                       int n, int nrhs, cudaStream_t s) {
   int64_t c = (int64_t)n * nrhs;
   if (c == 0) return;
-  k_permute_in<ACC><<<nblocks(c, 256), 256, 0, s>>>(x, ldx, xp, perm, n, nrhs);
+  k_permute_in<ACC><<<nblocks(c, 256), 256, 0, s>>>(x, ldx, xp, perm, scale, n, nrhs);
 }
 
 template <typename ACC>
-void launch_permute_out_add(const ACC* xp, const int* perm, double* x, int ldx, int n,
-                            int nrhs, bool add, cudaStream_t s) {
+void launch_permute_out_add(const ACC* xp, const int* perm, const double* scale, double* x,
+                            int ldx, int n, int nrhs, bool add, cudaStream_t s) {
   int64_t c = (int64_t)n * nrhs;
   if (c == 0) return;
-  k_permute_out<ACC><<<nblocks(c, 256), 256, 0, s>>>(xp, perm, x, ldx, n, nrhs, add);
+  k_permute_out<ACC><<<nblocks(c, 256), 256, 0, s>>>(xp, perm, scale, x, ldx, n, nrhs, add);
+}
+
+void launch_scale_vals(double* val, const int* row, const int* col, const double* scale,
+                       int64_t count, cudaStream_t s) {
+  if (count <= 0) return;
+  k_scale_vals<<<nblocks(count, 256), 256, 0, s>>>(val, row, col, scale, count);
 }
 
 void launch_residual(const int64_t* rowptr, const int* col, const double* aval, int n,
@@ -1417,13 +1438,13 @@ template bool launch_solve_small<float, float>(bool, const float*, const FrontDe
 template bool launch_solve_small<double, double>(bool, const double*, const FrontDesc*, int,
                                                  const int*, double*, int, int, int, bool,
                                                  cudaStream_t);
-template void launch_permute_in<float>(const double*, int, float*, const int*, int, int,
-                                       cudaStream_t);
-template void launch_permute_in<double>(const double*, int, double*, const int*, int, int,
-                                        cudaStream_t);
-template void launch_permute_out_add<float>(const float*, const int*, double*, int, int, int,
-                                            bool, cudaStream_t);
-template void launch_permute_out_add<double>(const double*, const int*, double*, int, int, int,
-                                             bool, cudaStream_t);
+template void launch_permute_in<float>(const double*, int, float*, const int*, const double*,
+                                       int, int, cudaStream_t);
+template void launch_permute_in<double>(const double*, int, double*, const int*, const double*,
+                                        int, int, cudaStream_t);
+template void launch_permute_out_add<float>(const float*, const int*, const double*, double*,
+                                            int, int, int, bool, cudaStream_t);
+template void launch_permute_out_add<double>(const double*, const int*, const double*, double*,
+                                             int, int, int, bool, cudaStream_t);
 
 }  // namespace sylver_gb300

@@ -502,6 +502,7 @@ int factorize_ldlt(FKeep& fk, const double* val_dev, cudaStream_t s) {
     if (nz) SG_CUDA(cudaMemcpyAsync(fk.val.p, val_dev, nz * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
   }
+  fk.apply_scale(s);
   SG_CUDA(cudaMemcpyAsync(&fk.anorm_h, fk.anorm.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   fk.not_first_pass = fk.not_second_pass = 0;
   cudaEvent_t e0, e1;

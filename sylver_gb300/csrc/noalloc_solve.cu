@@ -17,6 +17,9 @@
 //  * Set-up: the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress) with that device current and caches it; make that
 //    first call before any stream capture.
+//  * Device: the factorization lives on the library's device.  The call is
+//    refused (SYLVER_ERROR_CALL_SEQUENCE) when another device is current or
+//    the caller's stream belongs to another device, before anything runs.
 //  * Sharing: every call uses the same array.  The kernel fully rewrites the
 //    slab rows it reads (zeroing the rows it accumulates into), so stale
 //    contents from an earlier call never leak into a result, but two calls
@@ -24,6 +27,7 @@
 //    threads) race on the array and give wrong answers.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cstdint>
 
 #include "../../include/sylver_gb300.h"
@@ -37,7 +41,9 @@ static __device__ __align__(256) double g_noalloc_scratch[NOALLOC_SCRATCH_DOUBLE
 
 namespace {
 constexpr int kMaxDevices = 64;
-double* g_scratch_addr[kMaxDevices] = {nullptr};
+// per-device address cache; two host threads may race on the first lookup,
+// both store the same address
+std::atomic<double*> g_scratch_addr[kMaxDevices];
 }  // namespace
 
 // Device address of the static scratch on the current device (set-up on the
@@ -49,16 +55,18 @@ static double* noalloc_scratch_ptr(int* err) {
     *err = SYLVER_ERROR_CUDA_UNKNOWN;
     return nullptr;
   }
-  if (!g_scratch_addr[dev]) {
+  double* cached = g_scratch_addr[dev].load(std::memory_order_acquire);
+  if (!cached) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       *err = SYLVER_ERROR_CUDA_UNKNOWN;
       return nullptr;
     }
-    g_scratch_addr[dev] = static_cast<double*>(p);
+    cached = static_cast<double*>(p);
+    g_scratch_addr[dev].store(cached, std::memory_order_release);
   }
-  return g_scratch_addr[dev];
+  return cached;
 }
 
 }  // namespace sylver_gb300
@@ -90,10 +98,23 @@ extern "C" int spldlt_tree_solve_fwd_noalloc_dbl(bool posdef, void const* tree, 
   }
   const int chunk = nrhs < 32 ? nrhs : 32;
   if ((size_t)scratch_rows * (size_t)chunk > NOALLOC_SCRATCH_DOUBLES) return SYLVER_ERROR_X_SIZE;
+  // the factorization's device memory belongs to the library's device: the
+  // current device and the caller's stream must be that device's
+  const int lib_dev = Runtime::get().device;
+  int cur = -1;
+  if (cudaGetDevice(&cur) != cudaSuccess || cur != lib_dev) return SYLVER_ERROR_CALL_SEQUENCE;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : Runtime::get().stream;
+  if (stream) {
+    int sdev = -1;
+    if (cudaStreamGetDevice(s, &sdev) != cudaSuccess || sdev != lib_dev)
+      return SYLVER_ERROR_CALL_SEQUENCE;
+  }
   int err = 0;
   double* scratch = noalloc_scratch_ptr(&err);
   if (!scratch) return err;
-  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : Runtime::get().stream;
+  // clear an error left by earlier work so that the check after the launches
+  // sees only this call's
+  cudaGetLastError();
   try {
     const double* arena = fk->arena.as<double>();
     for (int r0 = 0; r0 < nrhs; r0 += 32) {
@@ -104,6 +125,7 @@ extern "C" int spldlt_tree_solve_fwd_noalloc_dbl(bool posdef, void const* tree, 
         launch_solve_fwd<double, double>(arena, fr + L.f0, L.f1 - L.f0, rows, xr, ldx, nr,
                                          scratch, scr + L.f0, !posdef, s);
     }
+    if (cudaGetLastError() != cudaSuccess) return SYLVER_ERROR_CUDA_UNKNOWN;
     if (cudaStreamSynchronize(s) != cudaSuccess) return SYLVER_ERROR_CUDA_UNKNOWN;
   } catch (const std::exception&) {
     return SYLVER_ERROR_CUDA_UNKNOWN;

@@ -8,6 +8,7 @@
 // whole posdef factorization is one captured CUDA graph.
 #include "numeric.hpp"
 #include "ldlt.hpp"
+#include "../../include/sylver_gb300.h"
 
 #include <algorithm>
 #include <cmath>
@@ -107,6 +108,52 @@ int64_t AKeep::nnz_val() const {
 }
 
 int64_t FKeep::nnz_orig() const { return ak->nnz_val(); }
+
+void AKeep::build_val_rowcol() {
+  const int64_t nz = nnz_val();
+  if ((int64_t)vrow.size() == nz) return;
+  vrow.assign(nz, -1);
+  vcol.assign(nz, -1);
+  if (!clean.crow.empty()) {
+    for (int c = 0; c < n; ++c)
+      for (int64_t k = clean.cptr[c]; k < clean.cptr[c + 1]; ++k)
+        for (int64_t q = clean.srcptr[k]; q < clean.srcptr[k + 1]; ++q) {
+          vrow[clean.src[q]] = clean.crow[k];
+          vcol[clean.src[q]] = c;
+        }
+    return;
+  }
+  // tree-level seam: val is indexed by nlist sources, the variables are the
+  // rlist values (entry dest of a front is row dest % nrow, column dest / nrow)
+  for (int f = 0; f < st.nnodes; ++f) {
+    const int64_t r0 = st.rptr[f] - 1;
+    const int64_t nrow = st.rptr[f + 1] - st.rptr[f];
+    for (int64_t k = st.nptr[f] - 1; k < st.nptr[f + 1] - 1; ++k) {
+      const int64_t srcv = st.nlist[2 * k] - 1, dst = st.nlist[2 * k + 1] - 1;
+      vrow[srcv] = st.rlist[r0 + dst % nrow] - 1;
+      vcol[srcv] = st.rlist[r0 + dst / nrow] - 1;
+    }
+  }
+}
+
+void FKeep::set_scale(const double* scale_host, cudaStream_t s) {
+  has_scale = scale_host != nullptr && ak->n > 0;
+  if (!has_scale) return;
+  ak->build_val_rowcol();
+  if (dvrow.bytes < ak->vrow.size() * sizeof(int) || !dvrow.p) {
+    dvrow.upload(ak->vrow, s);
+    dvcol.upload(ak->vcol, s);
+  }
+  dscale.ensure((size_t)ak->n * sizeof(double));
+  SG_CUDA(cudaMemcpyAsync(dscale.p, scale_host, (size_t)ak->n * sizeof(double),
+                          cudaMemcpyHostToDevice, s));
+}
+
+void FKeep::apply_scale(cudaStream_t s) {
+  if (!has_scale) return;
+  launch_scale_vals(val.as<double>(), dvrow.as<int>(), dvcol.as<int>(), dscale.as<double>(),
+                    nnz_orig(), s);
+}
 
 namespace {
 // fronts that get the blocked multi-CTA solve
@@ -607,6 +654,7 @@ int FKeep::factorize(const double* val_dev, cudaStream_t s) {
     if (nz) SG_CUDA(cudaMemcpyAsync(val.p, val_dev, nz * sizeof(double),
                                     cudaMemcpyDeviceToDevice, s));
   }
+  apply_scale(s);
   cudaEvent_t e0, e1;
   SG_CUDA(cudaEventCreate(&e0));
   SG_CUDA(cudaEventCreate(&e1));
@@ -658,6 +706,7 @@ int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, c
     int64_t nz = nnz_orig();
     SG_CUDA(cudaMemcpyAsync(val.p, val_dev, nz * sizeof(double), cudaMemcpyDeviceToDevice, s));
   }
+  apply_scale(s);
   SG_CUDA(cudaMemsetAsync(status.p, 0, sizeof(unsigned), s));
   std::vector<cudaEvent_t> ev(ops.size() + 1);
   for (auto& e : ev) SG_CUDA(cudaEventCreate(&e));
@@ -980,17 +1029,22 @@ int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
   last_ir_iters = 0;
   last_bwd_err = -1.0;
   ir_hist.clear();
+  // S on the way in for jobs 0/1 and on the way out for jobs 0/3/4
+  // (src/spldlt_factorize_mod.F90:945-955, :1040-1050)
+  const double* sc = has_scale ? dscale.as<double>() : nullptr;
   auto one_solve = [&](const double* rhs, int ldr, double* out, int ldo, bool add, int jb) {
+    const double* sin = (jb == 0 || jb == 1) ? sc : nullptr;
+    const double* sout = (jb == 0 || jb == 3 || jb == 4) ? sc : nullptr;
     if (f32) {
-      launch_permute_in<float>(rhs, ldr, xp.as<float>(), perm, n, nrhs, s);
+      launch_permute_in<float>(rhs, ldr, xp.as<float>(), perm, sin, n, nrhs, s);
       if (ldlt) ldlt_solve_pivot_order(*this, jb, xp.as<float>(), nrhs, s);
       else solve_pivot_order<float>(jb, xp.p, nrhs, s);
-      launch_permute_out_add<float>(xp.as<float>(), perm, out, ldo, n, nrhs, add, s);
+      launch_permute_out_add<float>(xp.as<float>(), perm, sout, out, ldo, n, nrhs, add, s);
     } else {
-      launch_permute_in<double>(rhs, ldr, xp.as<double>(), perm, n, nrhs, s);
+      launch_permute_in<double>(rhs, ldr, xp.as<double>(), perm, sin, n, nrhs, s);
       if (ldlt) ldlt_solve_pivot_order(*this, jb, xp.as<double>(), nrhs, s);
       else solve_pivot_order<double>(jb, xp.p, nrhs, s);
-      launch_permute_out_add<double>(xp.as<double>(), perm, out, ldo, n, nrhs, add, s);
+      launch_permute_out_add<double>(xp.as<double>(), perm, sout, out, ldo, n, nrhs, add, s);
     }
   };
   const bool refine = job == 0 && (f32 || ir_max_iter > 0);
@@ -1029,7 +1083,8 @@ int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
     last_bwd_err = worst;
     ir_hist.push_back(worst);
     last_ir_iters = it;
-    if (worst <= ir_tol || it >= maxit) break;
+    if (worst <= ir_tol) break;
+    if (it >= maxit) return SYLVER_GB300_WARNING_IR_NOT_CONVERGED;
     one_solve(resid.as<double>(), n, x, ldx, true, 0);
   }
   return 0;

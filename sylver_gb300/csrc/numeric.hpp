@@ -100,6 +100,11 @@ struct AKeep {
   // a scan of every map, too slow to repeat per factorization)
   int64_t nnz_val() const;
   mutable int64_t nz_val_ = -1;
+  // per entry of the caller's val array: its row and column variable (user
+  // order, 0-based; -1 for entries the analysis does not use), for the
+  // scaling S A S.  Built on the first scaled factorization.
+  std::vector<int> vrow, vcol;
+  void build_val_rowcol();
 };
 
 // One kernel launch of the factor schedule.
@@ -168,7 +173,13 @@ struct FKeep {
   double u = 0.01;
   double small_piv = 1e-20;
   bool action = true;
-  std::vector<double> scale;  // user scaling S (empty: none)
+  // scaling S (user order, FP64 on the device): the factorization is of
+  // S A S (init_a_block, src/kernels/assemble.hxx:162-180); solves apply S on
+  // the way in and out by job (src/spldlt_factorize_mod.F90:945-1050)
+  bool has_scale = false;
+  DevMem dscale, dvrow, dvcol;
+  void set_scale(const double* scale_host, cudaStream_t s);  // null: none
+  void apply_scale(cudaStream_t s);  // val <- S val S in place (no-op without S)
 
   // tensor-core updates (FP32 Cholesky): stacked transposed operands, split
   // into three BF16 planes

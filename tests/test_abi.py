@@ -28,9 +28,56 @@ def test_exports_match_header(sylver):
     assert set(sylver.EXPORTS) <= names
 
 
+LAYOUTS = os.path.join(ROOT, "tests", "golden", "struct_layouts.json")
+# our header's name for each reference struct
+OURS = {"sylver_inform_t": "sylver_inform_t", "sylver_options_t": "sylver_options_t",
+        "options_c": "sylver_options_c", "inform_c": "sylver_inform_c"}
+
+
+def test_struct_layouts_compiled_against_header(tmp_path):
+    """sizeof and offsetof of the four boundary structs, compiled by the C
+    compiler against include/sylver_gb300.h, equal the values compiled from
+    the reference's own definitions (tests/golden/make_layouts.py)."""
+    import json
+    import shutil
+    import subprocess
+    ref = json.load(open(LAYOUTS))
+    cc = shutil.which("gcc") or shutil.which("cc")
+    assert cc, "no C compiler"
+    src = ["#include <stddef.h>", "#include <stdio.h>", '#include "sylver_gb300.h"',
+           "int main(void){"]
+    for rname, cname in OURS.items():
+        src.append(f'printf("{rname} sizeof %zu\\n", sizeof({cname}));')
+        for m in ref[rname]:
+            if m != "sizeof":
+                src.append(f'printf("{rname} {m} %zu\\n", offsetof({cname}, {m}));')
+    src.append("return 0;}")
+    (tmp_path / "p.c").write_text("\n".join(src) + "\n")
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(tmp_path / "p.c"), "-o",
+                    str(tmp_path / "p")], check=True)
+    out = subprocess.run([str(tmp_path / "p")], capture_output=True, text=True, check=True)
+    got = {}
+    for line in out.stdout.splitlines():
+        s, m, v = line.split()
+        got.setdefault(s, {})[m] = int(v)
+    for rname in OURS:
+        assert got[rname] == ref[rname], rname
+
+
+def test_ctypes_mirrors_match_layouts(sylver):
+    """The Python binding's Structure mirrors have the same layouts."""
+    import json
+    ref = json.load(open(LAYOUTS))
+    for rname, cls in (("sylver_inform_t", sylver.Inform), ("sylver_options_t", sylver.Options),
+                       ("options_c", sylver.OptionsC), ("inform_c", sylver.InformC)):
+        assert ctypes.sizeof(cls) == ref[rname]["sizeof"], rname
+        for m, off in ref[rname].items():
+            if m != "sizeof":
+                assert getattr(cls, m).offset == off, (rname, m)
+
+
 def test_struct_layouts(sylver):
-    # sylver_inform_t / sylver_options_t sizes as compiled by the C compiler
-    assert ctypes.sizeof(sylver.Inform) == 4 * 8 + 8 * 2 + 4 * 6 + 80
+    # option defaults (src/sylver_datatypes_mod.F90:97-198)
     o = sylver.default_options()
     assert o.nemin == 32 and o.nb == 256 and abs(o.u - 0.01) < 1e-15 and o.action
     assert o.ordering == 1 and abs(o.small - 1e-20) < 1e-35

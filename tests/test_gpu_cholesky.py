@@ -202,3 +202,22 @@ def test_fp32_blocked_not_posdef(sylver, gpu):
     an = sylver.Analysis(m.n, m.ptr, m.row)
     f = sylver.Factor(an, True, m.val, precision=sylver.FP32)
     assert f.flag == -6
+
+
+def test_refinement_not_converged_is_reported(sylver, gpu):
+    """Refinement that stops at ir_max_iter above ir_tol returns the warning
+    SYLVER_GB300_WARNING_IR_NOT_CONVERGED (9) in inform.flag, with the error
+    reached in the statistics; a converged refinement returns 0."""
+    p = w.lognormal27(12, nrhs=2)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    f = sylver.Factor(an, True, p.a.val, precision=sylver.FP32, ir_tol=1e-30, ir_max_iter=2)
+    x = f.solve(p.rhs)
+    assert f.solve_inform.flag == sylver.WARNING_IR_NOT_CONVERGED
+    it, be = f.solve_stats()
+    assert it == 2 and 1e-30 < be
+    assert len(f.solve_history()) == 3
+    assert np.all(np.isfinite(x))
+    g = sylver.Factor(an, True, p.a.val, precision=sylver.FP32, ir_tol=1e-14, ir_max_iter=10)
+    g.solve(p.rhs)
+    assert g.solve_inform.flag == 0
+    assert g.solve_stats()[1] <= 1e-14

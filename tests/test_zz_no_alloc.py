@@ -32,7 +32,9 @@ def test_noalloc_forward_solve_matches(sylver, gpu, posdef):
     assert f.flag == 0
     n = p.a.n
     P = ctypes.c_void_p
-    for call, nrhs in enumerate((3, 5)):
+    # 40 right-hand sides run as two chunks (32 + 8): the second chunk reuses
+    # the scratch slabs the first one left behind
+    for call, nrhs in enumerate((3, 5, 40)):
         b = _rhs(n, nrhs, 100 + call)
         ldx = n + 7
         # existing entry point: host memory, allocates its own device buffers
@@ -70,3 +72,34 @@ def test_noalloc_rejects_bad_sizes(sylver, gpu):
     f32 = sylver.Factor(an, True, p.a.val, precision=sylver.FP32)
     assert lib.spldlt_tree_solve_fwd_noalloc_dbl(True, f32.fkeep, 1, P(x.data_ptr()), p.a.n,
                                                  None) == -98
+
+
+def test_noalloc_rejects_level_beyond_scratch(sylver, gpu):
+    """A level whose slabs (sum of its front rows x min(nrhs, 32) doubles)
+    exceed the 2,097,152-double static array is refused before any launch,
+    and x is left as it was."""
+    import torch
+    lib = sylver.load()
+    p = w.laplace2d(400, nrhs=1)  # widest level about 175,000 rows
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    f = sylver.Factor(an, True, p.a.val)
+    assert f.flag == 0
+    n, nrhs = p.a.n, 32
+    b = _rhs(n, nrhs, 7)
+    x_dev = torch.from_numpy(np.ascontiguousarray(b.T)).cuda()
+    torch.cuda.synchronize()
+    P = ctypes.c_void_p
+    rc = lib.spldlt_tree_solve_fwd_noalloc_dbl(True, f.fkeep, nrhs, P(x_dev.data_ptr()), n, None)
+    assert rc == -10
+    assert np.array_equal(x_dev.cpu().numpy().T, b)
+    # one right-hand side fits (about 175,000 doubles) and matches the
+    # allocating entry point
+    x1 = np.asfortranarray(b[:, :1].copy())
+    rc = lib.spldlt_tree_solve_fwd_dbl(True, f.fkeep, 1, x1.ctypes.data_as(P), n)
+    assert rc == 0
+    x1_dev = torch.from_numpy(b[:, 0].copy()).cuda()
+    torch.cuda.synchronize()
+    rc = lib.spldlt_tree_solve_fwd_noalloc_dbl(True, f.fkeep, 1, P(x1_dev.data_ptr()), n, None)
+    assert rc == 0
+    got = x1_dev.cpu().numpy()
+    assert np.abs(got - x1[:, 0]).max() <= 1e-12 * np.abs(x1).max()
