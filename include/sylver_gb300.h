@@ -260,6 +260,14 @@ int sylver_gb300_akeep_arrays(void const* akeep, int* sptr, int* sparent, long* 
  * permutation applied by delays; for tests.  Returns number of pivots. */
 int sylver_gb300_fkeep_diag(void const* fkeep, double* d, int* piv_order);
 
+/* Per-front sizes of an LDL^T factorization in front (postorder) order:
+ * rows m (with delayed rows), fully-summed columns n (own plus delayed in)
+ * and columns eliminated; any pointer may be null.  D^-1 and the pivot order
+ * of sylver_gb300_fkeep_diag come front by front in this order, nelim
+ * entries each.  Returns the number of fronts (0 for a Cholesky factor).
+ * No reference counterpart; for tests. */
+int sylver_gb300_fkeep_fronts(void const* fkeep, int* m, int* n, int* nelim);
+
 /* The CUDA stream (cudaStream_t) all library work is issued on; callers that
  * time with CUDA events record them on this stream. */
 void* sylver_gb300_stream(void);

@@ -32,7 +32,8 @@ def build(force: bool = False) -> str:
         return _SO
     os.makedirs(_BUILD, exist_ok=True)
     tmp = _SO + f".tmp{os.getpid()}"
-    subprocess.check_call(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", src, "-o", tmp])
+    subprocess.check_call(["g++", "-O3", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared",
+                           src, "-o", tmp])
     os.replace(tmp, _SO)
     return _SO
 
@@ -82,10 +83,12 @@ def load():
     P = ctypes.c_void_p
     lib.oracle_factor.restype = P
     lib.oracle_factor.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P,
-                                  P, P, ctypes.c_double, ctypes.c_double, ctypes.c_int, P]
+                                  P, P, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                  ctypes.c_int, P]
     lib.oracle_solve.restype = ctypes.c_int
     lib.oracle_solve.argtypes = [P, ctypes.c_int, ctypes.c_int, P, ctypes.c_int]
     lib.oracle_free.argtypes = [P]
+    lib.oracle_set_inplace.argtypes = [ctypes.c_int]
     lib.oracle_front.restype = ctypes.c_int
     lib.oracle_front.argtypes = [P, ctypes.c_int, P, P, P, P]
     _lib = lib
@@ -102,9 +105,15 @@ class OracleFactor:
     STAT_NAMES = ("flag", "num_neg", "num_zero", "num_two", "num_delay", "maxfront",
                   "not_first_pass", "not_second_pass", "matrix_rank")
 
-    def __init__(self, posdef, symb, val, u=0.01, small=1e-20, action=True):
+    def __init__(self, posdef, symb, val, u=0.01, small=1e-20, action=True, tpp_cols=0,
+                 inplace=False):
         """symb: dict with n, nnodes, sptr, sparent, rptr, rlist, nptr, nlist,
-        perm (all 1-based, reference layout)."""
+        perm (all 1-based, reference layout).  LDL^T: a-posteriori pivoting in
+        blocks of 32 then threshold partial pivoting on the failed columns;
+        fronts with at most tpp_cols fully-summed columns use threshold
+        partial pivoting only.  inplace=True runs the block steps in the
+        reference's own layout (failed columns left in place until
+        permute_failed), a check of the default layout."""
         lib = load()
         self._keep = {k: np.ascontiguousarray(v) for k, v in symb.items()
                       if isinstance(v, np.ndarray)}
@@ -113,12 +122,14 @@ class OracleFactor:
         self.posdef = bool(posdef)
         self.val = np.ascontiguousarray(val, dtype=np.float64)
         st = np.zeros(9, dtype=np.int32)
+        lib.oracle_set_inplace(int(bool(inplace)))
         self.h = lib.oracle_factor(
             int(posdef), self.n, int(symb["nnodes"]),
             _p(k["sptr"].astype(np.int32)) if k["sptr"].dtype != np.int32 else _p(k["sptr"]),
             _p(k["sparent"]), _p(k["rptr"]), _p(k["rlist"]), _p(k["nptr"]),
             _p(k["nlist"]), _p(k["perm"]), _p(self.val), float(u), float(small),
-            int(action), _p(st))
+            int(action), int(tpp_cols), _p(st))
+        lib.oracle_set_inplace(0)
         self.stats = dict(zip(self.STAT_NAMES, (int(v) for v in st)))
         self.flag = self.stats["flag"]
 

@@ -125,6 +125,7 @@ EXPORTS = (
     "spldlt_tree_solve_bwd_posdef_dbl", "spldlt_factorize_mixed", "spldlt_factorize_device",
     "spldlt_solve_device", "sylver_gb300_solve_stats", "sylver_gb300_akeep_sizes",
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
+    "sylver_gb300_fkeep_fronts",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
     "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
     "sylver_gb300_get_schedule", "sylver_gb300_profile_solve", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
@@ -167,6 +168,7 @@ def load(path: str | None = None):
                                          ctypes.POINTER(L), ctypes.POINTER(L)]),
         "sylver_gb300_akeep_arrays": (I, [P, P, P, P, P, P, P, P]),
         "sylver_gb300_fkeep_diag": (I, [P, P, P]),
+        "sylver_gb300_fkeep_fronts": (I, [P, P, P, P]),
         "sylver_gb300_fkeep_counters": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I),
                                             ctypes.POINTER(D)]),
         "sylver_gb300_stream": (P, []),
@@ -343,6 +345,13 @@ class Factor:
         if rc != 0:
             raise RuntimeError(f"profile_solve failed: {rc}")
         return {k: dict(ms=float(ms[i]), launches=int(nl[i])) for i, k in enumerate(self.SOLVE_KINDS)}
+
+    def fronts(self):
+        """Per-front (m, n, nelim) of an LDL^T factor, postorder."""
+        nn = self.analysis.symbolic()["nnodes"]
+        m = np.zeros(max(nn, 1), np.int32); n = np.zeros_like(m); ne = np.zeros_like(m)
+        k = load().sylver_gb300_fkeep_fronts(self.fkeep, _p(m), _p(n), _p(ne))
+        return m[:max(k, 0)], n[:max(k, 0)], ne[:max(k, 0)]
 
     def diag(self, n):
         d = np.zeros(2 * max(n, 1), dtype=np.float64)

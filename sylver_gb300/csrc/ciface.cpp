@@ -364,6 +364,12 @@ int sylver_gb300_fkeep_diag(void const* fkeep, double* d, int* piv_order) {
   return ldlt_export_diag(*fk, d, piv_order);
 }
 
+int sylver_gb300_fkeep_fronts(void const* fkeep, int* m, int* n, int* nelim) {
+  const FKeep* fk = static_cast<const FKeep*>(fkeep);
+  if (!fk) return -1;
+  return ldlt_export_fronts(*fk, m, n, nelim);
+}
+
 void* sylver_gb300_stream(void) {
   Runtime& rt = Runtime::get();
   rt.init();

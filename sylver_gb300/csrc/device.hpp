@@ -187,9 +187,10 @@ void launch_zero_lower(T* arena, const ZeroTask* t, int ntask, cudaStream_t s);
 template <typename T>
 void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
                    int64_t count, bool atomic, cudaStream_t s);
+// atomic = false: at most one child per parent in this launch (see kernel).
 template <typename T>
 void launch_extend_add(T* arena, const ChildDesc* cd, const EaItem* items, const int* maps,
-                       int nitems, cudaStream_t s);
+                       int nitems, cudaStream_t s, bool atomic = true);
 template <typename T>
 void launch_small_chol(T* arena, const SmallTask* t, int ntask, int maxm, unsigned* status,
                        cudaStream_t s);

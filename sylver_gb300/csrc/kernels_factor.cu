@@ -11,6 +11,7 @@
 //                                     src/kernels/factor.hxx:56-260,
 //                                     src/factor.hxx:19-148
 #include "device.hpp"
+#include "tile_update.cuh"
 
 namespace sylver_gb300 {
 
@@ -47,11 +48,14 @@ __global__ void k_init_a(T* __restrict__ arena, const double* __restrict__ val,
 }
 
 // One warp per (child, CB column): parent(map[i], map[j]) += cb(i, j), i >= j.
-// Two children of one parent may hit the same parent entry, hence atomics.
+// Two children of one parent may hit the same parent entry: with `atomic`
+// the launch may hold several children of a parent; without it the caller
+// gives each launch at most one child per parent (children in a fixed order
+// across launches), which makes the sums deterministic.
 template <typename T>
 __global__ void k_extend_add(T* __restrict__ arena, const ChildDesc* __restrict__ cd,
                              const EaItem* __restrict__ items, const int* __restrict__ maps,
-                             int nitems) {
+                             int nitems, bool atomic) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (warp >= nitems) return;
@@ -65,7 +69,9 @@ __global__ void k_extend_add(T* __restrict__ arena, const ChildDesc* __restrict_
   for (int i = j + lane; i < c.mc; i += 32) {
     const int pi = map[i];
     const int r = max(pi, pj), cc = min(pi, pj);
-    atomic_add(dst + (int64_t)cc * c.ld_p + r, src[i]);
+    T* d = dst + (int64_t)cc * c.ld_p + r;
+    if (atomic) atomic_add(d, src[i]);
+    else *d += src[i];
   }
 }
 
@@ -199,101 +205,18 @@ __global__ void __launch_bounds__(RT) k_panel_trsm(T* __restrict__ arena,
 }
 
 // ---------------------------------------------------------------------------
-// SIMT tile update C[rows, cols] -= sum_k A[rows,k] A[cols,k] with a 16x16
-// thread grid, RMxRN register micro-tiles split in two halves (rows
-// ty*RM/2.. and TM/2+ty*RM/2..) and double-buffered KT-deep shared tiles.
+// SIMT tile update C[rows, cols] -= sum_k A[rows,k] B[cols,k], one task per CTA
+// (body in tile_update.cuh).
 template <typename T, int TM, int TN, int KT>
 __global__ void __launch_bounds__(256) k_update(T* __restrict__ arena,
                                                 const T* __restrict__ abuf,
                                                 const UpdTask* __restrict__ tasks) {
-  constexpr int RM = TM / 16, RN = TN / 16;
-  constexpr int HM = RM / 2, HN = RN / 2;
-  constexpr int LA = (KT * TM) / 256, LB = (KT * TN) / 256;
   __shared__ __align__(16) T As[2][KT][TM];
   __shared__ __align__(16) T Bs[2][KT][TN];
   const UpdTask t = tasks[blockIdx.x];
-  const T* A = abuf + t.a_off;
-  const T* B = arena + t.b_off;
-  T* C = arena + t.c_off;
-  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-  T ra[LA], rb[LB];
-  auto gload = [&](int kc) {
-#pragma unroll
-    for (int q = 0; q < LA; ++q) {
-      int e = tid + q * 256;
-      int i = e % TM, kk = e / TM;
-      int row = t.row0 + i, k = kc + kk;
-      ra[q] = (row < t.rowEnd && k < t.k1) ? A[(int64_t)k * t.lda + row] : T(0);
-    }
-#pragma unroll
-    for (int q = 0; q < LB; ++q) {
-      int e = tid + q * 256;
-      int i = e % TN, kk = e / TN;
-      int col = t.col0 + i, k = kc + kk;
-      rb[q] = (col < t.colEnd && k < t.k1) ? B[(int64_t)k * t.ldb + col] : T(0);
-    }
-  };
-  auto sstore = [&](int buf) {
-#pragma unroll
-    for (int q = 0; q < LA; ++q) {
-      int e = tid + q * 256;
-      As[buf][e / TM][e % TM] = ra[q];
-    }
-#pragma unroll
-    for (int q = 0; q < LB; ++q) {
-      int e = tid + q * 256;
-      Bs[buf][e / TN][e % TN] = rb[q];
-    }
-  };
-  T acc[RM][RN];
-#pragma unroll
-  for (int i = 0; i < RM; ++i)
-#pragma unroll
-    for (int j = 0; j < RN; ++j) acc[i][j] = T(0);
-
-  int kc = t.k0;
-  gload(kc);
-  sstore(0);
-  __syncthreads();
-  int buf = 0;
-  for (; kc < t.k1; kc += KT) {
-    const bool more = kc + KT < t.k1;
-    if (more) gload(kc + KT);
-#pragma unroll
-    for (int kk = 0; kk < KT; ++kk) {
-      T av[RM], bv[RN];
-#pragma unroll
-      for (int i = 0; i < HM; ++i) {
-        av[i] = As[buf][kk][ty * HM + i];
-        av[HM + i] = As[buf][kk][TM / 2 + ty * HM + i];
-      }
-#pragma unroll
-      for (int j = 0; j < HN; ++j) {
-        bv[j] = Bs[buf][kk][tx * HN + j];
-        bv[HN + j] = Bs[buf][kk][TN / 2 + tx * HN + j];
-      }
-#pragma unroll
-      for (int i = 0; i < RM; ++i)
-#pragma unroll
-        for (int j = 0; j < RN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
-    }
-    if (more) {
-      sstore(buf ^ 1);
-      __syncthreads();
-      buf ^= 1;
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < RM; ++i) {
-    int row = t.row0 + ((i < HM) ? ty * HM + i : TM / 2 + ty * HM + (i - HM));
-    if (row >= t.rowEnd) continue;
-#pragma unroll
-    for (int j = 0; j < RN; ++j) {
-      int col = t.col0 + ((j < HN) ? tx * HN + j : TN / 2 + tx * HN + (j - HN));
-      if (col >= t.colEnd || col > row) continue;
-      C[(int64_t)col * t.ldc + row] -= acc[i][j];
-    }
-  }
+  tile_update_body<T, TM, TN, KT>(arena + t.c_off, t.ldc, abuf + t.a_off, t.lda,
+                                  arena + t.b_off, t.ldb, t.row0, t.col0, t.rowEnd, t.colEnd,
+                                  t.k0, t.k1, As, Bs);
 }
 
 }  // namespace
@@ -316,10 +239,10 @@ void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_
 
 template <typename T>
 void launch_extend_add(T* arena, const ChildDesc* cd, const EaItem* items, const int* maps,
-                       int nitems, cudaStream_t s) {
+                       int nitems, cudaStream_t s, bool atomic) {
   if (nitems <= 0) return;
   int blocks = (nitems + 7) / 8;
-  k_extend_add<T><<<blocks, 256, 0, s>>>(arena, cd, items, maps, nitems);
+  k_extend_add<T><<<blocks, 256, 0, s>>>(arena, cd, items, maps, nitems, atomic);
 }
 
 template <typename T>
@@ -374,7 +297,7 @@ void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStr
   template void launch_init_a<T>(T*, const double*, const int64_t*, const int64_t*, int64_t, \
                                  bool, cudaStream_t);                                       \
   template void launch_extend_add<T>(T*, const ChildDesc*, const EaItem*, const int*, int,   \
-                                     cudaStream_t);                                         \
+                                     cudaStream_t, bool);                                   \
   template void launch_small_chol<T>(T*, const SmallTask*, int, int, unsigned*, cudaStream_t); \
   template void launch_diag_chol<T>(T*, const PanelTask*, int, unsigned*, cudaStream_t);     \
   template void launch_panel_trsm<T>(T*, const PanelTask*, int, cudaStream_t);               \

@@ -3,18 +3,25 @@
 // Replaces the reference's indefinite numeric tree (src/NumericTree.hxx:54-181,
 // :186-406), front allocation with delays (src/NumericFront.hxx:73-145),
 // assembly of delayed columns (src/kernels/assemble.hxx:926-1093), the APP
-// driver (src/factor_indef.hxx:1484-1646), the failed-pivot TPP pass
-// (src/factor_failed.hxx:29-157) and the inertia reduction
+// driver (src/factor_indef.hxx:1338-1474, :1484-1646), the failed-pivot TPP
+// pass (src/factor_failed.hxx:29-157) and the inertia reduction
 // (src/NumericTree.hxx:143-178).
 //
 // Fronts are processed level by level (height in the assembly tree).  Front
 // sizes depend on how many columns the children delayed, so each level is
-// planned on the host once its children are done.  Inside a level every
-// block-column step is one launch sequence over all fronts of the level:
-//   diag (complete pivoting, FP64) -> apply (solve + threshold test) ->
-//   host reads the passed counts -> commit -> trailing update (tile GEMM).
-// Columns that no block accepts go through threshold partial pivoting; what
-// still fails is delayed to the parent, whose front grows accordingly.
+// planned on the host once its children are done: that is the one host
+// synchronisation per level.  Inside a level everything runs on the device:
+// a front with n fully-summed columns takes ceil(n / 32) block steps
+// whatever fails (each step processes the next 32 columns not yet tried),
+// so the launch sequence is known in advance; where a block starts, how many
+// of its pivots pass and how many columns failed so far live in device state
+// that the kernels read.  Per step: diagonal block -> rows below (solve +
+// threshold test) -> commit (L, restore failed columns, L*D, D) -> trailing
+// update -> move of the failed columns behind the unprocessed ones.  Then
+// threshold partial pivoting on the failed columns, a relaxed pass at the
+// roots, and the contribution-block update once the host knows how many
+// columns each front eliminated.  Children's contributions are added in a
+// fixed order (one launch per child rank), so the factors are deterministic.
 #include "ldlt.hpp"
 
 #include <algorithm>
@@ -32,8 +39,8 @@ struct LdltState {
   std::vector<int64_t> off, d_off;
   std::vector<std::vector<int>> var;  // host copy after factorization
   int64_t arena_used = 0, var_used = 0, d_used = 0;
-  DevMem dvar, dall, blk, bdinv, lperm, npass_raw, npass, tppo;
-  DevMem fr, rt, up, sc;  // per-launch descriptor buffers + scratch
+  DevMem dvar, dall, blk, bdinv, lperm, state, mvvar;
+  DevMem fr, fr2, cmap, cmap2, up, sc, sc2;  // per-level descriptors + scratch
   DevMem ea_cd, ea_items, ea_maps, am_src, am_dst;
   // solve
   DevMem sfr, sscr, sdoff;
@@ -45,6 +52,9 @@ struct LdltState {
 namespace {
 
 inline int round_up(int v, int a) { return (v + a - 1) / a * a; }
+
+// threshold of the relaxed pass at the roots (keeps only the small-pivot test)
+constexpr double kRootU = 1e-300;
 inline int64_t round_up64(int64_t v, int64_t a) { return (v + a - 1) / a * a; }
 
 // grow a device buffer keeping its contents
@@ -96,6 +106,19 @@ void plan_ldlt(FKeep& fk) {
   fk.arena_elems = sym + sym / 8 + 1024;
 }
 
+namespace {
+
+// CTA slices of one launch: for each front (index into the level's LdltFront
+// array) `count` CTAs.
+void add_slice(std::vector<CtaMap>& v, int f, int count) {
+  count = std::max(count, 1);
+  for (int c = 0; c < count; ++c) v.push_back({f, c, count, 0});
+}
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace
+
 template <typename T>
 static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   const SymbolicTree& st = fk.ak->st;
@@ -112,40 +135,42 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   L.var.assign(ns, {});
   L.arena_used = L.var_used = L.d_used = 0;
   fk.arena.ensure((size_t)fk.arena_elems * sizeof(T));
-  L.blk.ensure(1);
   unsigned* status = fk.status.as<unsigned>();
   SG_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), s));
   long launches = 0;
   std::vector<int> pos(st.n, -1);
-  const double u = fk.u, small = fk.small_piv;
+  const int tpp_cols = Schedule::current().ldlt_tpp_cols;
+  fk.not_first_pass = fk.not_second_pass = 0;
+  fk.num_delay = 0;
 
   for (const Level& lev : fk.levels) {
     std::vector<int> F(fk.order.begin() + lev.f0, fk.order.begin() + lev.f1);
+    const int nslot = (int)F.size();
     // ---- sizes, variable lists, storage
     int64_t lvl_off0 = L.arena_used;
     std::vector<int> hvar_lvl;
-    for (int s : F) {
-      int sncol = st.ncol[s], snrow = st.nrow[s];
+    for (int s2 : F) {
+      int sncol = st.ncol[s2], snrow = st.nrow[s2];
       int ndin = 0;
-      for (int c : st.children[s]) ndin += L.n[c] - L.nelim[c];
-      L.n[s] = sncol + ndin;
-      L.m[s] = snrow + ndin;
-      L.ld[s] = round_up(std::max(L.m[s], 1), 4);
-      L.off[s] = L.arena_used;
-      L.arena_used += round_up64((int64_t)L.ld[s] * L.m[s], 64);
-      L.d_off[s] = L.d_used;
-      L.d_used += 2 * (int64_t)std::max(L.n[s], 1);
-      L.var_off[s] = (int)L.var_used;
-      L.var_used += L.m[s];
-      auto& v = L.var[s];
+      for (int c : st.children[s2]) ndin += L.n[c] - L.nelim[c];
+      L.n[s2] = sncol + ndin;
+      L.m[s2] = snrow + ndin;
+      L.ld[s2] = round_up(std::max(L.m[s2], 1), 4);
+      L.off[s2] = L.arena_used;
+      L.arena_used += round_up64((int64_t)L.ld[s2] * L.m[s2], 64);
+      L.d_off[s2] = L.d_used;
+      L.d_used += 2 * (int64_t)std::max(L.n[s2], 1);
+      L.var_off[s2] = (int)L.var_used;
+      L.var_used += L.m[s2];
+      auto& v = L.var[s2];
       v.clear();
-      const int* rl = &st.rlist[st.rptr[s] - 1];
+      const int* rl = &st.rlist[st.rptr[s2] - 1];
       for (int i = 0; i < sncol; ++i) v.push_back(rl[i] - 1);
-      for (int c : st.children[s])
-        for (int j = L.nelim[c]; j < L.n[c]; ++j) v.push_back(L.var[c][j]);
+      for (int c : st.children[s2])
+        for (int jj = L.nelim[c]; jj < L.n[c]; ++jj) v.push_back(L.var[c][jj]);
       for (int i = sncol; i < snrow; ++i) v.push_back(rl[i] - 1);
       hvar_lvl.insert(hvar_lvl.end(), v.begin(), v.end());
-      fk.maxfront = std::max(fk.maxfront, L.m[s]);
+      fk.maxfront = std::max(fk.maxfront, L.m[s2]);
     }
     if (L.arena_used > fk.arena_elems) {
       int64_t ne = std::max(L.arena_used, fk.arena_elems + fk.arena_elems / 4);
@@ -166,15 +191,15 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
     {
       std::vector<int64_t> asrc, adst;
       bool atomic = false;
-      for (int s : F) {
-        int snrow = st.nrow[s], sncol = st.ncol[s], ndin = L.n[s] - sncol;
+      for (int s2 : F) {
+        int snrow = st.nrow[s2], sncol = st.ncol[s2], ndin = L.n[s2] - sncol;
         int64_t prev = -1;
-        for (int64_t k = st.nptr[s] - 1; k < st.nptr[s + 1] - 1; ++k) {
+        for (int64_t k = st.nptr[s2] - 1; k < st.nptr[s2 + 1] - 1; ++k) {
           int64_t src = st.nlist[2 * k] - 1, dest = st.nlist[2 * k + 1] - 1;
           int64_t c = dest / snrow, r = dest % snrow;
           if (r >= sncol) r += ndin;
           asrc.push_back(src);
-          adst.push_back(L.off[s] + c * L.ld[s] + r);
+          adst.push_back(L.off[s2] + c * L.ld[s2] + r);
           if (dest == prev) atomic = true;
           prev = dest;
         }
@@ -185,231 +210,234 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
                        (int64_t)asrc.size(), atomic, s);
       launches++;
     }
-    // ---- children: delayed columns and contribution blocks
+    // ---- children: delayed columns and contribution blocks, one launch per
+    // child rank (the r-th child of every front), children in increasing
+    // index order, so every parent entry sums its terms in a fixed order
     {
+      int maxkids = 0;
+      for (int p2 : F) maxkids = std::max(maxkids, (int)st.children[p2].size());
       std::vector<ChildDesc> cds;
       std::vector<EaItem> items;
       std::vector<int> maps;
-      for (int p : F) {
-        for (int i = 0; i < L.m[p]; ++i) pos[L.var[p][i]] = i;
-        for (int c : st.children[p]) {
+      std::vector<int64_t> rank_item0(maxkids + 1, 0);
+      std::vector<std::vector<int>> pmaps(F.size());
+      for (size_t k = 0; k < F.size(); ++k) {
+        int p2 = F[k];
+        for (int i = 0; i < L.m[p2]; ++i) pos[L.var[p2][i]] = i;
+        auto& pm = pmaps[k];
+        for (int c : st.children[p2])
+          for (int i = L.nelim[c]; i < L.m[c]; ++i) pm.push_back(pos[L.var[c][i]]);
+      }
+      for (int r = 0; r < maxkids; ++r) {
+        rank_item0[r] = (int64_t)items.size();
+        for (size_t k = 0; k < F.size(); ++k) {
+          int p2 = F[k];
+          const auto& kids = st.children[p2];
+          if (r >= (int)kids.size()) continue;
+          int moff = 0;
+          for (int rr = 0; rr < r; ++rr) moff += L.m[kids[rr]] - L.nelim[kids[rr]];
+          int c = kids[r];
           int mc = L.m[c] - L.nelim[c];
           if (mc <= 0) continue;
           ChildDesc cd;
           cd.cb_off = L.off[c] + (int64_t)L.nelim[c] * L.ld[c] + L.nelim[c];
-          cd.p_off = L.off[p];
+          cd.p_off = L.off[p2];
           cd.ld_c = L.ld[c];
-          cd.ld_p = L.ld[p];
+          cd.ld_p = L.ld[p2];
           cd.mc = mc;
           cd.map_off = (int)maps.size();
-          for (int i = L.nelim[c]; i < L.m[c]; ++i) maps.push_back(pos[L.var[c][i]]);
+          maps.insert(maps.end(), pmaps[k].begin() + moff, pmaps[k].begin() + moff + mc);
           int ci = (int)cds.size();
           cds.push_back(cd);
-          for (int j = 0; j < mc; ++j) items.push_back({ci, j});
+          for (int jj = 0; jj < mc; ++jj) items.push_back({ci, jj});
         }
       }
+      rank_item0[maxkids] = (int64_t)items.size();
       if (!items.empty()) {
         put(L.ea_cd, cds, s);
         put(L.ea_items, items, s);
         put(L.ea_maps, maps, s);
-        launch_extend_add<T>(A, L.ea_cd.as<ChildDesc>(), L.ea_items.as<EaItem>(),
-                             L.ea_maps.as<int>(), (int)items.size(), s);
-        launches++;
+        for (int r = 0; r < maxkids; ++r) {
+          int cnt = (int)(rank_item0[r + 1] - rank_item0[r]);
+          if (cnt <= 0) continue;
+          launch_extend_add<T>(A, L.ea_cd.as<ChildDesc>(),
+                               L.ea_items.as<EaItem>() + rank_item0[r], L.ea_maps.as<int>(),
+                               cnt, s, /*atomic=*/false);
+          launches++;
+        }
       }
     }
-    // ---- block-column steps (a posteriori pivoting)
-    const int nslot = (int)F.size();
-    L.blk.ensure((size_t)nslot * LDLT_BW * (LDLT_BW + 1) * sizeof(double));
-    L.bdinv.ensure((size_t)nslot * 2 * LDLT_BW * sizeof(double));
-    L.lperm.ensure((size_t)nslot * LDLT_BW * sizeof(int));
-    L.npass_raw.ensure((size_t)nslot * sizeof(int));
-    L.npass.ensure((size_t)nslot * sizeof(int));
-    L.tppo.ensure((size_t)nslot * sizeof(int));
-    LdltStep stp{L.blk.as<double>(), L.bdinv.as<double>(), L.lperm.as<int>(),
-                 L.npass_raw.as<int>(), L.npass.as<int>(), dvar, L.dall.as<double>(), status,
-                 u, small, fk.action ? 1 : 0};
-    std::vector<int> p(nslot, 0);
-    std::vector<char> app_done(nslot, 0);
-    // small fronts may skip the block steps and go to TPP directly
-    const int tpp_cols = Schedule::current().ldlt_tpp_cols;
-    for (int q = 0; q < nslot; ++q) app_done[q] = L.n[F[q]] == 0 || L.n[F[q]] <= tpp_cols;
-    std::vector<int> hraw, hnp;
-    std::vector<double> hdv;
-    for (;;) {
-      std::vector<LdltFront> fr;
-      std::vector<int> slot;
-      int64_t scr = 0;
-      for (int q = 0; q < nslot; ++q) {
-        if (app_done[q]) continue;
-        int s2 = F[q];
-        LdltFront f{};
-        f.off = L.off[s2];
-        f.ld = L.ld[s2];
-        f.m = L.m[s2];
-        f.n = L.n[s2];
-        f.p = p[q];
-        f.w = std::min(LDLT_BW, L.n[s2] - p[q]);
-        f.fidx = q;
-        f.var_off = L.var_off[s2];
-        f.d_off = L.d_off[s2];
-        f.pan_off = scr;
-        scr += (int64_t)f.m * LDLT_BW;
-        f.ldp_off = scr;
-        scr += (int64_t)f.m * LDLT_BW;
-        fr.push_back(f);
-        slot.push_back(q);
-      }
-      if (fr.empty()) break;
+    // ---- level descriptors and scratch
+    std::vector<LdltFront> fr(nslot);
+    int64_t scr = 0, ivar = 0;
+    int maxblk = 0;
+    for (int q = 0; q < nslot; ++q) {
+      int s2 = F[q];
+      LdltFront& f = fr[q];
+      f.off = L.off[s2];
+      f.ld = L.ld[s2];
+      f.m = L.m[s2];
+      f.n = L.n[s2];
+      f.fidx = q;
+      f.var_off = L.var_off[s2];
+      f.d_off = L.d_off[s2];
+      f.nblk = (f.n == 0 || f.n <= tpp_cols) ? 0 : ceil_div(f.n, LDLT_BW);
+      f.p = 0;
+      f.pan_off = scr;
+      scr += (int64_t)f.m * LDLT_BW;
+      f.ldp_off = scr;
+      scr += (int64_t)f.m * LDLT_BW;
+      f.mv_off = scr;
+      scr += f.nblk > 0 ? (int64_t)f.m * f.n : 0;
+      scr = round_up64(scr, 32);
+      f.mvvar_off = (int)ivar;
+      ivar += f.n;
+      maxblk = std::max(maxblk, f.nblk);
+    }
+    if (L.sc.bytes < (size_t)std::max<int64_t>(scr, 1) * sizeof(T))
       L.sc.ensure((size_t)std::max<int64_t>(scr, 1) * sizeof(T));
-      put(L.fr, fr, s);
-      std::vector<int> init_np(nslot, LDLT_BW);
-      for (auto& f : fr) init_np[f.fidx] = f.w;
-      put(L.npass_raw, init_np, s);
-      L.npass_raw.ensure((size_t)nslot * sizeof(int));
-      stp.npass_raw = L.npass_raw.as<int>();
-      // apply row tiles (rows below the block)
-      std::vector<RowTask> at;
-      for (int k = 0; k < (int)fr.size(); ++k)
-        for (int r0 = fr[k].p + fr[k].w; r0 < fr[k].m; r0 += LDLT_RT) at.push_back({k, r0});
-      launch_ldlt_diag<T>(A, L.fr.as<LdltFront>(), (int)fr.size(), stp, s);
-      launches++;
-      if (!at.empty()) {
-        put(L.rt, at, s);
-        launch_ldlt_apply<T>(A, L.sc.as<T>(), L.fr.as<LdltFront>(), L.rt.as<RowTask>(),
-                             (int)at.size(), stp, s);
-        launches++;
-      }
-      hraw.resize(nslot);
-      hdv.resize((size_t)nslot * 2 * LDLT_BW);
-      SG_CUDA(cudaMemcpyAsync(hraw.data(), L.npass_raw.p, nslot * sizeof(int),
-                              cudaMemcpyDeviceToHost, s));
-      SG_CUDA(cudaMemcpyAsync(hdv.data(), L.bdinv.p, hdv.size() * sizeof(double),
-                              cudaMemcpyDeviceToHost, s));
-      SG_CUDA(cudaStreamSynchronize(s));
-      // drop a 2x2 pivot split by the threshold failure (Column::adjust)
-      hnp.assign(nslot, 0);
-      for (auto& f : fr) {
-        int np = std::min(hraw[f.fidx], f.w);
-        const double* d = &hdv[(size_t)f.fidx * 2 * LDLT_BW];
-        if (np > 0 && std::isfinite(d[2 * (np - 1)]) && d[2 * (np - 1) + 1] != 0.0) np--;
-        hnp[f.fidx] = np;
-      }
-      put(L.npass, hnp, s);
-      stp.npass = L.npass.as<int>();
-      // commit rows [p, m)
-      std::vector<RowTask> ct;
-      for (int k = 0; k < (int)fr.size(); ++k)
-        for (int r0 = fr[k].p; r0 < fr[k].m; r0 += LDLT_RT) ct.push_back({k, r0});
-      put(L.rt, ct, s);
-      launch_ldlt_commit<T>(A, L.sc.as<T>(), L.fr.as<LdltFront>(), L.rt.as<RowTask>(),
-                            (int)ct.size(), stp, s);
-      launches++;
-      // trailing update of the fully-summed part
-      std::vector<UpdTask> ut;
-      for (auto& f : fr) {
-        int np = hnp[f.fidx];
-        if (np == 0) continue;
-        int o = f.p + np;
-        for (int cj = 0; o + cj * TM < f.n; ++cj)
-          for (int ri = cj; o + ri * TM < f.m; ++ri)
-            ut.push_back({f.off, f.ldp_off, f.off + (int64_t)f.p * f.ld, f.ld, f.m, f.ld,
-                          o + ri * TM, o + cj * TM, f.m, f.n, 0, np, 0});
-      }
-      if (!ut.empty()) {
-        put(L.up, ut, s);
-        launch_update<T>(A, L.sc.as<T>(), L.up.as<UpdTask>(), (int)ut.size(), s);
-        launches++;
-      }
-      for (auto& f : fr) {
-        int q = f.fidx, np = hnp[q];
-        p[q] += np;
-        fk.not_first_pass += 0;
-        if (np == 0 || p[q] >= L.n[F[q]]) app_done[q] = 1;
+    L.mvvar.ensure((size_t)std::max<int64_t>(ivar, 1) * sizeof(int));
+    put(L.fr, fr, s);
+    // per-step CTA maps: diag, apply, commit, update, move
+    std::vector<CtaMap> maps;
+    struct StepMaps { int64_t o[5]; int n[5]; };
+    std::vector<StepMaps> sm(maxblk);
+    for (int k = 0; k < maxblk; ++k) {
+      for (int kind = 0; kind < 5; ++kind) {
+        sm[k].o[kind] = (int64_t)maps.size();
+        for (int q = 0; q < nslot; ++q) {
+          const LdltFront& f = fr[q];
+          if (f.nblk <= k) continue;
+          const int w = std::min(LDLT_BW, f.n - LDLT_BW * k);
+          const int p0 = LDLT_BW * k;  // block start when nothing failed so far
+          int cnt = 1;
+          if (kind == 1) cnt = ceil_div(std::max(f.m - p0 - w, 1), LDLT_RT);
+          if (kind == 2) cnt = ceil_div(f.m - p0, LDLT_RT);
+          if (kind == 3) {
+            const int o = std::min(p0 + w, f.n - 1);
+            const int R = ceil_div(f.m - o, TM), C = ceil_div(f.n - o, TM);
+            cnt = C * R - C * (C - 1) / 2;
+          }
+          if (kind == 4) cnt = ceil_div(f.n, 8);
+          add_slice(maps, q, cnt);
+        }
+        sm[k].n[kind] = (int)((int64_t)maps.size() - sm[k].o[kind]);
       }
     }
-    // ---- threshold partial pivoting on what the blocks did not accept
-    for (int pass = 0; pass < 2; ++pass) {
-      std::vector<LdltFront> fr;
-      for (int q = 0; q < nslot; ++q) {
-        int s2 = F[q];
-        if (p[q] >= L.n[s2]) continue;
-        bool root = st.sparent[s2] - 1 >= ns;
-        if (pass == 1 && !root) continue;
-        LdltFront f{};
-        f.off = L.off[s2];
-        f.ld = L.ld[s2];
-        f.m = L.m[s2];
-        f.n = L.n[s2];
-        f.p = p[q];
-        f.fidx = q;
-        f.var_off = L.var_off[s2];
-        f.d_off = L.d_off[s2];
-        fr.push_back(f);
-        if (pass == 0) fk.not_first_pass += L.n[s2] - p[q];
-        else fk.not_second_pass += L.n[s2] - p[q];
-      }
-      if (fr.empty()) continue;
-      put(L.fr, fr, s);
-      // nothing above a root can take delays: its second pass keeps only the
-      // small-pivot test (plain partial pivoting)
-      double ueff = pass == 0 ? u : 1e-300;
-      launch_ldlt_tpp<T>(A, L.fr.as<LdltFront>(), (int)fr.size(), stp, ueff, L.tppo.as<int>(), s);
-      launches++;
-      std::vector<int> out(nslot);
-      SG_CUDA(cudaMemcpyAsync(out.data(), L.tppo.p, nslot * sizeof(int), cudaMemcpyDeviceToHost,
-                              s));
-      SG_CUDA(cudaStreamSynchronize(s));
-      for (auto& f : fr) p[f.fidx] = out[f.fidx];
+    put(L.cmap, maps, s);
+    // per-slot step buffers and state (p/nf ping-pong, p_final)
+    L.blk.ensure((size_t)std::max(nslot, 1) * LDLT_BW * (LDLT_BW + 1) * sizeof(double));
+    L.bdinv.ensure((size_t)std::max(nslot, 1) * 2 * LDLT_BW * sizeof(double));
+    L.lperm.ensure((size_t)std::max(nslot, 1) * LDLT_BW * sizeof(int));
+    L.state.ensure((size_t)std::max(nslot, 1) * 10 * sizeof(int));
+    SG_CUDA(cudaMemsetAsync(L.state.p, 0, (size_t)std::max(nslot, 1) * 10 * sizeof(int), s));
+    int* stt = L.state.as<int>();
+    int* Pbuf[2] = {stt, stt + nslot};
+    int* NFbuf[2] = {stt + 2 * nslot, stt + 3 * nslot};
+    int* p_final = stt + 4 * nslot;
+    int* ndiag = stt + 5 * nslot;
+    int* npass_raw = stt + 6 * nslot;
+    int* npass = stt + 7 * nslot;
+    int* tpp1 = stt + 8 * nslot;
+    int* tpp2 = stt + 9 * nslot;
+    LdltStep stp{L.blk.as<double>(), L.bdinv.as<double>(), L.lperm.as<int>(), ndiag, npass_raw,
+                 npass, nullptr, nullptr, nullptr, nullptr, p_final, dvar, L.mvvar.as<int>(),
+                 L.dall.as<double>(), status, fk.u, fk.small_piv, fk.action ? 1 : 0, 0};
+    const LdltFront* dfr = L.fr.as<LdltFront>();
+    const CtaMap* dcm = L.cmap.as<CtaMap>();
+    T* sc = L.sc.as<T>();
+    // ---- a-posteriori block steps
+    for (int k = 0; k < maxblk; ++k) {
+      stp.k = k;
+      stp.p_cur = Pbuf[k & 1];
+      stp.nf_cur = NFbuf[k & 1];
+      stp.p_next = Pbuf[(k + 1) & 1];
+      stp.nf_next = NFbuf[(k + 1) & 1];
+      launch_app_diag<T>(A, sc, dfr, dcm + sm[k].o[0], sm[k].n[0], stp, s);
+      launch_app_apply<T>(A, sc, dfr, dcm + sm[k].o[1], sm[k].n[1], stp, s);
+      launch_app_commit<T>(A, sc, dfr, dcm + sm[k].o[2], sm[k].n[2], stp, s);
+      launch_app_update<T>(A, sc, dfr, dcm + sm[k].o[3], sm[k].n[3], stp, s);
+      launch_app_move<T>(A, sc, dfr, dcm + sm[k].o[4], sm[k].n[4], stp, s);
+      launches += 6;
     }
-    for (int q = 0; q < nslot; ++q) L.nelim[F[q]] = p[q];
+    // ---- threshold partial pivoting on what the block steps did not take;
+    // at a root nothing can take delays, so a second pass keeps only the
+    // small-pivot test (plain partial pivoting)
+    launch_ldlt_tpp<T>(A, dfr, nslot, stp, fk.u, p_final, tpp1, s);
+    SG_CUDA(cudaMemcpyAsync(tpp2, tpp1, nslot * sizeof(int), cudaMemcpyDeviceToDevice, s));
+    std::vector<LdltFront> roots;
+    for (int q = 0; q < nslot; ++q)
+      if (st.sparent[F[q]] - 1 >= ns) roots.push_back(fr[q]);
+    if (!roots.empty()) {
+      put(L.fr2, roots, s);
+      launch_ldlt_tpp<T>(A, L.fr2.as<LdltFront>(), (int)roots.size(), stp, kRootU, tpp1, tpp2,
+                         s);
+      launches++;
+    }
+    launches += 1;
+    // ---- the level's one host synchronisation: eliminated counts and the
+    // (pivoted) variable lists for the parents' maps
+    std::vector<int> h(3 * nslot);
+    SG_CUDA(cudaMemcpyAsync(h.data(), p_final, nslot * sizeof(int), cudaMemcpyDeviceToHost, s));
+    SG_CUDA(cudaMemcpyAsync(h.data() + nslot, tpp1, 2 * nslot * sizeof(int),
+                            cudaMemcpyDeviceToHost, s));
+    if (!hvar_lvl.empty())
+      SG_CUDA(cudaMemcpyAsync(hvar_lvl.data(), dvar + L.var_off[F[0]],
+                              hvar_lvl.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
+    SG_CUDA(cudaStreamSynchronize(s));
+    {
+      size_t o = 0;
+      for (int s2 : F) {
+        std::copy(hvar_lvl.begin() + o, hvar_lvl.begin() + o + L.m[s2], L.var[s2].begin());
+        o += L.m[s2];
+      }
+    }
+    for (int q = 0; q < nslot; ++q) {
+      const int s2 = F[q], nn = L.n[s2];
+      const int pf = h[q], t1 = h[nslot + q], t2 = h[2 * nslot + q];
+      L.nelim[s2] = t2;
+      // src/factor_failed.hxx:58-59, :115-120 (pivot_method tpp for fronts
+      // that skip the block steps)
+      if (fr[q].nblk > 0) {
+        fk.not_first_pass += nn - pf;
+        if (pf < nn) fk.not_second_pass += nn - t1;
+      } else {
+        fk.not_first_pass += nn - t1;
+      }
+      fk.num_delay += nn - t2;
+    }
     // ---- contribution blocks: CB -= (L D) L^T over all eliminated columns
     {
-      std::vector<LdltFront> fr;
-      std::vector<RowTask> rt;
+      std::vector<LdltFront> cfr;
+      std::vector<CtaMap> cm;
       std::vector<UpdTask> ut;
-      int64_t scr = 0;
+      int64_t cscr = 0;
       for (int q = 0; q < nslot; ++q) {
         int s2 = F[q];
         int m = L.m[s2], n = L.n[s2], ne = L.nelim[s2];
         if (m <= n || ne == 0) continue;
-        LdltFront f{};
-        f.off = L.off[s2];
-        f.ld = L.ld[s2];
-        f.m = m;
-        f.n = n;
+        LdltFront f = fr[q];
         f.p = ne;
-        f.fidx = q;
-        f.d_off = L.d_off[s2];
-        f.ldp_off = scr;
-        scr += (int64_t)m * ne;
-        int k = (int)fr.size();
-        fr.push_back(f);
-        for (int r0 = n; r0 < m; r0 += LDLT_RT) rt.push_back({k, r0});
+        f.ldp_off = cscr;
+        cscr += (int64_t)m * ne;
+        int kf = (int)cfr.size();
+        cfr.push_back(f);
+        add_slice(cm, kf, ceil_div(m - n, LDLT_RT));
         for (int cj = 0; n + cj * TM < m; ++cj)
           for (int ri = cj; n + ri * TM < m; ++ri)
             ut.push_back({f.off, f.ldp_off, f.off, f.ld, m, f.ld, n + ri * TM, n + cj * TM, m, m,
                           0, ne, 0});
       }
-      if (!fr.empty()) {
-        L.sc.ensure((size_t)std::max<int64_t>(scr, 1) * sizeof(T));
-        put(L.fr, fr, s);
-        put(L.rt, rt, s);
+      if (!cfr.empty()) {
+        if (L.sc2.bytes < (size_t)std::max<int64_t>(cscr, 1) * sizeof(T))
+          L.sc2.ensure((size_t)std::max<int64_t>(cscr, 1) * sizeof(T));
+        put(L.fr2, cfr, s);
+        put(L.cmap2, cm, s);
         put(L.up, ut, s);
-        launch_ldlt_calc_ld<T>(A, L.sc.as<T>(), L.fr.as<LdltFront>(), L.rt.as<RowTask>(),
-                               (int)rt.size(), stp, s);
-        launch_update<T>(A, L.sc.as<T>(), L.up.as<UpdTask>(), (int)ut.size(), s);
+        launch_ldlt_calc_ld<T>(A, L.sc2.as<T>(), L.fr2.as<LdltFront>(), L.cmap2.as<CtaMap>(),
+                               (int)cm.size(), stp, s);
+        launch_update<T>(A, L.sc2.as<T>(), L.up.as<UpdTask>(), (int)ut.size(), s);
         launches += 2;
-      }
-    }
-    // ---- bring the (pivoted) variable lists back for the parents' maps
-    if (!hvar_lvl.empty()) {
-      SG_CUDA(cudaMemcpyAsync(hvar_lvl.data(), dvar + L.var_off[F[0]],
-                              hvar_lvl.size() * sizeof(int), cudaMemcpyDeviceToHost, s));
-      SG_CUDA(cudaStreamSynchronize(s));
-      size_t o = 0;
-      for (int s2 : F) {
-        std::copy(hvar_lvl.begin() + o, hvar_lvl.begin() + o + L.m[s2], L.var[s2].begin());
-        o += L.m[s2];
       }
     }
   }
@@ -421,7 +449,7 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   SG_CUDA(cudaMemcpyAsync(&sth, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   SG_CUDA(cudaStreamSynchronize(s));
   fk.launches = launches;
-  fk.num_neg = fk.num_two = fk.num_zero = fk.num_delay = 0;
+  fk.num_neg = fk.num_two = fk.num_zero = 0;
   fk.num_factor = 0;
   int rank = 0;
   int uneliminated = 0;
@@ -429,8 +457,7 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
     const double* d = &D[L.d_off[s2]];
     int ne = L.nelim[s2];
     fk.num_factor += (int64_t)ne * L.m[s2] - (int64_t)ne * (ne - 1) / 2;
-    if (st.sparent[s2] - 1 < ns) fk.num_delay += L.n[s2] - ne;
-    else uneliminated += L.n[s2] - ne;
+    if (st.sparent[s2] - 1 >= ns) uneliminated += L.n[s2] - ne;
     for (int i = 0; i < ne;) {
       double a11 = d[2 * i], a21 = d[2 * i + 1];
       if (i + 1 == ne || std::isfinite(d[2 * i + 2])) {
@@ -585,6 +612,18 @@ int ldlt_export_diag(const FKeep& fk, double* d, int* piv_order) {
       k++;
     }
   return k;
+}
+
+int ldlt_export_fronts(const FKeep& fk, int* m, int* n, int* nelim) {
+  if (!fk.ldlt) return 0;
+  const LdltState& L = *fk.ldlt;
+  const int ns = (int)L.nelim.size();
+  for (int s = 0; s < ns; ++s) {
+    if (m) m[s] = L.m[s];
+    if (n) n[s] = L.n[s];
+    if (nelim) nelim[s] = L.nelim[s];
+  }
+  return ns;
 }
 
 }  // namespace sylver_gb300

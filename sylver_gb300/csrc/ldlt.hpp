@@ -11,6 +11,7 @@ int factorize_ldlt(FKeep& fk, const double* val_dev, cudaStream_t s);
 void ldlt_solve_pivot_order(FKeep& fk, int job, float* xp, int nrhs, cudaStream_t s);
 void ldlt_solve_pivot_order(FKeep& fk, int job, double* xp, int nrhs, cudaStream_t s);
 int ldlt_export_diag(const FKeep& fk, double* d, int* piv_order);
+int ldlt_export_fronts(const FKeep& fk, int* m, int* n, int* nelim);
 // Device tables of the forward solve of an LDL^T factorization (level-ordered
 // front descriptors, slab offsets, row-variable lists) and the largest
 // per-level slab row count; false before a factorization.

@@ -20,6 +20,9 @@ LIB = os.path.join(BUILD, "libsylver_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr", "-I", os.path.join(HERE, "..", "include")]
+# LDL^T kernels: no multiply-add contraction (every fused multiply-add there
+# is written out, in an order a CPU restatement can repeat bit for bit)
+FILE_FLAGS = {"kernels_ldlt.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -37,8 +40,8 @@ def _stale(obj: str, src: str) -> bool:
     if not os.path.exists(obj):
         return True
     t = os.path.getmtime(obj)
-    deps = [src] + glob.glob(os.path.join(CSRC, "*.hpp")) + glob.glob(
-        os.path.join(HERE, "..", "include", "*.h"))
+    deps = [src, os.path.abspath(__file__)] + glob.glob(os.path.join(CSRC, "*.hpp")) + \
+        glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(HERE, "..", "include", "*.h"))
     return any(os.path.getmtime(d) > t for d in deps)
 
 
@@ -52,7 +55,8 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
         o = os.path.join(BUILD, os.path.basename(s) + ".o")
         objs.append(o)
         if force or _stale(o, s):
-            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *(extra or []), "-c", s, "-o", o]
+            cmd = [nvcc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(os.path.basename(s), []),
+                   *(extra or []), "-c", s, "-o", o]
             jobs.append(cmd)
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:

@@ -82,3 +82,69 @@ def test_oracle_inertia_closed_form_full_size_small(sylver, orc):
     o = orc.OracleFactor(False, an.symbolic(), p.a.val, u=U)
     assert o.stats["num_neg"] == p.inertia[0]
     assert o.stats["num_zero"] == 0
+
+
+def _cause_delays_sparse(k=8, seed=3):
+    """The reference's cause_delays idea (tests/common.hxx:753-790) on a
+    sparse matrix: n/8 rows/columns scaled by 1000 with small diagonals."""
+    rng = np.random.default_rng(seed)
+    p = w.shifted_laplace3d(k, nrhs=1)
+    full = p.a.to_scipy_full().tolil()
+    n = p.a.n
+    for idx in rng.choice(n, size=n // 8, replace=False):
+        full[idx, :] = full[idx, :] * 1000.0
+        full[:, idx] = full[:, idx] * 1000.0
+    full = full.tocsr()
+    for idx in range(n):
+        if abs(full[idx, idx]) > 100:
+            full[idx, idx] = full[idx, idx] * 1e-6
+    return w.SymMatrix.from_scipy(full), p.order
+
+
+@pytest.mark.parametrize("case", ["dense_indef_64", "dense_indef_delays_96", "kkt_4",
+                                  "shifted_laplace3d_9", "cause_delays", "kkt6"])
+@pytest.mark.parametrize("u", [0.01, 0.3])
+def test_oracle_app_layout_matches_reference_layout(sylver, orc, case, u):
+    """The oracle moves a block's failed columns behind the unprocessed ones
+    at once; the reference leaves them in place, reaches them through the
+    blocks to their left (ApplyT/UpdateT) and permutes them to the back at
+    the end (src/factor_indef.hxx:885-1288).  Both restatements, same
+    arithmetic, must give the same factors bit for bit."""
+    if case == "cause_delays":
+        a, order = _cause_delays_sparse()
+    elif case == "kkt6":
+        p = w.kkt(6, nrhs=1)
+        a = p.a
+        order = sylver.Analysis(a.n, a.ptr, a.row).symbolic()["perm"]
+    else:
+        g = load_golden(case)
+        a, order = w.SymMatrix(g["n"], g["ptr"], g["row"], g["val"]), g["order"]
+    an = sylver.Analysis(a.n, a.ptr, a.row, order=order)
+    sy = an.symbolic()
+    o1 = orc.OracleFactor(False, sy, a.val, u=u)
+    o2 = orc.OracleFactor(False, sy, a.val, u=u, inplace=True)
+    assert o1.stats == o2.stats
+    for s in range(sy["nnodes"]):
+        f1, f2 = o1.front(s), o2.front(s)
+        assert (f1["m"], f1["n"], f1["nelim"]) == (f2["m"], f2["n"], f2["nelim"])
+        np.testing.assert_array_equal(f1["var"], f2["var"])
+        ne = f1["nelim"]
+        assert np.array_equal(f1["d"][:2 * ne], f2["d"][:2 * ne])
+        assert np.array_equal(np.tril(f1["a"]), np.tril(f2["a"]))
+
+
+def test_oracle_app_fails_and_delays(sylver, orc):
+    """The block steps leave columns to the threshold partial pivoting pass
+    (not_first_pass) and some of those are delayed to parents."""
+    a, order = _cause_delays_sparse()
+    an = sylver.Analysis(a.n, a.ptr, a.row, order=order)
+    o = orc.OracleFactor(False, an.symbolic(), a.val, u=0.01)
+    assert o.stats["not_first_pass"] > 0
+    assert o.stats["num_delay"] > 0
+    full = a.to_scipy_full()
+    ev = np.linalg.eigvalsh(full.toarray())
+    assert o.stats["num_neg"] == int(np.sum(ev < 0))
+    b = np.random.default_rng(5).standard_normal((a.n, 1))
+    x = o.solve(b)
+    x = x + o.solve(b - full @ x)
+    assert w.backward_error(full, x, b).max() <= 1e-14
