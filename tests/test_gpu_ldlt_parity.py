@@ -224,4 +224,4 @@ def test_config1_laplace2d_100(sylver, orc, gpu, precision):
     o = orc.OracleFactor(True, an.symbolic(), p.a.val)
     xo = o.solve(p.rhs)
     assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
-    assert np.abs(x[:, 0] - p.x_true).max() <= 1e-10
+    assert np.abs(x - p.x_true.reshape(x.shape)).max() <= 1e-10
