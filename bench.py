@@ -48,6 +48,9 @@ def parse():
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--tol", type=float, default=1e-14)
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-ldlt", action="store_true",
+                    help="skip the indefinite (shifted 7-point 48^3) factor + solve leg")
+    ap.add_argument("--ldlt-k", type=int, default=48)
     ap.add_argument("--cpu-sample-k", type=int, default=0,
                     help="grid edge of the CPU baseline sample (0: auto)")
     return ap.parse_args()
@@ -206,8 +209,8 @@ def run_ours(args, rank, ws):
         sinf = sg.Inform()
         lib.spldlt_solve_device(0, nrhs, P(x_d.data_ptr()), n, an.akeep, fkeep,
                                 ctypes.byref(opts), ctypes.byref(sinf))
-        if sinf.flag < 0:
-            raise RuntimeError(f"solve failed {sinf.flag}")
+        if sinf.flag != 0:
+            raise RuntimeError(f"solve flag {sinf.flag} (not converged or failed)")
 
     def timed(fn, steps, warm):
         for _ in range(warm):
@@ -256,9 +259,11 @@ def run_ours(args, rank, ws):
         sinf = sg.Inform()
         lib.spldlt_solve(0, nrhs, x_host.ctypes.data_as(P), n, an.akeep, f2, ctypes.byref(opts),
                          ctypes.byref(sinf))
+        if sinf.flag != 0:
+            raise RuntimeError(f"solve flag {sinf.flag}")
 
-    e2e_steps = max(1, min(args.steps, 3))
-    t_e2e, wall_e2e = timed(step_e2e, e2e_steps, 1)
+    e2e_steps = args.steps
+    t_e2e, wall_e2e = timed(step_e2e, e2e_steps, args.warmup)
     be_e2e = float(w.backward_error(full, x_host, prob.rhs).max())
     lib.spldlt_free_fkeep(ctypes.byref(f2))
 
@@ -302,6 +307,8 @@ def run_ours(args, rank, ws):
                 "fp32_speedup": round(t64 / (t_dev / args.steps), 2)}
         lib.spldlt_free_fkeep(ctypes.byref(f3))
 
+    ldlt = ldlt_leg(args, lib, stream) if (rank == 0 and not args.no_ldlt) else None
+
     t_step = allmax(t_dev / args.steps, ws)
     t_e2e_step = allmax(t_e2e / e2e_steps, ws)
     launches_step = int(nl.value) + 0
@@ -342,16 +349,79 @@ def run_ours(args, rank, ws):
                      "traffic_unit": "bytes per launch (dram read + write)",
                      "traffic_source": ("one-pass ncu capture of every launch at this size, "
                                         "profiles/traffic_lognormal27_80.json") if trec else None,
-                     "time_share": round(float(ms[dom] / max(ms.sum(), 1e-9)), 3)},
+                     "share_of_profiled_factorization": round(float(ms[dom] / max(ms.sum(), 1e-9)), 3),
+                     "share_of_step": round(float(ms[dom]) / (t_dev / args.steps * 1e3), 3)},
         "kernel_profile_ms": prof,
         "accuracy": {"ir_iters": it.value, "bwd_err_device": be.value,
                      "bwd_err_host_check": be_host},
         "fp64_gpu_path": fp64,
+        "ldlt_config2": ldlt,
         "clocks": clk.summary(),
         "gpu_launches": int(launches_step * args.steps),
         "cpu_baseline": cpu,
     }
     lib.spldlt_free_fkeep(ctypes.byref(fkeep))
+    return out
+
+
+def ldlt_leg(args, lib, stream):
+    """Indefinite LDL^T on the shifted 7-point Laplacian (k^3 minus sigma*I,
+    4 right-hand sides, APP threshold u = 0.01): factor + refined solve per
+    step, device-resident values and right-hand sides, CUDA events on the
+    library stream; FP32 factors + FP64 refinement and plain FP64 factors.
+    Reported beside the headline; not part of its timed region."""
+    import torch
+    import sylver_gb300 as sg
+    from sylver_gb300 import workloads as w
+    p = w.shifted_laplace3d(args.ldlt_k, nrhs=4)
+    a = p.a
+    an = sg.Analysis(a.n, a.ptr, a.row, order=p.order)
+    flops = float(an.inform.num_flops)
+    n, nrhs = a.n, 4
+    val_d = torch.from_numpy(a.val).cuda()
+    b_d = torch.from_numpy(np.ascontiguousarray(p.rhs.T)).cuda()
+    x_d = torch.empty_like(b_d)
+    opts = sg.default_options()
+    P = ctypes.c_void_p
+    full = a.to_scipy_full()
+    out = {"workload": f"shifted 7-point Laplacian {args.ldlt_k}^3 minus sigma*I, n={n}, "
+                       f"nrhs={nrhs}, APP u=0.01", "factor_flops": flops}
+    for name, prec in (("fp32_ir", sg.FP32), ("fp64", sg.FP64)):
+        fk = ctypes.c_void_p()
+        inf = sg.Inform()
+        tf = ts = 0.0
+        steps = 3
+        for it in range(steps + 1):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            torch.cuda.synchronize()
+            e[0].record(stream)
+            lib.spldlt_factorize_device(False, P(val_d.data_ptr()), an.akeep, ctypes.byref(fk),
+                                        ctypes.byref(opts), ctypes.byref(inf), prec, 1e-14, 20)
+            e[1].record(stream)
+            with torch.cuda.stream(stream):
+                x_d.copy_(b_d)
+            sinf = sg.Inform()
+            lib.spldlt_solve_device(0, nrhs, P(x_d.data_ptr()), n, an.akeep, fk,
+                                    ctypes.byref(opts), ctypes.byref(sinf))
+            e[2].record(stream)
+            torch.cuda.synchronize()
+            if it > 0:
+                tf += e[0].elapsed_time(e[1]) / steps
+                ts += e[1].elapsed_time(e[2]) / steps
+        it_, be = ctypes.c_int(), ctypes.c_double()
+        lib.sylver_gb300_solve_stats(fk, ctypes.byref(it_), ctypes.byref(be))
+        x = x_d.cpu().numpy().T
+        out[name] = {"factor_ms": round(tf, 3), "solve_ms": round(ts, 3),
+                     "gflops": round(flops / ((tf + ts) * 1e-3) / 1e9, 1),
+                     "ir_iters": it_.value,
+                     "bwd_err_host_check": float(w.backward_error(full, np.asfortranarray(x),
+                                                                  p.rhs).max()),
+                     "inertia": [inf.num_neg, n - inf.matrix_rank, inf.matrix_rank - inf.num_neg],
+                     "num_delay": inf.num_delay, "num_two": inf.num_two}
+        lib.spldlt_free_fkeep(ctypes.byref(fk))
+    out["inertia_closed_form"] = list(p.inertia)
+    out["fp32_speedup_vs_fp64"] = round((out["fp64"]["factor_ms"] + out["fp64"]["solve_ms"]) /
+                                        (out["fp32_ir"]["factor_ms"] + out["fp32_ir"]["solve_ms"]), 2)
     return out
 
 

@@ -52,6 +52,8 @@ constexpr int LDB = BW + 1;
 
 __device__ __forceinline__ double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fma_(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float mul_(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double dinf() { return __longlong_as_double(0x7ff0000000000000LL); }
 
 __device__ __forceinline__ int block_width(const LdltFront& F, int k) {
@@ -65,9 +67,10 @@ __device__ __forceinline__ int extra_rows(const LdltFront& F, int w) {
 
 // Warp-wide argmax of v over lanes (first maximum: lowest index on ties);
 // lanes with nothing to offer pass v = -1, idx = -1.
-__device__ __forceinline__ void warp_argmax(double& v, int& idx) {
+template <typename C>
+__device__ __forceinline__ void warp_argmax(C& v, int& idx) {
   for (int o = 16; o > 0; o >>= 1) {
-    double ov = __shfl_xor_sync(0xffffffffu, v, o);
+    C ov = __shfl_xor_sync(0xffffffffu, v, o);
     int oi = __shfl_xor_sync(0xffffffffu, idx, o);
     if (ov > v || (ov == v && oi >= 0 && (idx < 0 || oi < idx))) {
       v = ov;
@@ -91,7 +94,8 @@ template <typename T>
 __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __restrict__ scratch,
                                                   const LdltFront* __restrict__ fr,
                                                   const CtaMap* __restrict__ cm, LdltStep st) {
-  __shared__ double a[BW][LDB];  // a[j][i] = panel(i, j); i >= j, or i >= w (extra rows)
+  using C = T;  // block arithmetic; FP64 for the pivot tests and 2x2 inverses
+  __shared__ C a[BW][LDB];  // a[j][i] = panel(i, j); i >= j, or i >= w (extra rows)
   __shared__ double dv[2 * BW];
   __shared__ int perm[BW];
   __shared__ int s_nd;
@@ -104,7 +108,7 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
   auto prow = [&](int i) { return i < w ? p + i : F.n + (i - w); };  // panel row -> front row
   for (int idx = tid; idx < R * w; idx += blockDim.x) {
     int i = idx % R, j = idx / R;
-    if (i >= j) a[j][i] = (double)A[(int64_t)(p + j) * ld + prow(i)];
+    if (i >= j) a[j][i] = (C)A[(int64_t)(p + j) * ld + prow(i)];
   }
   if (tid < BW) perm[tid] = tid;
   if (tid < 2 * BW) dv[tid] = 0.0;
@@ -116,7 +120,7 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
       if (x > y) { int t = x; x = y; y = t; }
       int kk = lane;
       if (kk < R) {
-        double t;
+        C t;
         if (kk < x) { t = a[kk][x]; a[kk][x] = a[kk][y]; a[kk][y] = t; }
         else if (kk == x) { t = a[x][x]; a[x][x] = a[y][y]; a[y][y] = t; }
         else if (kk < y) { t = a[x][kk]; a[x][kk] = a[kk][y]; a[kk][y] = t; }
@@ -127,17 +131,17 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
     };
     // 1x1 pivot at s: candidate columns (s, cend), rows [j, R)
     auto elim1 = [&](int s, int cend) {
-      const double di = 1.0 / a[s][s];
+      const C di = C(1) / a[s][s];
       const int j = lane;
       if (j > s && j < cend) {
-        const double lj = mul_(a[s][j], di);
+        const C lj = mul_(a[s][j], di);
         for (int i = j; i < R; ++i) a[j][i] = fma_(-a[s][i], lj, a[j][i]);
       }
       __syncwarp();
       if (lane > s && lane < R) a[s][lane] = mul_(a[s][lane], di);
       if (lane == 0) {
-        a[s][s] = 1.0;
-        dv[2 * s] = di;
+        a[s][s] = C(1);
+        dv[2 * s] = (double)di;
         dv[2 * s + 1] = 0.0;
       }
       __syncwarp();
@@ -150,19 +154,19 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
       const int j = lane;
       if (j > s + 1 && j < cend) {
         const double w1 = a[s][j], w2 = a[s + 1][j];
-        const double l1 = fma_(i11, w1, mul_(i12, w2)), l2 = fma_(i12, w1, mul_(i22, w2));
+        const C l1 = (C)fma_(i11, w1, mul_(i12, w2)), l2 = (C)fma_(i12, w1, mul_(i22, w2));
         for (int i = j; i < R; ++i) a[j][i] = fma_(-a[s + 1][i], l2, fma_(-a[s][i], l1, a[j][i]));
       }
       __syncwarp();
       if (lane > s + 1 && lane < R) {
         const double w1 = a[s][lane], w2 = a[s + 1][lane];
-        a[s][lane] = fma_(i11, w1, mul_(i12, w2));
-        a[s + 1][lane] = fma_(i12, w1, mul_(i22, w2));
+        a[s][lane] = (C)fma_(i11, w1, mul_(i12, w2));
+        a[s + 1][lane] = (C)fma_(i12, w1, mul_(i22, w2));
       }
       if (lane == 0) {
-        a[s][s] = 1.0;
-        a[s][s + 1] = 0.0;
-        a[s + 1][s + 1] = 1.0;
+        a[s][s] = C(1);
+        a[s][s + 1] = C(0);
+        a[s + 1][s + 1] = C(1);
         dv[2 * s] = i11;
         dv[2 * s + 1] = i12;
         dv[2 * s + 2] = dinf();
@@ -172,7 +176,7 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
     };
     // zero pivot at s: column of L is zero
     auto elim0 = [&](int s) {
-      if (lane >= s && lane < R) a[s][lane] = (lane == s) ? 1.0 : 0.0;
+      if (lane >= s && lane < R) a[s][lane] = (lane == s) ? C(1) : C(0);
       if (lane == 0) {
         dv[2 * s] = 0.0;
         dv[2 * s + 1] = 0.0;
@@ -184,15 +188,15 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
     if (w == BW) {
       // ---- complete pivoting (block_ldlt)
       while (s < w) {
-        double best = -1.0;
+        C best = C(-1);
         int bi = -1, bj = -1;
         if (lane >= s && lane < w)
           for (int i = lane; i < w; ++i) {
-            double v = fabs(a[lane][i]);
+            C v = fabs(a[lane][i]);
             if (v > best) { best = v; bi = i; bj = lane; }
           }
         for (int o = 16; o > 0; o >>= 1) {
-          double ob = __shfl_xor_sync(0xffffffffu, best, o);
+          C ob = __shfl_xor_sync(0xffffffffu, best, o);
           int oi = __shfl_xor_sync(0xffffffffu, bi, o);
           int oj = __shfl_xor_sync(0xffffffffu, bj, o);
           if (ob > best || (ob == best && (oj < bj || (oj == bj && oi < bi)))) {
@@ -203,7 +207,7 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
         if (!(amax >= st.small)) {
           // the rest of the block is (numerically) zero: zero pivots
           for (int kk = s; kk < w; ++kk) {
-            if (lane >= kk && lane < w) a[kk][lane] = (lane == kk) ? 1.0 : 0.0;
+            if (lane >= kk && lane < w) a[kk][lane] = (lane == kk) ? C(1) : C(0);
             if (lane == 0) { dv[2 * kk] = 0.0; dv[2 * kk + 1] = 0.0; }
           }
           if (lane == 0) atomicOr(st.status, st.action ? ST_ZERO_PIVOT : ST_SINGULAR);
@@ -215,7 +219,7 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
         bool two = false;
         int piv = t;
         if (t != qq) {
-          double dt = fabs(a[t][t]), dq = fabs(a[qq][qq]);
+          double dt = fabs((double)a[t][t]), dq = fabs((double)a[qq][qq]);
           if (fmax(dt, dq) >= mul_(st.u, amax)) piv = (dt >= dq) ? t : qq;
           else two = true;
         }
@@ -236,14 +240,14 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
       while (s < w) {
         int decided = 0, piv = -1, tpiv = -1;
         for (int c = s; c < w && !decided; ++c) {
-          auto colv = [&](int i, int col) { return i > col ? a[col][i] : a[i][col]; };
+          auto colv = [&](int i, int col) -> double { return i > col ? a[col][i] : a[i][col]; };
           double v = -1.0;
           int vi = -1;
           if (lane >= s && lane < R && lane != c) { v = fabs(colv(lane, c)); vi = lane; }
           warp_argmax(v, vi);
           const double amax = fmax(v, 0.0);
           const int t = vi;
-          const double acc = fabs(a[c][c]);
+          const double acc = fabs((double)a[c][c]);
           if (amax < st.small && acc < st.small) { decided = 3; piv = c; break; }
           if (acc >= mul_(st.u, amax)) { decided = 1; piv = c; break; }
           if (t >= 0 && t < w) {
@@ -292,7 +296,7 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
   }
   __syncthreads();
   const int nd = s_nd;
-  double* blk = st.blk + (int64_t)q * BW * LDB;
+  C* blk = reinterpret_cast<C*>(st.blk) + (int64_t)q * BW * LDB;
   for (int idx = tid; idx < BW * LDB; idx += blockDim.x) blk[idx] = (&a[0][0])[idx];
   if (tid < 2 * BW) st.bdinv[q * 2 * BW + tid] = dv[tid];
   if (tid < BW) st.lperm[q * BW + tid] = perm[tid];
@@ -325,22 +329,23 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
 }
 
 // apply D^-1 to the first nd entries of a solved row (apply_pivot OP_N)
-__device__ __forceinline__ void apply_dinv(double* x, const double* dv, int nd, double small) {
+template <typename C>
+__device__ __forceinline__ void apply_dinv(C* x, const double* dv, int nd, double small) {
 #pragma unroll
   for (int k = 0; k < BW;) {
     if (k >= nd) break;
     if (k + 1 < nd && isinf(dv[2 * k + 2])) {
       const double x1 = x[k], x2 = x[k + 1];
-      x[k] = fma_(dv[2 * k], x1, mul_(dv[2 * k + 1], x2));
-      x[k + 1] = fma_(dv[2 * k + 1], x1, mul_(dv[2 * k + 3], x2));
+      x[k] = (C)fma_(dv[2 * k], x1, mul_(dv[2 * k + 1], x2));
+      x[k + 1] = (C)fma_(dv[2 * k + 1], x1, mul_(dv[2 * k + 3], x2));
       k += 2;
     } else {
       const double d = dv[2 * k];
       if (d == 0.0) {
         const double v = x[k];
-        x[k] = (fabs(v) < small) ? 0.0 : dinf() * v;
+        x[k] = (C)((fabs(v) < small) ? 0.0 : dinf() * v);
       } else {
-        x[k] = mul_(x[k], d);
+        x[k] = mul_(x[k], (C)d);
       }
       k += 1;
     }
@@ -364,10 +369,11 @@ __global__ void __launch_bounds__(LDLT_RT) k_app_apply(const T* __restrict__ are
                                                       const LdltFront* __restrict__ fr,
                                                       const CtaMap* __restrict__ cm,
                                                       LdltStep st) {
-  __shared__ double L[BW][LDB];
+  using C = T;
+  __shared__ C L[BW][LDB];
   __shared__ double dv[2 * BW];
   __shared__ int perm[BW];
-  __shared__ double xs[BW][LDLT_RT + 1];
+  __shared__ C xs[BW][LDLT_RT + 1];
   __shared__ int fail;
   const CtaMap c = cm[blockIdx.x];
   const LdltFront F = fr[c.f];
@@ -375,7 +381,7 @@ __global__ void __launch_bounds__(LDLT_RT) k_app_apply(const T* __restrict__ are
   const int p = st.p_cur[q], nd = st.ndiag[q];
   const T* A = arena + F.off;
   const int ld = F.ld, tid = threadIdx.x;
-  const double* blk = st.blk + (int64_t)q * BW * LDB;
+  const C* blk = reinterpret_cast<const C*>(st.blk) + (int64_t)q * BW * LDB;
   for (int idx = tid; idx < BW * LDB; idx += blockDim.x) (&L[0][0])[idx] = blk[idx];
   if (tid < 2 * BW) dv[tid] = st.bdinv[q * 2 * BW + tid];
   if (tid < BW) perm[tid] = st.lperm[q * BW + tid];
@@ -389,20 +395,20 @@ __global__ void __launch_bounds__(LDLT_RT) k_app_apply(const T* __restrict__ are
     const int ci = t0 + tid;
     if (ci < nrow) {
       const int r = br.row(ci);
-      for (int k = 0; k < nd; ++k) xs[k][tid] = (double)A[(int64_t)(p + perm[k]) * ld + r];
+      for (int k = 0; k < nd; ++k) xs[k][tid] = (C)A[(int64_t)(p + perm[k]) * ld + r];
       // x L^T = a  (unit lower L)
       for (int j = 0; j < nd; ++j) {
-        const double xj = xs[j][tid];
+        const C xj = xs[j][tid];
         for (int k = j + 1; k < nd; ++k) xs[k][tid] = fma_(-xj, L[j][k], xs[k][tid]);
       }
-      double x[BW];
+      C x[BW];
 #pragma unroll
-      for (int k = 0; k < BW; ++k) x[k] = (k < nd) ? xs[k][tid] : 0.0;
+      for (int k = 0; k < BW; ++k) x[k] = (k < nd) ? xs[k][tid] : C(0);
       apply_dinv(x, dv, nd, st.small);
       int first = nd;
 #pragma unroll
       for (int k = BW - 1; k >= 0; --k)
-        if (k < nd && fabs(x[k]) > lim) first = k;
+        if (k < nd && fabs((double)x[k]) > lim) first = k;
       if (first < nd) atomicMin(&fail, first);
 #pragma unroll
       for (int k = 0; k < BW; ++k)
@@ -425,17 +431,18 @@ __global__ void __launch_bounds__(LDLT_RT) k_app_commit(T* __restrict__ arena,
                                                        const LdltFront* __restrict__ fr,
                                                        const CtaMap* __restrict__ cm,
                                                        LdltStep st) {
-  __shared__ double L[BW][LDB];
+  using C = T;
+  __shared__ C L[BW][LDB];
   __shared__ double dv[2 * BW];
   __shared__ int perm[BW];
-  __shared__ double orig[BW][LDLT_RT + 1];
+  __shared__ C orig[BW][LDLT_RT + 1];
   const CtaMap c = cm[blockIdx.x];
   const LdltFront F = fr[c.f];
   const int q = F.fidx, w = block_width(F, st.k);
   const int p = st.p_cur[q], nd = st.ndiag[q];
   T* A = arena + F.off;
   const int ld = F.ld, tid = threadIdx.x;
-  const double* blk = st.blk + (int64_t)q * BW * LDB;
+  const C* blk = reinterpret_cast<const C*>(st.blk) + (int64_t)q * BW * LDB;
   for (int idx = tid; idx < BW * LDB; idx += blockDim.x) (&L[0][0])[idx] = blk[idx];
   if (tid < 2 * BW) dv[tid] = st.bdinv[q * 2 * BW + tid];
   if (tid < BW) perm[tid] = st.lperm[q * BW + tid];
@@ -454,34 +461,34 @@ __global__ void __launch_bounds__(LDLT_RT) k_app_commit(T* __restrict__ arena,
     // the tile that starts at p, so no other CTA writes what this one reads)
     if (r < F.m) {
       for (int k = np; k < w; ++k) {
-        double v = 0.0;
+        C v = C(0);
         if (in_blk) {
           if (i >= k) {
             int ai = perm[i], ak = perm[k];
             int rr = max(ai, ak), cc = min(ai, ak);
-            v = (double)A[(int64_t)(p + cc) * ld + p + rr];
+            v = (C)A[(int64_t)(p + cc) * ld + p + rr];
           }
         } else {
-          v = (double)A[(int64_t)(p + perm[k]) * ld + r];
+          v = (C)A[(int64_t)(p + perm[k]) * ld + r];
         }
         orig[k][tid] = v;
       }
     }
     __syncthreads();
     if (r < F.m) {
-      double l[BW];
+      C l[BW];
 #pragma unroll
       for (int k = 0; k < BW; ++k) {
-        double v = 0.0;
+        C v = C(0);
         if (k < np) {
-          if (in_blk) v = (i > k) ? L[k][i] : (i == k ? 1.0 : 0.0);
-          else v = (double)pan[(int64_t)k * ldp_ + r];
+          if (in_blk) v = (i > k) ? L[k][i] : (i == k ? C(1) : C(0));
+          else v = (C)pan[(int64_t)k * ldp_ + r];
         }
         l[k] = v;
       }
       for (int k = 0; k < w; ++k) {
         if (in_blk && i < k) continue;
-        double v = (k < np) ? l[k] : orig[k][tid];
+        C v = (k < np) ? l[k] : orig[k][tid];
         A[(int64_t)(p + k) * ld + r] = (T)v;
       }
       if (r >= p + np) {
@@ -490,12 +497,13 @@ __global__ void __launch_bounds__(LDLT_RT) k_app_commit(T* __restrict__ arena,
             const double a = dv[2 * k], b = dv[2 * k + 1], cc = dv[2 * k + 3];
             const double det = __dsub_rn(mul_(a, cc), mul_(b, b));
             const double d11 = cc / det, d21 = -b / det, d22 = a / det;
-            ldp[(int64_t)k * ldp_ + r] = (T)fma_(l[k], d11, mul_(l[k + 1], d21));
-            ldp[(int64_t)(k + 1) * ldp_ + r] = (T)fma_(l[k], d21, mul_(l[k + 1], d22));
+            const double l0 = l[k], l1 = l[k + 1];
+            ldp[(int64_t)k * ldp_ + r] = (T)fma_(l0, d11, mul_(l1, d21));
+            ldp[(int64_t)(k + 1) * ldp_ + r] = (T)fma_(l0, d21, mul_(l1, d22));
             k += 2;
           } else {
             const double d = dv[2 * k];
-            ldp[(int64_t)k * ldp_ + r] = (T)((d == 0.0) ? 0.0 : l[k] / d);
+            ldp[(int64_t)k * ldp_ + r] = (T)((d == 0.0) ? C(0) : l[k] / (C)d);
             k += 1;
           }
         }
@@ -796,8 +804,8 @@ __global__ void __launch_bounds__(LDLT_RT) k_ldlt_calc_ld(const T* __restrict__ 
         k += 2;
       } else {
         const double d = D[2 * k];
-        const double l = A[(int64_t)k * F.ld + r];
-        out[(int64_t)k * ldo + r] = (T)((d == 0.0) ? 0.0 : l / d);
+        const T l = A[(int64_t)k * F.ld + r];
+        out[(int64_t)k * ldo + r] = (d == 0.0) ? T(0) : l / (T)d;
         k += 1;
       }
     }

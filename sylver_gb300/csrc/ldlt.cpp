@@ -28,8 +28,10 @@
 #include <cmath>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 
 #include "ldlt_dev.hpp"
+#include "tc.hpp"
 
 namespace sylver_gb300 {
 
@@ -41,6 +43,7 @@ struct LdltState {
   int64_t arena_used = 0, var_used = 0, d_used = 0;
   DevMem dvar, dall, blk, bdinv, lperm, state, mvvar;
   DevMem fr, fr2, cmap, cmap2, up, sc, sc2;  // per-level descriptors + scratch
+  DevMem tcsplit, tctask, tcplanes;          // FP32 contribution blocks on the tensor cores
   DevMem ea_cd, ea_items, ea_maps, am_src, am_dst;
   // solve
   DevMem sfr, sscr, sdoff;
@@ -137,6 +140,7 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   fk.arena.ensure((size_t)fk.arena_elems * sizeof(T));
   unsigned* status = fk.status.as<unsigned>();
   SG_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), s));
+  SG_CUDA(cudaMemsetAsync(fk.tcerr.p, 0, sizeof(unsigned), s));
   long launches = 0;
   std::vector<int> pos(st.n, -1);
   const int tpp_cols = Schedule::current().ldlt_tpp_cols;
@@ -407,11 +411,20 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
       fk.num_delay += nn - t2;
     }
     // ---- contribution blocks: CB -= (L D) L^T over all eliminated columns
+    // (form_contrib).  FP32 fronts with enough contribution rows run it on the
+    // tensor cores: L and L*D of the contribution rows are split into 3xBF16
+    // K-major planes (L*D rows stacked after L rows) and every 128 x 128 tile
+    // takes its A rows from L*D and its B rows from L; the rest use SIMT tiles.
     {
       std::vector<LdltFront> cfr;
       std::vector<CtaMap> cm;
       std::vector<UpdTask> ut;
-      int64_t cscr = 0;
+      std::vector<TcSplit> spl, spd;
+      std::vector<TcTask> tct;
+      int64_t cscr = 0, tcrows = 0, max_rows = 0;
+      int pitch = 0;
+      const bool tc_ok = std::is_same<T, float>::value && fk.use_tc;
+      const int tc_min = Schedule::current().tc_rows();
       for (int q = 0; q < nslot; ++q) {
         int s2 = F[q];
         int m = L.m[s2], n = L.n[s2], ne = L.nelim[s2];
@@ -423,31 +436,74 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
         int kf = (int)cfr.size();
         cfr.push_back(f);
         add_slice(cm, kf, ceil_div(m - n, LDLT_RT));
-        for (int cj = 0; n + cj * TM < m; ++cj)
-          for (int ri = cj; n + ri * TM < m; ++ri)
-            ut.push_back({f.off, f.ldp_off, f.off, f.ld, m, f.ld, n + ri * TM, n + cj * TM, m, m,
-                          0, ne, 0});
+        const int mc = m - n;
+        if (tc_ok && tc_min > 0 && mc >= tc_min) {
+          pitch = std::max(pitch, (ne + TC_KCHUNK - 1) / TC_KCHUNK * TC_KCHUNK);
+          const int64_t bl = tcrows, bd = tcrows + mc;
+          tcrows += 2 * (int64_t)mc;
+          max_rows = std::max<int64_t>(max_rows, mc);
+          spl.push_back({f.off, f.ld, m, n, ne, (int)bl, 0});
+          spd.push_back({f.ldp_off, m, m, n, ne, (int)bd, 0});
+          const int nk = (ne + TC_KCHUNK - 1) / TC_KCHUNK;
+          for (int cj = 0; n + cj * 128 < m; ++cj)
+            for (int ri = cj; n + ri * 128 < m; ++ri)
+              tct.push_back({f.off, f.ld, n + ri * 128, n + cj * 128, m, m,
+                             (int)(bd + ri * 128), (int)(bl + cj * 128), nk, 0});
+        } else {
+          for (int cj = 0; n + cj * TM < m; ++cj)
+            for (int ri = cj; n + ri * TM < m; ++ri)
+              ut.push_back({f.off, f.ldp_off, f.off, f.ld, m, f.ld, n + ri * TM, n + cj * TM, m,
+                            m, 0, ne, 0});
+        }
       }
       if (!cfr.empty()) {
         if (L.sc2.bytes < (size_t)std::max<int64_t>(cscr, 1) * sizeof(T))
           L.sc2.ensure((size_t)std::max<int64_t>(cscr, 1) * sizeof(T));
         put(L.fr2, cfr, s);
         put(L.cmap2, cm, s);
-        put(L.up, ut, s);
         launch_ldlt_calc_ld<T>(A, L.sc2.as<T>(), L.fr2.as<LdltFront>(), L.cmap2.as<CtaMap>(),
                                (int)cm.size(), stp, s);
-        launch_update<T>(A, L.sc2.as<T>(), L.up.as<UpdTask>(), (int)ut.size(), s);
-        launches += 2;
+        launches++;
+        if (!ut.empty()) {
+          put(L.up, ut, s);
+          launch_update<T>(A, L.sc2.as<T>(), L.up.as<UpdTask>(), (int)ut.size(), s);
+          launches++;
+        }
+        if constexpr (std::is_same<T, float>::value) {
+          if (!tct.empty()) {
+            // planes of tcrows x pitch BF16 each, 128-byte aligned
+            const int64_t pstride = (tcrows * pitch + 63) / 64 * 64;
+            if (L.tcplanes.bytes < (size_t)3 * pstride * sizeof(uint16_t))
+              L.tcplanes.ensure((size_t)3 * pstride * sizeof(uint16_t));
+            uint16_t* planes = L.tcplanes.as<uint16_t>();
+            std::vector<TcSplit> all(spl);
+            all.insert(all.end(), spd.begin(), spd.end());
+            put(L.tcsplit, all, s);
+            put(L.tctask, tct, s);
+            launch_split_t(A, L.tcsplit.as<TcSplit>(), (int)spl.size(), max_rows, planes,
+                           pstride, pitch, s);
+            launch_split_t(L.sc2.as<float>(), L.tcsplit.as<TcSplit>() + spl.size(),
+                           (int)spd.size(), max_rows, planes, pstride, pitch, s);
+            CUtensorMap maps[3];
+            for (int qq = 0; qq < 3; ++qq)
+              make_panel_map(&maps[qq], planes + qq * pstride, tcrows, pitch);
+            launch_update_tc(maps, A, L.tctask.as<TcTask>(), (int)tct.size(),
+                             fk.tcerr.as<unsigned>(), s);
+            launches += 3;
+          }
+        }
       }
     }
   }
   // ---- statistics and inertia from D (src/NumericTree.hxx:143-178)
   std::vector<double> D(std::max<int64_t>(L.d_used, 1));
-  unsigned sth = 0;
+  unsigned sth = 0, tce = 0;
   SG_CUDA(cudaMemcpyAsync(D.data(), L.dall.p, L.d_used * sizeof(double), cudaMemcpyDeviceToHost,
                           s));
   SG_CUDA(cudaMemcpyAsync(&sth, status, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  SG_CUDA(cudaMemcpyAsync(&tce, fk.tcerr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   SG_CUDA(cudaStreamSynchronize(s));
+  if (tce) throw CudaError("tensor-core update: a bounded wait timed out");
   fk.launches = launches;
   fk.num_neg = fk.num_two = fk.num_zero = 0;
   fk.num_factor = 0;
