@@ -255,6 +255,11 @@ int sylver_gb300_akeep_sizes(void const* akeep, int* n, int* nnodes, long* rlist
 int sylver_gb300_akeep_arrays(void const* akeep, int* sptr, int* sparent, long* rptr,
                               int* rlist, long* nptr, long* nlist, int* perm);
 
+/* Scaling saved by a matching-based analysis (options.ordering = 2), user
+ * order, n entries; returns n, or 0 when the analysis saved none.  No
+ * reference counterpart (the reference keeps it in akeep%scaling). */
+int sylver_gb300_akeep_scaling(void const* akeep, double* scale);
+
 /* Pivot-order D^-1 of an LDL^T factorization (2 entries per pivot, the
  * reference's storage: 1x1 [d, 0], 2x2 [a, b, Inf, c]) and the pivot-order
  * permutation applied by delays; for tests.  Returns number of pivots. */

@@ -125,7 +125,7 @@ EXPORTS = (
     "spldlt_tree_solve_bwd_posdef_dbl", "spldlt_factorize_mixed", "spldlt_factorize_device",
     "spldlt_solve_device", "sylver_gb300_solve_stats", "sylver_gb300_akeep_sizes",
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
-    "sylver_gb300_fkeep_fronts",
+    "sylver_gb300_fkeep_fronts", "sylver_gb300_akeep_scaling",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
     "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
     "sylver_gb300_get_schedule", "sylver_gb300_profile_solve", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
@@ -169,6 +169,7 @@ def load(path: str | None = None):
         "sylver_gb300_akeep_arrays": (I, [P, P, P, P, P, P, P, P]),
         "sylver_gb300_fkeep_diag": (I, [P, P, P]),
         "sylver_gb300_fkeep_fronts": (I, [P, P, P, P]),
+        "sylver_gb300_akeep_scaling": (I, [P, P]),
         "sylver_gb300_fkeep_counters": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I),
                                             ctypes.POINTER(D)]),
         "sylver_gb300_stream": (P, []),
@@ -223,7 +224,7 @@ def default_options() -> Options:
 class Analysis:
     """Result of spldlt_analyse (owns akeep)."""
 
-    def __init__(self, n, ptr, row, order=None, options=None, check=True):
+    def __init__(self, n, ptr, row, order=None, options=None, check=True, val=None):
         lib = load()
         self.options = options or default_options()
         if order is not None:
@@ -236,10 +237,19 @@ class Analysis:
         self.n = int(n)
         self.akeep = ctypes.c_void_p()
         self.inform = Inform()
+        self._val = None if val is None else np.ascontiguousarray(val, dtype=np.float64)
         lib.spldlt_analyse(self.n, _p(self._order) if self._order is not None else None,
-                           _p(self._ptr), _p(self._row), None, ctypes.byref(self.akeep),
+                           _p(self._ptr), _p(self._row),
+                           _p(self._val) if self._val is not None else None,
+                           ctypes.byref(self.akeep),
                            bool(check), ctypes.byref(self.options), ctypes.byref(self.inform))
         self.flag = self.inform.flag
+
+    def scaling(self):
+        """Scaling saved by a matching-based analysis (user order) or None."""
+        s = np.zeros(max(self.n, 1))
+        k = load().sylver_gb300_akeep_scaling(self.akeep, _p(s))
+        return s[:k] if k > 0 else None
 
     def symbolic(self):
         """SymbolicTree arrays (1-based, reference layout) + perm."""

@@ -17,10 +17,20 @@
 #include "analyse.hpp"
 #include "ldlt.hpp"
 #include "numeric.hpp"
+#include "scaling.hpp"
 
 using namespace sylver_gb300;
 
 namespace {
+
+// Values of the cleaned lower-triangle matrix (duplicates summed) from the
+// caller's val array.
+std::vector<double> clean_values(const AnalyseResult& c, const double* val) {
+  std::vector<double> v(c.crow.size(), 0.0);
+  for (size_t k = 0; k < c.crow.size(); ++k)
+    for (int64_t q = c.srcptr[k]; q < c.srcptr[k + 1]; ++q) v[k] += val[c.src[q]];
+  return v;
+}
 
 void clear_inform(sylver_inform_t* inf) {
   if (inf) std::memset(inf, 0, sizeof(*inf));
@@ -97,9 +107,50 @@ void factorize_common(bool posdef, const double* val_host, const double* val_dev
     }
     const int64_t nz = ak->nnz_val();
     const double* vdev = val_dev;
-    // user scaling S A S (src/spldlt_factorize_mod.F90:727-733), applied on
-    // the device after the unscaled values are kept for the residual
-    fk->set_scale((scale && (!opt || opt->scaling <= 0)) ? scale : nullptr, rt.stream);
+    // scaling S A S (src/spldlt_factorize_mod.F90:727-830), applied on the
+    // device after the unscaled values are kept for the residual:
+    //   scaling <= 0: the caller's `scale` (none when null);
+    //   1, 2: maximum-product matching scaling of these values (the
+    //         reference's Hungarian and auction variants compute the same
+    //         kind of scaling; both use the matching here);
+    //   3: the scaling saved by the matching-based ordering;
+    //   >= 4: infinity-norm equilibration.
+    // Computed scalings are copied to `scale` when it is given.
+    const int sopt = opt ? opt->scaling : 0;
+    std::vector<double> comp;
+    const double* use_scale = nullptr;
+    if (sopt <= 0) {
+      use_scale = scale;
+    } else if (sopt == 3) {
+      if (ak->mscale.empty()) {
+        inform->flag = SYLVER_ERROR_NO_SAVED_SCALING;
+        if (!fkeep) delete fk;
+        return;
+      }
+      comp = ak->mscale;
+    } else {
+      std::vector<double> hv;
+      const double* hval = val_host;
+      if (!hval) {
+        hv.resize(std::max<int64_t>(nz, 1));
+        if (nz) SG_CUDA(cudaMemcpy(hv.data(), val_dev, nz * sizeof(double),
+                                   cudaMemcpyDeviceToHost));
+        hval = hv.data();
+      }
+      SymCsc full = expand_lower(ak->n, ak->clean.cptr, ak->clean.crow,
+                                 clean_values(ak->clean, hval));
+      if (sopt <= 2) {
+        std::vector<int> match;
+        matching_scaling(full, match, comp);
+      } else {
+        equilibration_scaling(full, comp);
+      }
+    }
+    if (!comp.empty()) {
+      use_scale = comp.data();
+      if (scale) std::copy(comp.begin(), comp.end(), scale);
+    }
+    fk->set_scale(use_scale, rt.stream);
     if (val_host) {
       fk->val.ensure(std::max<int64_t>(nz, 1) * sizeof(double));
       if (nz) SG_CUDA(cudaMemcpyAsync(fk->val.p, val_host, nz * sizeof(double),
@@ -109,6 +160,10 @@ void factorize_common(bool posdef, const double* val_host, const double* val_dev
     int flag = posdef ? fk->factorize(vdev, rt.stream) : factorize_ldlt(*fk, vdev, rt.stream);
     fill_inform_from_fkeep(*fk, inform);
     inform->flag = flag;
+    // the matching-based ordering's scaling was not used
+    // (src/spldlt_factorize_mod.F90:721-725)
+    if (flag == 0 && !ak->mscale.empty() && sopt != 3)
+      inform->flag = SYLVER_WARNING_MATCH_ORD_NO_SCALE;
     if (!fkeep) delete fk;
   } catch (const std::bad_alloc&) {
     inform->flag = SYLVER_ERROR_ALLOCATION;
@@ -221,7 +276,6 @@ void sylver_default_options(sylver_options_t* o) {
 void spldlt_analyse(int n, int* order, long const* ptr, int const* row, double const* val,
                     void** akeep, bool check, sylver_options_t const* options,
                     sylver_inform_t* inform) {
-  (void)val;
   clear_inform(inform);
   if (!akeep) {
     inform->flag = SYLVER_ERROR_UNKNOWN;
@@ -236,8 +290,17 @@ void spldlt_analyse(int n, int* order, long const* ptr, int const* row, double c
     *akeep = ak;
     ak->n = n;
     ak->check = check;
-    AnalyseInput in{n, reinterpret_cast<const int64_t*>(ptr), row, order, check,
-                    options ? options->ordering : 1, options ? options->nemin : 32};
+    const int ordering = options ? options->ordering : 1;
+    if (ordering < 0 || ordering > 2) {
+      ak->flag = inform->flag = SYLVER_ERROR_ORDER;  // src/spldlt_analyse_mod.F90:692-696
+      return;
+    }
+    if (ordering == 2 && !val) {
+      ak->flag = inform->flag = SYLVER_ERROR_VAL;  // :698-703
+      return;
+    }
+    AnalyseInput in{n, reinterpret_cast<const int64_t*>(ptr), row, order, check, ordering,
+                    options ? options->nemin : 32};
     ak->clean = clean_matrix(in);
     ak->matrix_outrange = ak->clean.matrix_outrange;
     ak->matrix_dup = ak->clean.matrix_dup;
@@ -247,6 +310,21 @@ void spldlt_analyse(int n, int* order, long const* ptr, int const* row, double c
       inform->flag = ak->flag;
       return;
     }
+    // matching-based ordering (match_order_metis, :787-816): the order comes
+    // from the compressed matching graph and its scaling is saved for
+    // factorize (options.scaling = 3)
+    std::vector<int> morder;
+    int msing = 0;
+    if (ordering == 2) {
+      SymCsc full = expand_lower(n, ak->clean.cptr, ak->clean.crow, clean_values(ak->clean, val));
+      std::vector<int> match;
+      msing = matching_scaling(full, match, ak->mscale);
+      std::vector<int> pos = matching_order(full, match);
+      morder.resize(n);
+      for (int i = 0; i < n; ++i) morder[i] = pos[i] + 1;
+      in.order = morder.data();
+      in.ordering = 0;
+    }
     std::string err;
     int fl = analyse(in, ak->clean, ak->st, err);
     if (fl < 0) {
@@ -255,6 +333,7 @@ void spldlt_analyse(int n, int* order, long const* ptr, int const* row, double c
       return;
     }
     ak->flag = ak->clean.flag;
+    if (msing && ak->flag == 0) ak->flag = SYLVER_WARNING_ANAL_SINGULAR;
     ak->build_full_csr();
     fill_inform_from_akeep(*ak, inform);
   } catch (const std::bad_alloc&) {
@@ -356,6 +435,13 @@ int sylver_gb300_akeep_arrays(void const* akeep, int* sptr, int* sparent, long* 
   if (nlist) for (size_t i = 0; i < st.nlist.size(); ++i) nlist[i] = (long)st.nlist[i];
   if (perm) for (size_t i = 0; i < st.perm.size(); ++i) perm[i] = st.perm[i] + 1;
   return 0;
+}
+
+int sylver_gb300_akeep_scaling(void const* akeep, double* scale) {
+  const AKeep* ak = static_cast<const AKeep*>(akeep);
+  if (!ak || ak->mscale.empty()) return 0;
+  if (scale) std::copy(ak->mscale.begin(), ak->mscale.end(), scale);
+  return (int)ak->mscale.size();
 }
 
 int sylver_gb300_fkeep_diag(void const* fkeep, double* d, int* piv_order) {

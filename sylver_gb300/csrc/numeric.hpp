@@ -105,6 +105,9 @@ struct AKeep {
   // scaling S A S.  Built on the first scaled factorization.
   std::vector<int> vrow, vcol;
   void build_val_rowcol();
+  // scaling saved by the matching-based ordering (options.ordering = 2),
+  // user order; used by factorize with options.scaling = 3
+  std::vector<double> mscale;
 };
 
 // One kernel launch of the factor schedule.

@@ -123,3 +123,43 @@ def test_ldlt_delays_move_up(sylver, gpu):
     b = np.asfortranarray(rng.standard_normal((a.n, 1)))
     x = f.solve(b)
     assert w.backward_error(full, x, b).max() <= 1e-14
+
+
+@pytest.mark.parametrize("scaling", [0, 1, 3, 4])
+def test_kkt_matching_ordering_and_scalings(sylver, gpu, scaling):
+    """Matching-based ordering (options.ordering = 2) on the saddle-point
+    matrix with each scaling option: 0 none, 1 matching scaling of the
+    values, 3 the scaling saved by the analysis, 4 equilibration.  Inertia by
+    Haynsworth and a refined backward error <= 1e-14 in every case; the
+    saved scaling leaves no warning, the others warn that it went unused
+    (flag 8, src/spldlt_factorize_mod.F90:721-725)."""
+    p = w.kkt(10, nrhs=1)
+    o = sylver.default_options()
+    o.ordering = 2
+    o.scaling = scaling
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, options=o, val=p.a.val)
+    assert an.flag >= 0
+    f = sylver.Factor(an, False, p.a.val, ir_max_iter=10, options=o)
+    assert f.flag == (0 if scaling == 3 else 8), f.inform.as_dict()
+    assert f.inform.num_neg == p.inertia[0]
+    x = f.solve(p.rhs)
+    assert w.backward_error(p.a.to_scipy_full(), x, p.rhs).max() <= 1e-14
+    print("kkt10 ordering=2 scaling", scaling, "delays", f.inform.num_delay,
+          "two", f.inform.num_two)
+
+
+def test_kkt_matching_ordering_fewer_delays(sylver, gpu):
+    """The matched 2x2 pairs stay together: fewer delayed pivots than the
+    plain nested dissection on the same saddle-point matrix."""
+    p = w.kkt(12, nrhs=1)
+    plain = sylver.Analysis(p.a.n, p.a.ptr, p.a.row)
+    f0 = sylver.Factor(plain, False, p.a.val)
+    o = sylver.default_options()
+    o.ordering = 2
+    o.scaling = 3
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, options=o, val=p.a.val)
+    f1 = sylver.Factor(an, False, p.a.val, options=o)
+    print("kkt12 delays: nested dissection", f0.inform.num_delay, "matching",
+          f1.inform.num_delay)
+    assert f0.inform.num_neg == f1.inform.num_neg == p.inertia[0]
+    assert f1.inform.num_delay < f0.inform.num_delay
