@@ -288,6 +288,15 @@ void* sylver_gb300_stream(void);
 int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, long* launches,
                                 double* flops);
 
+/* Re-run the Cholesky factorization held by fkeep launch by launch with CUDA
+ * events (no graph) and add each launch's time to its level of the assembly
+ * tree (leaves are level 0): level_ms[l] for l < number of levels (set-up
+ * and the solve inverses are not counted).  Returns the number of levels, or
+ * a reference flag (-10 when max_levels is too small).  The learned
+ * scheduler trains on these per-level timings.  No reference counterpart. */
+int sylver_gb300_profile_levels(void* fkeep, double const* val_dev, double* level_ms,
+                                int max_levels);
+
 /* Time one forward + backward sweep of the Cholesky factor held by fkeep for
  * nrhs (1..32) right-hand sides (zeros, in an internal buffer), launch by
  * launch with CUDA events and no graph, accumulated per kernel kind:

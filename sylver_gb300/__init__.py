@@ -125,7 +125,7 @@ EXPORTS = (
     "spldlt_tree_solve_bwd_posdef_dbl", "spldlt_factorize_mixed", "spldlt_factorize_device",
     "spldlt_solve_device", "sylver_gb300_solve_stats", "sylver_gb300_akeep_sizes",
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
-    "sylver_gb300_fkeep_fronts", "sylver_gb300_akeep_scaling",
+    "sylver_gb300_fkeep_fronts", "sylver_gb300_akeep_scaling", "sylver_gb300_profile_levels",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
     "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
     "sylver_gb300_get_schedule", "sylver_gb300_profile_solve", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
@@ -170,6 +170,7 @@ def load(path: str | None = None):
         "sylver_gb300_fkeep_diag": (I, [P, P, P]),
         "sylver_gb300_fkeep_fronts": (I, [P, P, P, P]),
         "sylver_gb300_akeep_scaling": (I, [P, P]),
+        "sylver_gb300_profile_levels": (I, [P, P, P, I]),
         "sylver_gb300_fkeep_counters": (I, [P, ctypes.POINTER(L), ctypes.POINTER(I),
                                             ctypes.POINTER(D)]),
         "sylver_gb300_stream": (P, []),
@@ -343,6 +344,15 @@ class Factor:
             raise RuntimeError(f"profile failed: {rc}")
         return {k: dict(ms=float(ms[i]), launches=int(nl[i]), flops=float(fl[i]))
                 for i, k in enumerate(self.KINDS)}
+
+    def profile_levels(self, val_dev_ptr=None):
+        """Per-level factorization time (ms) of one extra, launch-by-launch
+        factorization (Cholesky), leaves first."""
+        ml = np.zeros(256)
+        k = load().sylver_gb300_profile_levels(self.fkeep, val_dev_ptr, _p(ml), 256)
+        if k < 0:
+            raise RuntimeError(f"profile_levels failed: {k}")
+        return ml[:k]
 
     SOLVE_KINDS = ("small_fwd", "small_bwd", "gather_fwd", "gather_bwd", "scatter_fwd",
                    "scatter_bwd", "diag_fwd", "rows_fwd", "rows_bwd", "diag_bwd", "cb_bwd",

@@ -473,6 +473,24 @@ int sylver_gb300_profile_factor(void* fkeep, double const* val_dev, double* ms, 
   }
 }
 
+int sylver_gb300_profile_levels(void* fkeep, double const* val_dev, double* level_ms,
+                                int max_levels) {
+  FKeep* fk = static_cast<FKeep*>(fkeep);
+  if (!fk || !level_ms) return SYLVER_ERROR_CALL_SEQUENCE;
+  const int nl = (int)fk->levels.size();
+  if (max_levels < nl) return SYLVER_ERROR_X_SIZE;
+  std::vector<double> ms(12), fl(12);
+  std::vector<long> cnt(12);
+  for (int l = 0; l < nl; ++l) level_ms[l] = 0.0;
+  try {
+    int rc = fk->profile(val_dev, ms.data(), cnt.data(), fl.data(), Runtime::get().stream,
+                         level_ms);
+    return rc < 0 ? rc : nl;
+  } catch (const std::exception&) {
+    return SYLVER_ERROR_CUDA_UNKNOWN;
+  }
+}
+
 int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches) {
   FKeep* fk = static_cast<FKeep*>(fkeep);
   if (!fk || !ms || !launches) return SYLVER_ERROR_CALL_SEQUENCE;

@@ -282,8 +282,10 @@ void FKeep::plan_cholesky() {
   blk_pw = PW;
   std::vector<int> pos(st.n, -1);
   ops.clear();
+  op_level.clear();
   ops.push_back({Op::MEMSET, 0, 0, 0});
   ops.push_back({Op::INIT, 0, ninit, 0});
+  op_level.assign(ops.size(), -1);
   for (auto& L : levels) {
     // extend-add of children into this level's fronts
     int64_t i0 = (int64_t)items.size();
@@ -488,9 +490,11 @@ void FKeep::plan_cholesky() {
       if (PW == 0) ops.push_back({Op::SPLIT, sp0, (int64_t)tcs.size(), lvl});
       ops.push_back({Op::TCUPD, tk0, (int64_t)tct.size(), lvl});
     }
+    op_level.resize(ops.size(), (int)(&L - levels.data()));
   }
 
   ops.push_back({Op::INV, 0, 0, 0});
+  op_level.resize(ops.size(), -1);
   // algorithmic flops of update launches: lower-triangle entries x 2K
   op_flops.assign(ops.size(), 0.0);
   for (const auto& tf : tcop_flops) op_flops[tf.first] = tf.second;
@@ -695,7 +699,8 @@ int FKeep::factorize(const double* val_dev, cudaStream_t s) {
   return flag;
 }
 
-int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, cudaStream_t s) {
+int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, cudaStream_t s,
+                   double* level_ms) {
   for (int k = 0; k < 12; ++k) {
     ms[k] = 0.0;
     nl[k] = 0;
@@ -727,6 +732,7 @@ int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, c
     ms[k] += t;
     nl[k] += 1;
     flops[k] += op_flops.empty() ? 0.0 : op_flops[q];
+    if (level_ms && q < op_level.size() && op_level[q] >= 0) level_ms[op_level[q]] += t;
   }
   for (auto& e : ev) cudaEventDestroy(e);
   return 0;

@@ -215,6 +215,7 @@ struct FKeep {
   int64_t scratch_rows = 0;
   std::vector<Op> ops;
   std::vector<double> op_flops;      // algorithmic flops per op (update launches)
+  std::vector<int> op_level;         // level of each op (-1: whole-factor set-up / inverses)
   bool init_atomic = false;
   int64_t ninit = 0;
 
@@ -280,8 +281,10 @@ struct FKeep {
   int solve(int job, int nrhs, double* x_dev, int ldx, cudaStream_t s);
   // Solve with x already in pivot order (the tree-level seam), FP64 only.
   int solve_raw(int job, int nrhs, double* x_dev, int ldx, cudaStream_t s);
-  // Per-kind timing of the factor schedule (see sylver_gb300_profile_factor).
-  int profile(const double* val_dev, double* ms, long* launches, double* flops, cudaStream_t s);
+  // Per-kind timing of the factor schedule (see sylver_gb300_profile_factor);
+  // level_ms (optional, one entry per level) receives the time per level.
+  int profile(const double* val_dev, double* ms, long* launches, double* flops, cudaStream_t s,
+              double* level_ms = nullptr);
   // Per-kind timing of one forward + backward sweep (see sylver_gb300_profile_solve).
   int profile_solve(int nrhs, double* ms, long* launches, cudaStream_t s);
 

@@ -1,4 +1,4 @@
-"""Autotuner and learned scheduler for the factorization's kernel paths.
+"""Autotuners and learned schedulers for the factorization's kernel paths.
 
 A *schedule* (``sylver_gb300_schedule_t``) chooses which kernels process
 which fronts -- for LDL^T, the column count below which a front skips the
@@ -18,9 +18,25 @@ changes the arithmetic of a pivot decision or an update.
   outside the range it was trained on.  Measured time is the judge of its
   error.
 
+Cholesky (FP32 factors): the schedule is the blocked path's outer panel width
+and group (fs_panel_cols, fs_panel_group), the small-front cutoff
+(small_front_rows) and the tensor-core contribution-block threshold
+(tc_min_cb_rows).  ``CholAutotuner`` sweeps the candidate grid with measured
+factor times; ``CholLearnedScheduler`` predicts, for every candidate, the
+time of each level of the assembly tree from features of that level (front
+counts, sizes, flops) with the same GPU MLP, trained on the per-level
+CUDA-event timings the library records (``sylver_gb300_profile_levels``) on
+generated log-normal 27-point matrices; the predicted factor time is the sum
+over levels, and the argmin is proposed from the analysis alone (no
+factorization).  It falls back to the autotuner without weights or outside
+its training range.
+
     python -m sylver_gb300.scheduler record OUT.npz [count] [seed0]
     python -m sylver_gb300.scheduler train DATA.npz OUT_WEIGHTS.npz [epochs]
     python -m sylver_gb300.scheduler evaluate WEIGHTS.npz [count] [seed0]
+    python -m sylver_gb300.scheduler chol-record OUT.npz [count] [seed0]
+    python -m sylver_gb300.scheduler chol-train DATA.npz OUT_WEIGHTS.npz [epochs]
+    python -m sylver_gb300.scheduler chol-evaluate WEIGHTS.npz [k ...]
 """
 from __future__ import annotations
 
@@ -31,7 +47,7 @@ import time
 
 import numpy as np
 
-from . import FP64, Analysis, Factor, default_options, load, set_schedule
+from . import FP32, FP64, Analysis, Factor, default_options, load, set_schedule
 from . import workloads as w
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -266,8 +282,200 @@ def evaluate(weights, count=10, seed0=300):
     return res
 
 
+# ---------------------------------------------------------------------------
+# Cholesky schedules (FP32 factors), learned from per-level timings
+
+CHOL_CANDIDATES = tuple(
+    dict(fs_panel_cols=pc, fs_panel_group=g, small_front_rows=sm, tc_min_cb_rows=tc)
+    for pc in (64, 128, 256) for g in (1, 2, 4) if pc * g <= 512
+    for sm in (96, 128) for tc in (64, 256))
+CHOL_DEFAULT = dict(fs_panel_cols=64, fs_panel_group=4, small_front_rows=128, tc_min_cb_rows=64)
+CHOL_LEVEL_FEATURES = 10
+
+
+def spd_instance(seed):
+    """Training / evaluation instance of the SPD family: 27-point log-normal
+    Laplacian on k^3, k ~ U{16..44} (the 80^3 configuration at small scale)."""
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(16, 45))
+    return w.lognormal27(k, seed=seed, rhs_seed=seed + 1, nrhs=1)
+
+
+def spd_analyse(p):
+    return Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+
+
+def level_features(an):
+    """One row per level of the assembly tree (leaves first): fronts, sizes,
+    flops and the fractions of fronts each kernel path would take."""
+    sy = an.symbolic()
+    m = np.diff(sy["rptr"]).astype(np.float64)
+    n = np.diff(sy["sptr"]).astype(np.float64)
+    par = np.asarray(sy["sparent"]) - 1
+    nn = len(m)
+    h = np.zeros(nn, np.int64)
+    for i in range(nn):  # postorder: children first
+        if 0 <= par[i] < nn:
+            h[par[i]] = max(h[par[i]], h[i] + 1)
+    fl = (m * (m + 1) * (2 * m + 1) - (m - n) * (m - n + 1) * (2 * (m - n) + 1)) / 6.0
+    rows = []
+    for lv in range(int(h.max()) + 1 if nn else 0):
+        idx = np.nonzero(h == lv)[0]
+        mm, nv, ff = m[idx], n[idx], fl[idx]
+        rows.append([np.log2(1 + len(idx)) / 16, np.log2(1 + (mm * mm).sum()) / 40,
+                     np.log2(1 + mm.max()) / 16, np.log2(1 + nv.max()) / 16,
+                     np.log2(1 + ff.sum()) / 48, np.log2(1 + ff.max()) / 48,
+                     float(np.mean(nv >= 96)), float(np.mean(mm - nv >= 64)),
+                     float(np.mean(mm <= 128)), lv / 32.0])
+    return np.array(rows, dtype=np.float32)
+
+
+def chol_schedule_features(c):
+    return np.array([c["fs_panel_cols"] / 256.0, c["fs_panel_group"] / 8.0,
+                     c["small_front_rows"] / 128.0, np.log2(c["tc_min_cb_rows"]) / 8.0],
+                    dtype=np.float32)
+
+
+def chol_measure(an, p, sched, repeats=2, levels=False):
+    """Measured FP32 factor time (ms, CUDA events, best of `repeats`) under a
+    schedule, and optionally the per-level times of one more factorization."""
+    set_schedule(**sched)
+    try:
+        f = Factor(an, True, p.a.val, precision=FP32)
+        best = f.counters()["factor_ms"]
+        for _ in range(repeats - 1):
+            f.refactor(p.a.val, precision=FP32)
+            best = min(best, f.counters()["factor_ms"])
+        lv = f.profile_levels() if levels else None
+        return best, lv, f.flag
+    finally:
+        set_schedule()
+
+
+class CholAutotuner:
+    """Measured sweep over the Cholesky candidate schedules."""
+
+    def __init__(self, candidates=CHOL_CANDIDATES):
+        self.candidates = candidates
+
+    def tune(self, an, p):
+        times = []
+        for c in self.candidates:
+            ms, _, flag = chol_measure(an, p, c)
+            times.append(ms if flag >= 0 else np.inf)
+        best = int(np.argmin(times))
+        return self.candidates[best], times
+
+
+class CholLearnedScheduler:
+    """Per-level MLP over (level features, schedule); predicted factor time =
+    sum over levels; proposes the argmin from the analysis alone."""
+
+    def __init__(self, weights=None, autotuner=None):
+        self.autotuner = autotuner or CholAutotuner()
+        self.model = None
+        if weights and os.path.exists(weights):
+            z = np.load(weights)
+            self.mu, self.sd = z["mu"], z["sd"]
+            self.ymu, self.ysd = float(z["ymu"]), float(z["ysd"])
+            self.fmin, self.fmax = z["fmin"], z["fmax"]
+            self.model = Mlp(int(z["nin"]), int(z["nhidden"]))
+            self.model.set_params(z["params"])
+
+    def predict_ms(self, lf, candidates):
+        out = []
+        for c in candidates:
+            sf = np.repeat(chol_schedule_features(c)[None, :], len(lf), 0)
+            x = np.concatenate([lf, sf], 1)
+            y = self.model.forward((x - self.mu) / self.sd)
+            out.append(float(np.exp(y * self.ysd + self.ymu).sum()))
+        return np.array(out)
+
+    def in_range(self, lf):
+        span = self.fmax - self.fmin
+        return bool(np.all(lf >= self.fmin - 0.25 * span) and np.all(lf <= self.fmax + 0.25 * span))
+
+    def propose(self, an, p):
+        """Returns (schedule, how, factorizations_used)."""
+        lf = level_features(an)
+        if self.model is None or not self.in_range(lf):
+            best, times = self.autotuner.tune(an, p)
+            return best, "autotuner", 2 * len(times)
+        cands = self.autotuner.candidates
+        return cands[int(np.argmin(self.predict_ms(lf, cands)))], "mlp", 0
+
+
+def chol_record(out, count=24, seed0=500):
+    rows_x, rows_y, meta = [], [], []
+    t0 = time.time()
+    for s in range(seed0, seed0 + count):
+        p = spd_instance(s)
+        an = spd_analyse(p)
+        lf = level_features(an)
+        for ci, c in enumerate(CHOL_CANDIDATES):
+            ms, lv, flag = chol_measure(an, p, c, repeats=1, levels=True)
+            if flag < 0:
+                continue
+            for l in range(min(len(lv), len(lf))):
+                rows_x.append(np.concatenate([lf[l], chol_schedule_features(c)]))
+                rows_y.append(np.log(lv[l] + 1e-3))
+                meta.append((s, ci, l, lv[l], ms))
+        print(f"seed {s} n={p.a.n} levels {len(lf)} ({time.time() - t0:.0f}s)", flush=True)
+    np.savez_compressed(out, x=np.array(rows_x, np.float32), y=np.array(rows_y, np.float32),
+                        meta=np.array(meta))
+
+
+def chol_train(data, out, epochs=6000, seed=0):
+    z = np.load(data)
+    x, y = z["x"], z["y"]
+    mu, sd = x.mean(0), x.std(0) + 1e-6
+    ymu, ysd = float(y.mean()), float(y.std() + 1e-6)
+    m = Mlp(x.shape[1], HIDDEN, seed)
+    xn, yn = (x - mu) / sd, (y - ymu) / ysd
+    loss0, _ = m.loss_grad(xn, yn)
+    loss = m.train(xn, yn, epochs=epochs, lr=2e-3)
+    print(f"train {x.shape[0]} level samples: loss {loss0:.4f} -> {loss:.4f}")
+    nlf = CHOL_LEVEL_FEATURES
+    np.savez_compressed(out, params=m.params(), mu=mu, sd=sd, ymu=ymu, ysd=ysd, nin=x.shape[1],
+                        nhidden=HIDDEN, fmin=x[:, :nlf].min(0), fmax=x[:, :nlf].max(0),
+                        loss0=loss0, loss=loss)
+    return loss0, loss
+
+
+def chol_evaluate(weights, ks=(40, 56, 80)):
+    """Default vs learned vs measured sweep (factor ms) on k^3 log-normal
+    27-point matrices (seed 2, the benchmark's matrix at k = 80)."""
+    ls = CholLearnedScheduler(weights)
+    res = []
+    for k in ks:
+        p = w.lognormal27(k, nrhs=1)
+        an = spd_analyse(p)
+        t0 = time.perf_counter()
+        choice, how, used = ls.propose(an, p)
+        t_prop = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        best, times = ls.autotuner.tune(an, p)
+        t_sweep = time.perf_counter() - t0
+        ci = ls.autotuner.candidates.index(choice)
+        di = ls.autotuner.candidates.index(CHOL_DEFAULT)
+        res.append(dict(k=k, n=p.a.n, default_ms=times[di], best=best, best_ms=min(times),
+                        choice=choice, how=how, choice_ms=times[ci], propose_s=t_prop,
+                        sweep_s=t_sweep, factorizations_used=used))
+        print(res[-1], flush=True)
+    return res
+
+
 def main(argv):
     cmd = argv[0]
+    if cmd == "chol-record":
+        chol_record(argv[1], *(int(a) for a in argv[2:4]))
+        return
+    if cmd == "chol-train":
+        chol_train(argv[1], argv[2], *(int(a) for a in argv[3:4]))
+        return
+    if cmd == "chol-evaluate":
+        chol_evaluate(argv[1], tuple(int(a) for a in argv[2:]) or (40, 56, 80))
+        return
     if cmd == "record":
         record(argv[1], *(int(a) for a in argv[2:4]))
     elif cmd == "train":
