@@ -340,7 +340,7 @@ int spldlt_tree_solve_fwd_noalloc_dbl(bool posdef, void const* tree, int nrhs, d
  * front, never the arithmetic.  0 keeps the built-in default. */
 typedef struct {
   int small_front_rows;  /* Cholesky: fronts with at most this many rows are factorised whole
-                            by one CTA (capped at 96 FP64 / 128 FP32; default: the cap) */
+                            by one CTA (capped at 96 FP64 / 128 FP32; default 96) */
   int tc_min_cb_rows;    /* FP32 Cholesky: contribution blocks with at least this many rows
                             use the tensor-core update (default 64; negative: never) */
   int solve_large_cols;  /* fronts with at least this many eliminated columns use the blocked

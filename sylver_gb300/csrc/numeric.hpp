@@ -59,8 +59,10 @@ struct Schedule {
                              // path (multiple of 64, <= 256; <0: 64-column SIMT steps)
   int fs_panel_group = 0;    // FP32 Cholesky: outer panels per trailing fully-summed update
   static Schedule& current();
+  // default 96 rows: measured faster than the FP32 cap of 128 on 40^3, 56^3 and
+  // 80^3 log-normal 27-point matrices (schedule sweeps of the learned scheduler)
   int small_rows(int compiled_max) const {
-    return small_front_rows > 0 ? std::min(small_front_rows, compiled_max) : compiled_max;
+    return std::min(small_front_rows > 0 ? small_front_rows : 96, compiled_max);
   }
   int tc_rows() const { return tc_min_cb_rows == 0 ? 64 : tc_min_cb_rows; }
   int solve_cols() const { return solve_large_cols > 0 ? solve_large_cols : 96; }

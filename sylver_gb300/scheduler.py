@@ -289,7 +289,7 @@ CHOL_CANDIDATES = tuple(
     dict(fs_panel_cols=pc, fs_panel_group=g, small_front_rows=sm, tc_min_cb_rows=tc)
     for pc in (64, 128, 256) for g in (1, 2, 4) if pc * g <= 512
     for sm in (96, 128) for tc in (64, 256))
-CHOL_DEFAULT = dict(fs_panel_cols=64, fs_panel_group=4, small_front_rows=128, tc_min_cb_rows=64)
+CHOL_DEFAULT = dict(fs_panel_cols=64, fs_panel_group=4, small_front_rows=96, tc_min_cb_rows=64)
 CHOL_LEVEL_FEATURES = 10
 
 

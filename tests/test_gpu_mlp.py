@@ -112,3 +112,37 @@ def test_learned_schedule_gains_over_search_without_it(sylver, gpu):
     assert tot["mlp"] <= 1.10 * tot["best"] + 0.5
     assert tot["mlp"] <= 1.02 * tot["default"] + 0.5
     assert tot["mlp_s"] < 0.5 * tot["sweep_s"]
+
+
+CHOL_WEIGHTS = os.path.join(os.path.dirname(__file__), "..", "sylver_gb300", "data",
+                            "sched_chol_mlp.npz")
+
+
+def test_learned_cholesky_schedule_against_sweep(sylver, gpu):
+    """Cholesky schedule (panel width and group, small-front cutoff, tensor-core
+    threshold) from the per-level MLP, on held-out log-normal matrices (seeds
+    outside the training range 500-523): proposed from the analysis alone (no
+    factorization), within 5 % (+0.2 ms) of the measured sweep's best and not
+    slower than the default schedule by more than 2 % (+0.2 ms), judged by
+    measured factor time."""
+    from sylver_gb300 import scheduler as sc
+    assert os.path.exists(CHOL_WEIGHTS), "trained Cholesky schedule weights missing"
+    ls = sc.CholLearnedScheduler(CHOL_WEIGHTS)
+    assert ls.model is not None
+    tot = dict(default=0.0, best=0.0, mlp=0.0)
+    for s in (900, 901):
+        p = sc.spd_instance(s)
+        an = sc.spd_analyse(p)
+        choice, how, used = ls.propose(an, p)
+        assert how == "mlp" and used == 0
+        best, times = ls.autotuner.tune(an, p)
+        ci = ls.autotuner.candidates.index(choice)
+        di = ls.autotuner.candidates.index(sc.CHOL_DEFAULT)
+        tot["default"] += times[di]
+        tot["best"] += min(times)
+        tot["mlp"] += times[ci]
+        print(f"seed {s} n={p.a.n}: default {times[di]:.3f} best {min(times):.3f} "
+              f"mlp {times[ci]:.3f} {choice}")
+    print(tot)
+    assert tot["mlp"] <= 1.05 * tot["best"] + 0.2
+    assert tot["mlp"] <= 1.02 * tot["default"] + 0.2
