@@ -300,12 +300,12 @@ int sylver_gb300_profile_levels(void* fkeep, double const* val_dev, double* leve
 /* Time one forward + backward sweep of the Cholesky factor held by fkeep for
  * nrhs (1..32) right-hand sides (zeros, in an internal buffer), launch by
  * launch with CUDA events and no graph, accumulated per kernel kind:
- * 0 small fronts forward, 1 small fronts backward, 2 + k for the large-front
- * launches (k: 0/1 gather forward/backward, 2/3 scatter forward/backward,
- * 4 diagonal block forward, 5 rows below forward, 6 rows below backward,
- * 7 diagonal block backward, 8 contribution rows backward, 9 rows below
- * forward, one row per thread).  Arrays hold 12 entries.  Returns 0, or -98 for
- * an LDL^T factor or nrhs outside 1..32.  No reference counterpart. */
+ * 0 small fronts forward, 1 small fronts backward (pivot rows), 2 + k for the
+ * other launches (k: 0/1 gather forward/backward, 2/3 scatter forward/
+ * backward, 4 diagonal block forward, 5 rows below forward, 6 rows below
+ * backward, 7 diagonal block backward, 8 contribution rows backward, 9
+ * contribution rows forward).  Arrays hold 16 entries.  Returns 0, or -98 for an LDL^T factor or nrhs outside
+ * 1..32.  No reference counterpart. */
 int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches);
 
 /* Diagnostic: run the tensor-core (tcgen05, 3xBF16) contribution-block

@@ -338,7 +338,7 @@ class Factor:
 
     def profile(self, val_dev_ptr=None):
         """Per-kernel-kind timing of one extra factorization (no graph)."""
-        ms = np.zeros(12); nl = np.zeros(12, dtype=np.int64); fl = np.zeros(12)
+        ms = np.zeros(16); nl = np.zeros(16, dtype=np.int64); fl = np.zeros(12)
         rc = load().sylver_gb300_profile_factor(self.fkeep, val_dev_ptr, _p(ms), _p(nl), _p(fl))
         if rc != 0:
             raise RuntimeError(f"profile failed: {rc}")
@@ -356,11 +356,11 @@ class Factor:
 
     SOLVE_KINDS = ("small_fwd", "small_bwd", "gather_fwd", "gather_bwd", "scatter_fwd",
                    "scatter_bwd", "diag_fwd", "rows_fwd", "rows_bwd", "diag_bwd", "cb_bwd",
-                   "rows_fwd_thread")
+                   "cb_fwd")
 
     def profile_solve(self, nrhs=16):
         """Per-kernel-kind timing of one forward + backward sweep (no graph)."""
-        ms = np.zeros(12); nl = np.zeros(12, dtype=np.int64)
+        ms = np.zeros(16); nl = np.zeros(16, dtype=np.int64)
         rc = load().sylver_gb300_profile_solve(self.fkeep, int(nrhs), _p(ms), _p(nl))
         if rc != 0:
             raise RuntimeError(f"profile_solve failed: {rc}")

@@ -229,17 +229,13 @@ template <typename T, typename ACC>
 void launch_solve_fwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
                       ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
                       bool unit_diag, cudaStream_t s);
+// Small fronts (at most maxn pivot rows), one CTA each, pivot rows only:
+// forward y = L11^-1 x(pivots); backward z = L11^-T (x(pivots) - tacc), tacc
+// cleared.  The contribution rows are the LS_RECT_FWD / LS_RECT_BWD launches.
 template <typename T, typename ACC>
-void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
-                      ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
+void launch_small_tri(bool fwd, const T* arena, const FrontDesc* fr, int nfronts,
+                      const int* rlist, ACC* x, ACC* tacc, int n, int nrhs, int maxn,
                       bool unit_diag, cudaStream_t s);
-// Fronts of at most maxm rows with their right-hand-side rows on chip
-// (forward or backward); false, launching nothing, when maxm x nrhs rows do
-// not fit.
-template <typename T, typename ACC>
-bool launch_solve_small(bool fwd, const T* arena, const FrontDesc* fr, int nfronts,
-                        const int* rlist, ACC* x, int n, int nrhs, int maxm, bool unit_diag,
-                        cudaStream_t s);
 
 // Large-front blocked sweeps (block width 64).  Task f indexes the level's
 // FrontDesc array; c0/bw give the diagonal block, r0 the first row of a tile.
@@ -251,23 +247,27 @@ struct LTask {
 enum LsKind {
   LS_GATHER_FWD, LS_GATHER_BWD, LS_SCATTER_FWD, LS_SCATTER_BWD,
   LS_FWD_DIAG2, LS_FWD_UPD2, LS_BWD_RED2, LS_BWD_DIAG2,
-  LS_BWD_CB,   // contribution rows' share of every block, once before the steps (backward)
-  LS_FWD_ROWS  // forward update with one row per thread (steps with many rows)
+  LS_RECT_BWD,  // contribution rows' share of every pivot row, before the level (backward)
+  LS_RECT_FWD,  // contribution rows' update from all pivot rows, after the level (forward)
+  LS_SMALL_TRI  // the level's small fronts (launch_small_tri)
 };
 constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
 constexpr int LSOLVE_BW2 = 256;  // columns per solve step
 constexpr int LSOLVE_UPD_ROWS = 32;  // rows per forward-update CTA
 constexpr int LSOLVE_RED_ROWS = 64;  // rows per backward-reduction CTA
-constexpr int LSOLVE_CB_ROWS = 256;  // contribution rows per backward CB CTA
-constexpr int LSOLVE_ROWS_T = 128;   // rows per one-row-per-thread forward-update CTA
-// Large fronts are swept block by block; the backward steps reduce over the
-// fully-summed rows only, because the contribution rows (>= n) contribute to
-// every backward block once, before the backward blocks (LS_BWD_CB).
+constexpr int RECT_FWD_T = 128;      // threads of an LS_RECT_FWD task (two contribution rows each)
+constexpr int RECT_BWD_COLS = 128;   // pivot columns per LS_RECT_BWD task
+constexpr int RECT_BWD_T = 128;      // threads of an LS_RECT_BWD task (two columns each, two row halves)
+constexpr int RECT_BWD_ROWS = 256;   // contribution rows per LS_RECT_BWD task
+// Large fronts are swept block by block over their fully-summed rows only.
+// The contribution rows (>= n) of every front of a level are one separate
+// launch per direction: forward after the pivot rows are solved (x(cb) -=
+// L21 y, LS_RECT_FWD), backward before them (tacc(pivots) = L21^T x(cb),
+// LS_RECT_BWD; the pivot rows' gather subtracts and clears it).
 // Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
 // explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
 // index), tt: two 256 x 32 accumulators per front (backward steps alternate
-// between them; the backward gather clears both), cnt: one ticket counter
-// per front.
+// between them; the backward gather clears both).
 template <typename T, typename ACC>
 struct LsArgs {
   const T* arena;
@@ -281,13 +281,12 @@ struct LsArgs {
   const T* inv;
   const int64_t* inv_off;
   ACC* tt;
-  unsigned* cnt;
   const T* inv2;            // 256x256 inverses of the solve-step diagonal blocks
   const int64_t* inv2_off;  // per front of the level
   const T* inv2t;           // the same inverses transposed (row-major)
-  // per 256-column block of every large front: the contribution rows' share
-  // of the backward reduction, 256 x 32 (block index inv2_off[f]/256^2 + c0/256)
-  ACC* tcb;
+  // contribution rows' share of the backward reduction, laid out like x
+  // (n x nrhs, column stride n); zero between backward sweeps
+  ACC* tacc;
 };
 // Inverse of each 256-column diagonal block from its 64x64 inverses: task
 // (front f, c0, bw), output at inv2 + inv2_off[f] + (c0/256)*256*256
@@ -299,7 +298,8 @@ void launch_inv256(const T* arena, const FrontDesc* fr, const LTask* tasks, int 
                    const T* inv64, const int64_t* inv_off, T* inv2, T* inv2t,
                    const int64_t* inv2_off, cudaStream_t s);
 template <typename T, typename ACC>
-void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cudaStream_t s);
+void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, int aux,
+                   cudaStream_t s);
 // Explicit inverse of each diagonal block: task (front f, c0, bw), output at
 // inv + inv_off[f] + (c0/64)*64*64, column-major 64 x 64, identity padded.
 template <typename T>

@@ -22,9 +22,12 @@ constexpr int SB = 32;      // column block
 constexpr int MAXR = 32;    // right-hand sides per launch
 constexpr int RC = 8;       // right-hand sides per register chunk
 constexpr int GB = 8;       // gather/scatter elements in flight per thread
-// dynamic shared memory of the on-chip small-front kernels (right-hand-side
-// rows and their destinations)
-constexpr size_t SMALL_SOLVE_SMEM = 160 * 1024;
+// dynamic shared memory of the small-front triangle kernel (pivot rows of the
+// right-hand sides and their destinations)
+constexpr size_t TRI_SMEM = 96 * 1024;
+// right-hand sides per pass of the contribution-row kernels: 4 for a few,
+// else 16 (FP32) / 8 (FP64), more in several passes
+template <typename ACC> constexpr int RQ_MID = sizeof(ACC) == 8 ? 8 : 16;
 
 template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
 
@@ -142,264 +145,86 @@ __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
   }
 }
 
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_solve_bwd(const T* __restrict__ arena,
-                                                   const FrontDesc* __restrict__ fr,
-                                                   const int* __restrict__ rlist,
-                                                   ACC* __restrict__ x, int n, int nrhs,
-                                                   ACC* __restrict__ scratch,
-                                                   const int64_t* __restrict__ scr_off,
-                                                   bool unit) {
-  __shared__ ACC tt[SB][MAXR];
-  __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
-  const FrontDesc f = fr[blockIdx.x];
-  const T* L = arena + f.off;
-  const int ld = f.ld, m = f.m, nc = f.n;
-  const int* rl = rlist + f.rl;
-  ACC* xs = scratch + scr_off[blockIdx.x] * nrhs;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int nwarps = blockDim.x >> 5;
-  for (int base = 0; base < m * nrhs; base += GB * 256) {
-    ACC v[GB];
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int idx = base + tid + 256 * u, i = idx % m, r = idx / m;
-      v[u] = idx < m * nrhs ? x[(int64_t)r * n + rl[i]] : ACC(0);
-    }
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int idx = base + tid + 256 * u;
-      if (idx < m * nrhs) xs[idx] = v[u];
-    }
-  }
-  __shared__ ACC rdg[SB];
-  __syncthreads();
-  const int nblk = (nc + SB - 1) / SB;
-  for (int b = nblk - 1; b >= 0; --b) {
-    const int c0 = b * SB, bw = min(SB, nc - c0), c1 = c0 + bw;
-    for (int kk = warp; kk < bw; kk += nwarps) {
-      const T* col = L + (int64_t)(c0 + kk) * ld;
-      for (int r0 = 0; r0 < nrhs; r0 += RC) {
-        ACC acc[RC];
-#pragma unroll
-        for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
-#pragma unroll 4
-        for (int i = c1 + lane; i < m; i += 32) {
-          ACC l = (ACC)col[i];
-#pragma unroll
-          for (int q = 0; q < RC; ++q)
-            if (r0 + q < nrhs) acc[q] += l * xs[(int64_t)(r0 + q) * m + i];
-        }
-#pragma unroll
-        for (int q = 0; q < RC; ++q) {
-          ACC s = acc[q];
-          for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-          if (lane == 0 && r0 + q < nrhs) tt[kk][r0 + q] = s;
-        }
-      }
-    }
-    {
-      ACC lv[SB * SB / 256];
-#pragma unroll
-      for (int u = 0; u < SB * SB / 256; ++u) {
-        const int e = tid + 256 * u, i = e % SB, k = e / SB;
-        lv[u] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
-      }
-#pragma unroll
-      for (int u = 0; u < SB * SB / 256; ++u) {
-        const int e = tid + 256 * u;
-        Ld[e / SB][e % SB] = lv[u];
-        if (e % SB == e / SB) rdg[e % SB] = (e % SB < bw && !unit) ? ACC(1) / lv[u] : ACC(1);
-      }
-    }
-    __syncthreads();
-    // diagonal block (transposed): one right-hand side per warp at a time
-    for (int r = warp; r < nrhs; r += nwarps) {
-      ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] - tt[lane][r] : ACC(0);
-      for (int kk = bw - 1; kk >= 0; --kk) {
-        if (lane == kk) v = v * rdg[kk];
-        ACC zk = __shfl_sync(0xffffffffu, v, kk);
-        if (lane < kk) v -= Ld[lane][kk] * zk;
-      }
-      if (lane < bw) xs[(int64_t)r * m + c0 + lane] = v;
-    }
-    __syncthreads();
-  }
-  for (int base = 0; base < m * nrhs; base += GB * 256) {
-    ACC v[GB];
-    int dsti[GB];
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int idx = base + tid + 256 * u, i = idx % m;
-      const bool ok = idx < m * nrhs && i < nc;
-      v[u] = ok ? xs[idx] : ACC(0);
-      dsti[u] = ok ? rl[i] : -1;
-    }
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int idx = base + tid + 256 * u;
-      if (dsti[u] >= 0) x[(int64_t)(idx / m) * n + dsti[u]] = v[u];
-    }
-  }
-}
-
-// Small fronts whose right-hand-side rows fit in shared memory: the rows
-// (ys[r*m + i], r < nrhs) and their destinations stay on chip from the gather
-// to the scatter, so the column blocks touch global memory only for L.
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(256, sizeof(ACC) == 4 ? 3 : 2) k_solve_fwd_s(const T* __restrict__ arena,
-                                                     const FrontDesc* __restrict__ fr,
-                                                     const int* __restrict__ rlist,
-                                                     ACC* __restrict__ x, int n, int nrhs,
-                                                     bool unit) {
+// Small fronts, pivot rows only.  The front's n fully-summed rows of the
+// right-hand sides (ys[r*n + i], r < nrhs) and its row list stay in shared
+// memory from the gather to the write-back.
+//   forward   y = L11^-1 x(pivots), written back to x; the contribution rows
+//             receive -L21 y afterwards from k_rect_fwd, which reads y there;
+//   backward  z = L11^-T (x(pivots) - t), where t = L21^T x(contribution
+//             rows) was accumulated beforehand by k_rect_bwd into tacc (laid
+//             out like x); the gather takes t and clears it.
+// Column blocks of 32: the warps solve the diagonal block with shuffles, two
+// right-hand sides interleaved per warp; the rest of the triangle is updated
+// (forward) or reduced (backward) from 32-row tiles of L staged in shared
+// memory, thread (row or column = lane, right-hand sides warp + 8j).
+template <typename T, typename ACC, bool BWD>
+__global__ void __launch_bounds__(256) k_tri(const T* __restrict__ arena,
+                                             const FrontDesc* __restrict__ fr,
+                                             const int* __restrict__ rlist, ACC* __restrict__ x,
+                                             ACC* __restrict__ tacc, int n, int nrhs,
+                                             bool unit) {
   extern __shared__ __align__(16) unsigned char dsm[];
   __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
+  __shared__ ACC Lr[SB][SB + 1];  // backward: Lr[ii][k] = L(r0 + ii, c0 + k)
+  __shared__ ACC tt[SB][MAXR + 1];  // backward: the block's reduction over rows [c1, nc)
   __shared__ ACC rdg[SB];         // 1 / L(c0 + k, c0 + k)
   const FrontDesc f = fr[blockIdx.x];
   const T* L = arena + f.off;
-  const int ld = f.ld, m = f.m, nc = f.n, mr = m * nrhs;
+  const int ld = f.ld, nc = f.n, mr = nc * nrhs;
   ACC* ys = reinterpret_cast<ACC*>(dsm);
   int* rls = reinterpret_cast<int*>(ys + mr);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < m; i += 256) rls[i] = rlist[f.rl + i];
-  __syncthreads();
-  // the pivot rows are gathered; the rows below start at zero and collect
-  // this front's contribution, which the scatter adds to the ancestors'
-  // rows (sibling fronts of the launch add to the same rows)
-  for (int base = 0; base < mr; base += GB * 256) {
-    ACC v[GB];
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int idx = base + tid + 256 * u, i = idx % m;
-      v[u] = (idx < mr && i < nc) ? x[(int64_t)(idx / m) * n + rls[i]] : ACC(0);
-    }
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int idx = base + tid + 256 * u;
-      if (idx < mr) ys[idx] = v[u];
-    }
-  }
-  __syncthreads();
-  for (int c0 = 0; c0 < nc; c0 += SB) {
-    const int bw = min(SB, nc - c0), c1 = c0 + bw;
-    {
-      ACC lv[SB * SB / 256];
-#pragma unroll
-      for (int u = 0; u < SB * SB / 256; ++u) {
-        const int e = tid + 256 * u, i = e % SB, k = e / SB;
-        lv[u] = (i < bw && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + c0 + i] : ACC(0);
-      }
-#pragma unroll
-      for (int u = 0; u < SB * SB / 256; ++u) {
-        const int e = tid + 256 * u;
-        Ld[e / SB][e % SB] = lv[u];
-        if (e % SB == e / SB) rdg[e % SB] = (e % SB < bw && !unit) ? ACC(1) / lv[u] : ACC(1);
-      }
-    }
-    __syncthreads();
-    // diagonal block: one right-hand side per warp at a time
-    for (int r = warp; r < nrhs; r += 8) {
-      ACC v = (lane < bw) ? ys[r * m + c0 + lane] : ACC(0);
-      for (int kk = 0; kk < bw; ++kk) {
-        const ACC vk = __shfl_sync(0xffffffffu, v, kk) * rdg[kk];
-        if (lane == kk) v = vk;
-        if (lane > kk && lane < bw) v -= Ld[kk][lane] * vk;
-      }
-      if (lane < bw) ys[r * m + c0 + lane] = v;
-    }
-    __syncthreads();
-    // rows below the block: one row per thread, its block row of L loaded
-    // at once, eight right-hand sides per pass
-    for (int i = c1 + tid; i < m; i += 256) {
-      ACC lv[SB];
-#pragma unroll
-      for (int kk = 0; kk < SB; ++kk) lv[kk] = (kk < bw) ? (ACC)L[(int64_t)(c0 + kk) * ld + i] : ACC(0);
-      for (int r0 = 0; r0 < nrhs; r0 += RC) {
-        ACC acc[RC];
-#pragma unroll
-        for (int q = 0; q < RC; ++q) acc[q] = ACC(0);
-#pragma unroll
-        for (int kk = 0; kk < SB; ++kk) {
-          const int row = c0 + min(kk, bw - 1);
-#pragma unroll
-          for (int q = 0; q < RC; ++q) acc[q] += lv[kk] * ys[min(r0 + q, nrhs - 1) * m + row];
-        }
-#pragma unroll
-        for (int q = 0; q < RC; ++q)
-          if (r0 + q < nrhs) ys[(r0 + q) * m + i] -= acc[q];
-      }
-    }
-    __syncthreads();
-  }
-  for (int base = 0; base < mr; base += GB * 256) {
-#pragma unroll
-    for (int u = 0; u < GB; ++u) {
-      const int idx = base + tid + 256 * u;
-      if (idx >= mr) break;
-      const int i = idx % m;
-      ACC* dst = x + (int64_t)(idx / m) * n + rls[i];
-      if (i < nc) *dst = ys[idx];
-      else aadd(dst, ys[idx]);
-    }
-  }
-}
-
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(256) k_solve_bwd_s(const T* __restrict__ arena,
-                                                     const FrontDesc* __restrict__ fr,
-                                                     const int* __restrict__ rlist,
-                                                     ACC* __restrict__ x, int n, int nrhs,
-                                                     bool unit) {
-  extern __shared__ __align__(16) unsigned char dsm[];
-  __shared__ ACC tt[SB][MAXR];
-  __shared__ ACC Ld[SB][SB + 1];  // Ld[k][i] = L(c0 + i, c0 + k)
-  __shared__ ACC rdg[SB];
-  const FrontDesc f = fr[blockIdx.x];
-  const T* L = arena + f.off;
-  const int ld = f.ld, m = f.m, nc = f.n, mr = m * nrhs;
-  ACC* ys = reinterpret_cast<ACC*>(dsm);
-  int* rls = reinterpret_cast<int*>(ys + mr);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int i = tid; i < m; i += 256) rls[i] = rlist[f.rl + i];
+  for (int i = tid; i < nc; i += 256) rls[i] = rlist[f.rl + i];
   __syncthreads();
   for (int base = 0; base < mr; base += GB * 256) {
-    ACC v[GB];
+    // every load of the batch issued before the first store
+    ACC v[GB], tv[GB];
+    int64_t gi[GB];
 #pragma unroll
     for (int u = 0; u < GB; ++u) {
       const int idx = base + tid + 256 * u;
-      v[u] = idx < mr ? x[(int64_t)(idx / m) * n + rls[idx % m]] : ACC(0);
+      gi[u] = idx < mr ? (int64_t)(idx / nc) * n + rls[idx % nc] : -1;
+      v[u] = gi[u] >= 0 ? x[gi[u]] : ACC(0);
+      tv[u] = (BWD && gi[u] >= 0) ? tacc[gi[u]] : ACC(0);
     }
 #pragma unroll
     for (int u = 0; u < GB; ++u) {
       const int idx = base + tid + 256 * u;
-      if (idx < mr) ys[idx] = v[u];
+      if (idx < mr) ys[idx] = v[u] - tv[u];
+      if (BWD && gi[u] >= 0) tacc[gi[u]] = ACC(0);
     }
   }
   __syncthreads();
-  constexpr int RB = 16;  // right-hand sides per pass of a column
   const int nblk = (nc + SB - 1) / SB;
-  for (int b = nblk - 1; b >= 0; --b) {
+  for (int bi = 0; bi < nblk; ++bi) {
+    const int b = BWD ? nblk - 1 - bi : bi;
     const int c0 = b * SB, bw = min(SB, nc - c0), c1 = c0 + bw;
-    // tt[kk][r] = sum_{i >= c1} L(i, c0 + kk) x(i, r): one column per warp
-    for (int kk = warp; kk < bw; kk += 8) {
-      const T* col = L + (int64_t)(c0 + kk) * ld;
-      for (int r0 = 0; r0 < nrhs; r0 += RB) {
-        ACC acc[RB];
+    if (BWD) {
+      // tt[k][r] = sum_{i in [c1, nc)} L(i, c0 + k) z(i, r): thread (k =
+      // lane, right-hand sides warp + 8j)
+      ACC acc[MAXR / 8];
 #pragma unroll
-        for (int q = 0; q < RB; ++q) acc[q] = ACC(0);
-#pragma unroll 2
-        for (int i = c1 + lane; i < m; i += 32) {
-          const ACC l = (ACC)col[i];
+      for (int j = 0; j < MAXR / 8; ++j) acc[j] = ACC(0);
+      for (int r0 = c1; r0 < nc; r0 += SB) {
+        const int nrow = min(SB, nc - r0);
 #pragma unroll
-          for (int q = 0; q < RB; ++q) acc[q] += l * ys[min(r0 + q, nrhs - 1) * m + i];
+        for (int u = 0; u < SB * SB / 256; ++u) {
+          const int e = tid + 256 * u, ii = e % SB, k = e / SB;
+          Lr[ii][k] = (ii < nrow && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + r0 + ii] : ACC(0);
         }
+        __syncthreads();
+        for (int ii = 0; ii < nrow; ++ii) {
+          const ACC l = Lr[ii][lane];
 #pragma unroll
-        for (int q = 0; q < RB; ++q) {
-          ACC sv = acc[q];
-          for (int o = 16; o > 0; o >>= 1) sv += __shfl_xor_sync(0xffffffffu, sv, o);
-          if (lane == 0 && r0 + q < nrhs) tt[kk][r0 + q] = sv;
+          for (int j = 0; j < MAXR / 8; ++j) {
+            const int r = warp + 8 * j;
+            if (r < nrhs) acc[j] += l * ys[r * nc + r0 + ii];
+          }
         }
+        __syncthreads();
       }
+#pragma unroll
+      for (int j = 0; j < MAXR / 8; ++j) tt[lane][warp + 8 * j] = acc[j];
     }
     {
       ACC lv[SB * SB / 256];
@@ -416,24 +241,89 @@ __global__ void __launch_bounds__(256) k_solve_bwd_s(const T* __restrict__ arena
       }
     }
     __syncthreads();
-    // diagonal block (transposed): one right-hand side per warp at a time
-    for (int r = warp; r < nrhs; r += 8) {
-      ACC v = (lane < bw) ? ys[r * m + c0 + lane] - tt[lane][r] : ACC(0);
-      for (int kk = bw - 1; kk >= 0; --kk) {
-        if (lane == kk) v = v * rdg[kk];
-        const ACC zk = __shfl_sync(0xffffffffu, v, kk);
-        if (lane < kk) v -= Ld[lane][kk] * zk;
+    // diagonal block: right-hand sides r and r + 8 per warp, interleaved
+    for (int r = warp; r < nrhs; r += 16) {
+      const int r2 = r + 8;
+      const bool two = r2 < nrhs;
+      ACC v = ACC(0), w = ACC(0);
+      if (lane < bw) {
+        v = ys[r * nc + c0 + lane];
+        if (two) w = ys[r2 * nc + c0 + lane];
+        if (BWD) {
+          v -= tt[lane][r];
+          if (two) w -= tt[lane][r2];
+        }
       }
-      if (lane < bw) ys[r * m + c0 + lane] = v;
+      if (!BWD) {
+        for (int kk = 0; kk < bw; ++kk) {
+          const ACC vk = __shfl_sync(0xffffffffu, v, kk) * rdg[kk];
+          const ACC wk = __shfl_sync(0xffffffffu, w, kk) * rdg[kk];
+          if (lane == kk) {
+            v = vk;
+            w = wk;
+          }
+          if (lane > kk && lane < bw) {
+            const ACC l = Ld[kk][lane];
+            v -= l * vk;
+            w -= l * wk;
+          }
+        }
+      } else {
+        for (int kk = bw - 1; kk >= 0; --kk) {
+          if (lane == kk) {
+            v = v * rdg[kk];
+            w = w * rdg[kk];
+          }
+          const ACC zk = __shfl_sync(0xffffffffu, v, kk);
+          const ACC zw = __shfl_sync(0xffffffffu, w, kk);
+          if (lane < kk) {
+            const ACC l = Ld[lane][kk];
+            v -= l * zk;
+            w -= l * zw;
+          }
+        }
+      }
+      if (lane < bw) {
+        ys[r * nc + c0 + lane] = v;
+        if (two) ys[r2 * nc + c0 + lane] = w;
+      }
     }
     __syncthreads();
-  }
-  for (int base = 0; base < nc * nrhs; base += 256) {
-    const int idx = base + tid;
-    if (idx < nc * nrhs) {
-      const int i = idx % nc, r = idx / nc;
-      x[(int64_t)r * n + rls[i]] = ys[r * m + i];
+    if (!BWD) {
+      // rows [c1, nc) of the triangle in 32-row tiles: thread (row ii = lane,
+      // right-hand sides warp + 8j) subtracts L(r0 + ii, block) y(block)
+      for (int r0 = c1; r0 < nc; r0 += SB) {
+        const int nrow = min(SB, nc - r0);
+#pragma unroll
+        for (int u = 0; u < SB * SB / 256; ++u) {
+          const int e = tid + 256 * u, ii = e % SB, k = e / SB;
+          Lr[ii][k] = (ii < nrow && k < bw) ? (ACC)L[(int64_t)(c0 + k) * ld + r0 + ii] : ACC(0);
+        }
+        __syncthreads();
+        ACC acc[MAXR / 8];
+#pragma unroll
+        for (int j = 0; j < MAXR / 8; ++j) acc[j] = ACC(0);
+        for (int k = 0; k < bw; ++k) {
+          const ACC l = Lr[lane][k];
+#pragma unroll
+          for (int j = 0; j < MAXR / 8; ++j) {
+            const int r = warp + 8 * j;
+            if (r < nrhs) acc[j] += l * ys[r * nc + c0 + k];
+          }
+        }
+        if (lane < nrow)
+#pragma unroll
+          for (int j = 0; j < MAXR / 8; ++j) {
+            const int r = warp + 8 * j;
+            if (r < nrhs) ys[r * nc + r0 + lane] -= acc[j];
+          }
+        __syncthreads();
+      }
     }
+  }
+  for (int base = 0; base < mr; base += 256) {
+    const int idx = base + tid;
+    if (idx < mr) x[(int64_t)(idx / nc) * n + rls[idx % nc]] = ys[idx];
   }
 }
 
@@ -585,62 +475,71 @@ __global__ void k_axpy(double* __restrict__ x, int ldx, const double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Large fronts: blocked multi-CTA sweeps with explicit inverses of the 64x64
-// diagonal blocks (computed once per factorization).  Forward step b: every
-// CTA forms y_b = L_bb^-1 x_b itself and updates its own rows below the
-// block; y_b goes to a separate slab so no CTA overwrites what others read.
-// Backward step b: CTAs reduce L_{i,b}^T x_i over their rows into tt, and
-// the last CTA to finish (atomic ticket, no waiting) solves the block.
+// Large fronts: blocked sweeps over the fully-summed rows with explicit
+// inverses of the diagonal blocks (computed once per factorization).  The
+// pivot rows are gathered into a per-front slab (xs), solved block by block
+// (solved rows go to a second slab, ys, so no CTA overwrites what another
+// reads in the same step) and scattered back.  Each step is one launch of
+// independent tasks; the step kernels use programmatic dependent launch.
 
 constexpr int LB = LSOLVE_BW;
 
+// Gather of the pivot rows of a large front, one row per thread (256 rows
+// per task).  The contribution rows are handled by k_rect_fwd / k_rect_bwd
+// straight from x; backward, their share of each pivot row (in tacc) is
+// taken here and cleared, and both backward accumulators of the front start
+// at zero.
 template <typename T, typename ACC>
-__global__ void k_lgather(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
-  const LTask t = tasks[blockIdx.x];
+__device__ __forceinline__ void gather_body(const LTask& t, const LsArgs<T, ACC>& a, bool fwd) {
   const FrontDesc f = a.fr[t.f];
   if (!fwd && t.r0 == 0) {
-    // both backward accumulators of this front start at zero, and so do its
-    // contribution-row sums
     ACC* tf = a.tt + (int64_t)t.f * 2 * LSOLVE_BW2 * MAXR;
     for (int e = threadIdx.x; e < 2 * LSOLVE_BW2 * MAXR; e += blockDim.x) tf[e] = ACC(0);
-    const int nb = (f.n + LSOLVE_BW2 - 1) / LSOLVE_BW2;
-    ACC* cb = a.tcb + (a.inv2_off[t.f] / ((int64_t)LSOLVE_BW2 * LSOLVE_BW2)) * LSOLVE_BW2 * MAXR;
-    for (int e = threadIdx.x; e < nb * LSOLVE_BW2 * MAXR; e += blockDim.x) cb[e] = ACC(0);
   }
   const int i = t.r0 + threadIdx.x;
-  if (i >= f.m) return;
+  if (threadIdx.x >= 256 || i >= f.n) return;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const int v = a.rlist[f.rl + i];
-  const bool zero = fwd && i >= f.n;
   ACC val[MAXR];  // every load in flight before the first store
 #pragma unroll
-  for (int r = 0; r < MAXR; ++r)
-    val[r] = (r < a.nrhs && !zero) ? a.x[(int64_t)r * a.n + v] : ACC(0);
+  for (int r = 0; r < MAXR; ++r) val[r] = r < a.nrhs ? a.x[(int64_t)r * a.n + v] : ACC(0);
+  if (!fwd)
+#pragma unroll
+    for (int r = 0; r < MAXR; ++r)
+      if (r < a.nrhs) {
+        ACC* tp = a.tacc + (int64_t)r * a.n + v;
+        val[r] -= *tp;
+        *tp = ACC(0);
+      }
 #pragma unroll
   for (int r = 0; r < MAXR; ++r)
     if (r < a.nrhs) xs[(int64_t)r * f.m + i] = val[r];
 }
 
+// Scatter of the solved pivot rows (ys) of a large front back to x.
 template <typename T, typename ACC>
-__global__ void k_lscatter(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
-  const LTask t = tasks[blockIdx.x];
+__device__ __forceinline__ void scatter_body(const LTask& t, const LsArgs<T, ACC>& a) {
   const FrontDesc f = a.fr[t.f];
   const int i = t.r0 + threadIdx.x;
-  if (i >= f.m) return;
-  if (!fwd && i >= f.n) return;
-  const int64_t so = a.scr_off[t.f] * a.nrhs;
+  if (threadIdx.x >= 256 || i >= f.n) return;
   const int v = a.rlist[f.rl + i];
-  const ACC* src = (i >= f.n ? a.scratch : a.ys) + so + i;
+  const ACC* src = a.ys + a.scr_off[t.f] * a.nrhs + i;
   ACC val[MAXR];
 #pragma unroll
   for (int r = 0; r < MAXR; ++r) val[r] = r < a.nrhs ? src[(int64_t)r * f.m] : ACC(0);
 #pragma unroll
-  for (int r = 0; r < MAXR; ++r) {
-    if (r >= a.nrhs) break;
-    ACC* dst = a.x + (int64_t)r * a.n + v;
-    if (i >= f.n) aadd(dst, val[r]);
-    else *dst = val[r];
-  }
+  for (int r = 0; r < MAXR; ++r)
+    if (r < a.nrhs) a.x[(int64_t)r * a.n + v] = val[r];
+}
+
+template <typename T, typename ACC>
+__global__ void k_lgather(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
+  gather_body<T, ACC>(tasks[blockIdx.x], a, fwd);
+}
+
+template <typename T, typename ACC>
+__global__ void k_lscatter(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
+  scatter_body<T, ACC>(tasks[blockIdx.x], a);
 }
 
 // X = L^-1 for one diagonal block, thread j computes column j; L is read
@@ -679,7 +578,6 @@ __global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
 constexpr int BW2 = LSOLVE_BW2;
 constexpr int DMV_ROWS = 8;   // rows of the diagonal mat-vec per CTA (32 CTAs per block)
 constexpr int BRED_ROWS = LSOLVE_RED_ROWS;  // rows per backward-reduction CTA
-constexpr int CB_CHUNK = LSOLVE_CB_ROWS;    // contribution rows per backward CB CTA
 template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
 
 // X = inverse of the 256-column diagonal block (column-major, ld 256, lower):
@@ -772,17 +670,6 @@ __global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
     }
 }
 
-// Diagonal block of a 256-column solve step, as a product with its explicit
-// inverse, split over gridDim.y = 4 CTAs of 64 output rows:
-//   forward   y_b = X v,    v = xs(block)        -> ys(block)
-//   backward  z_b = X^T v,  v = xs(block) - tt   -> ys(block)
-// Solved rows (< n) live in ys in both directions, so no CTA overwrites
-// values another CTA of the same launch still reads.
-// (X^T read from the transposed copy, so both directions read the matrix
-// coalesced down a column).  Thread (row i, k-phase g) sums k = g (mod 4);
-// the four phases are reduced through shared memory.  The backward step
-// reads accumulator (c0/256)&1 and clears the other one, which the next
-// (lower) block's reduction fills.
 template <typename ACC> struct Vec4;
 template <> struct Vec4<float> {
   using V = float4;
@@ -793,80 +680,34 @@ template <> struct Vec4<double> {
   static constexpr int W = 2;
 };
 
-// Forward update of rows [r0, r0 + 128) below the block [c0, c0 + bw) of a
-// large front, one row per thread: x(i, :) -= L(i, c0:c0+bw) y(c0:c0+bw, :)
-// with sixteen right-hand sides per pass in registers and the block's solved
-// rows in shared memory.  For steps with many rows (the lower levels, many
-// fronts with narrow blocks), where the k-split update's per-CTA staging and
-// reduction cost more than the product.
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(LSOLVE_ROWS_T) k_fwd_rows(const LTask* __restrict__ tasks,
-                                                            LsArgs<T, ACC> a) {
-  using V = typename Vec4<ACC>::V;
-  constexpr int VW = Vec4<ACC>::W, RP = 16, KU = 16;
-  __shared__ __align__(16) ACC yb[BW2 * RP];  // yb[k*16 + q] = y(c0 + k, rg + q)
-  const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = a.fr[t.f];
-  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
-  const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  const int tid = threadIdx.x, i = t.r0 + tid, bw = t.bw;
-  const T* Li = a.arena + f.off + (int64_t)t.c0 * f.ld + i;
-  for (int rg = 0; rg < a.nrhs; rg += RP) {
-    const int nr = min(RP, a.nrhs - rg);
-    __syncthreads();  // the previous pass's block is no longer read
-    for (int e = tid; e < bw * RP; e += LSOLVE_ROWS_T) {
-      const int k = e % bw, q = e / bw;
-      yb[k * RP + q] = q < nr ? ysl[(int64_t)(rg + q) * f.m + t.c0 + k] : ACC(0);
-    }
-    __syncthreads();
-    if (i >= f.m) continue;
-    ACC acc[RP];
-#pragma unroll
-    for (int q = 0; q < RP; ++q) acc[q] = ACC(0);
-    for (int k0 = 0; k0 < bw; k0 += KU) {
-      ACC l[KU];
-#pragma unroll
-      for (int u = 0; u < KU; ++u)
-        l[u] = (k0 + u < bw) ? (ACC)Li[(int64_t)(k0 + u) * f.ld] : ACC(0);
-#pragma unroll
-      for (int u = 0; u < KU; ++u) {
-        const V* yv = reinterpret_cast<const V*>(yb + min(k0 + u, bw - 1) * RP);
-#pragma unroll
-        for (int q = 0; q < RP / VW; ++q) {
-          const V y4 = yv[q];
-          if constexpr (VW == 4) {
-            acc[4 * q + 0] += l[u] * y4.x;
-            acc[4 * q + 1] += l[u] * y4.y;
-            acc[4 * q + 2] += l[u] * y4.z;
-            acc[4 * q + 3] += l[u] * y4.w;
-          } else {
-            acc[2 * q + 0] += l[u] * y4.x;
-            acc[2 * q + 1] += l[u] * y4.y;
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < RP; ++q)
-      if (q < nr) xs[(int64_t)(rg + q) * f.m + i] -= acc[q];
-  }
+// Diagonal block of a 256-column step as a product with its explicit
+// inverse, DMV_ROWS = 8 output rows per task (32 tasks per block), 256
+// threads:
+//   forward   y_b = X v,    v = xs(block)        -> ys(block)
+//   backward  z_b = X^T v,  v = xs(block) - tt   -> ys(block)
+// (X^T read from the transposed copy, so both directions read the matrix
+// coalesced down a column.)  Thread (row i, k-phase g) sums k = g (mod 32);
+// the phases are reduced through shared memory.  The backward step reads
+// accumulator (c0/256)&1 and clears the other one, which the next (lower)
+// block's reduction fills.  With PDL the inverse slice is staged before the
+// wait for the previous launch.
+template <typename T, typename ACC> constexpr size_t diag_mv_smem() {
+  return sizeof(T) * DMV_ROWS * BW2 +
+         sizeof(ACC) * ((256 / DMV_ROWS) * DMV_ROWS * (RGn<ACC>::v + 1) + BW2 * RGn<ACC>::v);
 }
-
-template <typename T, typename ACC, bool BWD>
-__global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks,
-                                                 LsArgs<T, ACC> a) {
+template <typename T, typename ACC, bool BWD, bool PDL>
+__device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<T, ACC>& a,
+                                          unsigned char* dsm) {
   constexpr int RG = RGn<ACC>::v;
-  constexpr int DR = DMV_ROWS;  // output rows per CTA; 256 / DR k-phases per row
+  constexpr int DR = DMV_ROWS;  // output rows per task; 256 / DR k-phases per row
   constexpr int NG = 256 / DR;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
-  extern __shared__ __align__(16) unsigned char dsm[];
   T* Ms = reinterpret_cast<T*>(dsm);  // Ms[(k - klo)*DR + il] = M(i0 + il, k)
   ACC* part = reinterpret_cast<ACC*>(dsm + sizeof(T) * DR * BW2);  // [NG][DR][RG + 1]
-  __shared__ __align__(16) ACC vb[BW2 * RG];
-  const LTask t = tasks[blockIdx.x];
+  ACC* vb = part + NG * DR * (RG + 1);                               // [BW2][RG]
   const FrontDesc f = a.fr[t.f];
-  const int c0 = t.c0, bw = t.bw, i0 = DR * blockIdx.y;
+  const int c0 = t.c0, bw = t.bw, i0 = DR * sub;
   const int tid = threadIdx.x, il = tid % DR, g = tid / DR, i = i0 + il;
   const int64_t m = f.m;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
@@ -876,19 +717,19 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
   ACC* tf = a.tt + (int64_t)t.f * 2 * BW2 * MAXR;
   ACC* tcur = tf + ((c0 / BW2) & 1) * BW2 * MAXR;
   ACC* tnext = tf + (((c0 / BW2) + 1) & 1) * BW2 * MAXR;
-  const ACC* tcbb = a.tcb + (a.inv2_off[t.f] / ((int64_t)BW2 * BW2) + c0 / BW2) * BW2 * MAXR;
-  // entries k of v (and columns of the matrix slice) this CTA needs
+  // entries k of v (and columns of the matrix slice) this task needs
   const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + DR), nk = khi - klo;
-  pdl_trigger();
+  __syncthreads();  // the previous task's shared data is no longer read
+  if (PDL) pdl_trigger();
   if (i0 < bw) {
-    // the CTA's slice of the inverse, one wave of asynchronous copies
+    // the task's slice of the inverse, one wave of asynchronous copies
     for (int e = tid; e < nk * DR; e += 256) {
       const int rr = e % DR, k = klo + e / DR;
       cp_async(&Ms[e], &M[(int64_t)k * BW2 + i0 + rr]);
     }
   }
-  pdl_wait();
-  // rows beyond the block: nothing to compute (uniform per CTA)
+  if (PDL) pdl_wait();
+  // rows beyond the block: nothing to compute (uniform per task)
   for (int rg = 0; rg < (i0 < bw ? a.nrhs : 0); rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     __syncthreads();
@@ -903,7 +744,7 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
         v[u] = ACC(0);
         if (e < nk * RG && r < nr) {
           v[u] = xs[(int64_t)(rg + r) * m + c0 + k];
-          if (BWD) v[u] -= tcur[k * MAXR + rg + r] + tcbb[k * MAXR + rg + r];
+          if (BWD) v[u] -= tcur[k * MAXR + rg + r];
         }
       }
 #pragma unroll
@@ -955,29 +796,31 @@ __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks
     for (int e = tid; e < DR * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
 }
 
-// rows [r0, r0+32) below the block: xs_i -= L_i,blk y_blk; thread (row,
-// 16-column group g), 512 threads.  The 32 x 256 tile of L is staged in shared memory by one wave
-// of asynchronous copies; y is read as 16-byte vectors (one broadcast per
-// warp).
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ tasks,
-                                                  LsArgs<T, ACC> a) {
-  constexpr int RG = RGn<ACC>::v;
+// Fully-summed rows [r0, r0+32) (< n) below the block: xs_i -= L_i,blk y_blk;
+// NT threads, thread (row, column group g of 256 / (NT/32) columns).  The
+// 32 x 256 tile of L is staged in shared memory by one wave of asynchronous
+// copies; y is read as 16-byte vectors (one broadcast per warp).
+template <typename T, typename ACC, int NT> constexpr size_t upd_smem() {
+  return sizeof(T) * 32 * BW2 +
+         sizeof(ACC) * ((NT / 32) * 32 * (RGn<ACC>::v + 1) + BW2 * RGn<ACC>::v);
+}
+template <typename T, typename ACC, int NT, bool PDL>
+__device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a,
+                                         unsigned char* dsm) {
+  constexpr int RG = RGn<ACC>::v, NGU = NT / 32, KPG = BW2 / NGU;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
-  extern __shared__ __align__(16) unsigned char dsm[];
   T* Lt = reinterpret_cast<T*>(dsm);  // Lt[k*32 + rr] = L(r0 + rr, c0 + k)
-  ACC* red = reinterpret_cast<ACC*>(dsm + sizeof(T) * 32 * BW2);  // [16][32][RG + 1]
-  __shared__ __align__(16) ACC yb[BW2 * RG];
-  const LTask t = tasks[blockIdx.x];
+  ACC* red = reinterpret_cast<ACC*>(dsm + sizeof(T) * 32 * BW2);  // [NGU][32][RG + 1]
+  ACC* yb = red + NGU * 32 * (RG + 1);                              // [BW2][RG]
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
   const int tid = threadIdx.x, rr = tid % 32, g = tid / 32;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  const int nrow = min(32, f.m - t.r0);
+  const int nrow = min(32, f.n - t.r0);  // fully-summed rows only
   const int cfirst = t.c0, clast = t.c0 + t.bw;
-  pdl_trigger();
+  if (PDL) pdl_trigger();
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     ACC acc[RG];
@@ -986,31 +829,31 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
     for (int c0 = cfirst; c0 < clast; c0 += BW2) {
       const int bw = min(BW2, clast - c0);
       __syncthreads();  // the previous block's tiles are no longer read
-      for (int e = tid; e < BW2 * 32; e += 512) {
+      for (int e = tid; e < BW2 * 32; e += NT) {
         const int r2 = e & 31, k = e >> 5;
         if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
         else Lt[e] = T(0);
       }
-      pdl_wait();
+      if (PDL) pdl_wait();
       {
-        constexpr int NL = BW2 * RG / 512;
+        constexpr int NL = BW2 * RG / NT;
         ACC v[NL];
 #pragma unroll
         for (int u = 0; u < NL; ++u) {
-          const int e = tid + 512 * u, k = e % BW2, r = e / BW2;
+          const int e = tid + NT * u, k = e % BW2, r = e / BW2;
           v[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
         }
 #pragma unroll
         for (int u = 0; u < NL; ++u) {
-          const int e = tid + 512 * u;
+          const int e = tid + NT * u;
           yb[(e % BW2) * RG + e / BW2] = v[u];
         }
       }
       cp_async_wait_all();
       __syncthreads();
 #pragma unroll 8
-      for (int kk = 0; kk < 16; ++kk) {
-        const int k = g * 16 + kk;
+      for (int kk = 0; kk < KPG; ++kk) {
+        const int k = g * KPG + kk;
         const ACC l = (ACC)Lt[k * 32 + rr];
         const V* yv = reinterpret_cast<const V*>(yb + k * RG);
 #pragma unroll
@@ -1032,12 +875,12 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
     for (int q = 0; q < RG; ++q) red[(g * 32 + rr) * (RG + 1) + q] = acc[q];
     __syncthreads();
     // 32 rows x RG sums, spread over all threads
-    for (int e = tid; e < 32 * RG; e += 512) {
+    for (int e = tid; e < 32 * RG; e += NT) {
       const int r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
       if (r2 < nrow && q < nr) {
         ACC sum = ACC(0);
 #pragma unroll
-        for (int gg = 0; gg < 16; ++gg) sum += red[(gg * 32 + r2) * (RG + 1) + q];
+        for (int gg = 0; gg < NGU; ++gg) sum += red[(gg * 32 + r2) * (RG + 1) + q];
         xs[(int64_t)(rg + q) * f.m + i2] -= sum;
       }
     }
@@ -1045,149 +888,59 @@ __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ task
   }
 }
 
-// rows [r0, r0+BR) contribute tt[k][r] += sum_i L(i, c0+k) xs(i, r), k < bw.
-// The BR x 256 tile of L is staged in shared memory by one wave of
-// asynchronous copies; thread (column k = tid % 256, row half h = tid / 256),
-// 512 threads, the halves reduced through shared memory.  Every CTA of a
-// step adds into the same accumulator, so taller tiles mean fewer atomics
-// per address.
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ tasks,
-                                                  LsArgs<T, ACC> a) {
-  constexpr int RG = RGn<ACC>::v;
+// Fully-summed rows [r0, r0 + BRED_ROWS) (< n) below the block contribute
+// tt[k][r] += sum_i L(i, c0+k) z(i, r), k < bw, in 32-row sub-tiles of L
+// staged in shared memory by one wave of asynchronous copies; thread (column
+// k = tid % 256, row half h), the halves (NT = 512) reduced through shared
+// memory.  Every task of a step adds into the same accumulator; the
+// contribution rows' share was put into tacc by k_rect_bwd and taken out by
+// the gather.
+template <typename T, typename ACC> constexpr size_t red_smem() {
+  return sizeof(T) * 32 * (BW2 + 1) + sizeof(ACC) * (BW2 * (RGn<ACC>::v + 1) + 32 * RGn<ACC>::v);
+}
+template <typename T, typename ACC, int NT, bool PDL>
+__device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a,
+                                         unsigned char* dsm) {
+  constexpr int RG = RGn<ACC>::v, SR = 32, NH = NT / BW2;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
-  extern __shared__ __align__(16) unsigned char dsm[];
-  constexpr int BR = BRED_ROWS;
-  T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(BW2+1) + k] = L(r0 + ii, c0 + k)
-  ACC* half = reinterpret_cast<ACC*>(dsm + sizeof(T) * BR * (BW2 + 1));  // [BW2][RG + 1]
-  __shared__ __align__(16) ACC xt[BR][RG];
-  const LTask t = tasks[blockIdx.x];
+  T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(BW2+1) + k] = L(s0 + ii, c0 + k)
+  ACC* half = reinterpret_cast<ACC*>(dsm + sizeof(T) * SR * (BW2 + 1));  // [BW2][RG + 1]
+  ACC* xt = half + BW2 * (RG + 1);                                         // [SR][RG]
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
   const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, k = tid % BW2, h = tid / BW2;
-  // rows below the block: solved rows (< n) in ys, contribution rows in xs
-  const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / BW2) & 1)) * BW2 * MAXR;
-  // fully-summed rows [r0, n) only; the contribution rows' share comes from
-  // k_bwd_cb
-  const int nrow = min(BR, f.n - t.r0);
-  pdl_trigger();
-  for (int e = tid; e < BR * BW2; e += 512) {
-    const int ii = e % BR, kk = e / BR;
-    T* dst = &Lt[ii * (BW2 + 1) + kk];
-    if (ii < nrow && kk < bw) cp_async(dst, &L[(int64_t)(c0 + kk) * f.ld + t.r0 + ii]);
-    else *dst = T(0);
-  }
-  pdl_wait();
+  const int rend = min(t.r0 + BRED_ROWS, f.n);
+  __syncthreads();  // the previous task's shared data is no longer read
+  if (PDL) pdl_trigger();
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    for (int e = tid; e < BR * RG; e += blockDim.x) {
-      const int ii = e % BR, r = e / BR, row = t.r0 + ii;
-      const ACC* src = (row < f.n) ? ysl : xs;
-      xt[ii][r] = (ii < nrow && r < nr) ? src[(int64_t)(rg + r) * f.m + row] : ACC(0);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-#pragma unroll 8
-    for (int i2 = 0; i2 < BR / 2; ++i2) {
-      const int ii = h * (BR / 2) + i2;
-      const ACC l = (ACC)Lt[ii * (BW2 + 1) + k];
-      const V* xv = reinterpret_cast<const V*>(&xt[ii][0]);
-#pragma unroll
-      for (int q = 0; q < RG / VW; ++q) {
-        const V x4 = xv[q];
-        if constexpr (VW == 4) {
-          acc[4 * q + 0] += l * x4.x;
-          acc[4 * q + 1] += l * x4.y;
-          acc[4 * q + 2] += l * x4.z;
-          acc[4 * q + 3] += l * x4.w;
-        } else {
-          acc[2 * q + 0] += l * x4.x;
-          acc[2 * q + 1] += l * x4.y;
-        }
-      }
-    }
-    if (h == 1)
-#pragma unroll
-      for (int q = 0; q < RG; ++q) half[k * (RG + 1) + q] = acc[q];
-    __syncthreads();
-    if (h == 0 && k < bw)
-#pragma unroll
-      for (int q = 0; q < RG; ++q)
-        if (q < nr) aadd(&tf[k * MAXR + rg + q], acc[q] + half[k * (RG + 1) + q]);
-    __syncthreads();
-  }
-}
-
-// Contribution rows of a front, backward: their share of block c0's
-// reduction, tcb(k, r) += sum_i L(i, c0+k) x(i, r) over the CB_CHUNK rows
-// [r0, r0 + CB_CHUNK) >= n, in 32-row sub-tiles staged with double-buffered
-// cp.async; one set of atomics per CTA.  Thread (column k = tid % 256, row
-// half h = tid / 256), 512 threads.
-template <typename T, typename ACC>
-__global__ void __launch_bounds__(512) k_bwd_cb(const LTask* __restrict__ tasks,
-                                                LsArgs<T, ACC> a) {
-  constexpr int RG = RGn<ACC>::v;
-  constexpr int SR = 32;
-  using V = typename Vec4<ACC>::V;
-  constexpr int VW = Vec4<ACC>::W;
-  extern __shared__ __align__(16) unsigned char dsm[];
-  T* Lt = reinterpret_cast<T*>(dsm);  // [2][SR*(BW2+1)]
-  ACC* xt = reinterpret_cast<ACC*>(dsm + sizeof(T) * 2 * SR * (BW2 + 1));  // [2][SR*RG]
-  ACC* half = xt + 2 * SR * RG;       // [BW2][RG + 1]
-  const LTask t = tasks[blockIdx.x];
-  const FrontDesc f = a.fr[t.f];
-  const T* L = a.arena + f.off;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, k = tid % BW2, h = tid / BW2;
-  const ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
-  ACC* tf = a.tcb + (a.inv2_off[t.f] / ((int64_t)BW2 * BW2) + c0 / BW2) * BW2 * MAXR;
-  const int rend = min(t.r0 + CB_CHUNK, f.m);
-  const int nsub = (rend - t.r0 + SR - 1) / SR;
-  for (int rg = 0; rg < a.nrhs; rg += RG) {
-    const int nr = min(RG, a.nrhs - rg);
-    ACC acc[RG];
-#pragma unroll
-    for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    auto issue = [&](int sub, int buf) {
-      const int s0 = t.r0 + sub * SR, nrow = min(SR, rend - s0);
-      T* dst = Lt + buf * SR * (BW2 + 1);
-      for (int e = tid; e < SR * BW2; e += 512) {
+    for (int s0 = t.r0; s0 < rend; s0 += SR) {
+      const int nrow = min(SR, rend - s0);
+      __syncthreads();  // the previous sub-tile is no longer read
+      for (int e = tid; e < SR * BW2; e += NT) {
         const int ii = e % SR, kk = e / SR;
-        T* d = &dst[ii * (BW2 + 1) + kk];
-        if (ii < nrow && kk < bw) cp_async(d, &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]);
-        else *d = T(0);
+        T* dst = &Lt[ii * (BW2 + 1) + kk];
+        if (ii < nrow && kk < bw) cp_async(dst, &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]);
+        else *dst = T(0);
       }
-      ACC* xd = xt + buf * SR * RG;
-      for (int e = tid; e < SR * RG; e += 512) {
+      if (PDL) pdl_wait();
+      for (int e = tid; e < SR * RG; e += NT) {
         const int ii = e % SR, r = e / SR;
-        if (ii < nrow && r < nr) cp_async(&xd[ii * RG + r], &xs[(int64_t)(rg + r) * f.m + s0 + ii]);
-        else xd[ii * RG + r] = ACC(0);
+        xt[ii * RG + r] = (ii < nrow && r < nr) ? ysl[(int64_t)(rg + r) * f.m + s0 + ii] : ACC(0);
       }
-      asm volatile("cp.async.commit_group;" ::: "memory");
-    };
-    __syncthreads();
-    issue(0, 0);
-    for (int sub = 0; sub < nsub; ++sub) {
-      const int buf = sub & 1;
-      if (sub + 1 < nsub) {
-        issue(sub + 1, buf ^ 1);
-        asm volatile("cp.async.wait_group 1;" ::: "memory");
-      } else {
-        asm volatile("cp.async.wait_group 0;" ::: "memory");
-      }
+      cp_async_wait_all();
       __syncthreads();
-      const T* lt = Lt + buf * SR * (BW2 + 1);
-      const ACC* xb = xt + buf * SR * RG;
 #pragma unroll 8
-      for (int i2 = 0; i2 < SR / 2; ++i2) {
-        const int ii = h * (SR / 2) + i2;
-        const ACC l = (ACC)lt[ii * (BW2 + 1) + k];
-        const V* xv = reinterpret_cast<const V*>(&xb[ii * RG]);
+      for (int i2 = 0; i2 < SR / NH; ++i2) {
+        const int ii = h * (SR / NH) + i2;
+        const ACC l = (ACC)Lt[ii * (BW2 + 1) + k];
+        const V* xv = reinterpret_cast<const V*>(&xt[ii * RG]);
 #pragma unroll
         for (int q = 0; q < RG / VW; ++q) {
           const V x4 = xv[q];
@@ -1202,35 +955,301 @@ __global__ void __launch_bounds__(512) k_bwd_cb(const LTask* __restrict__ tasks,
           }
         }
       }
-      __syncthreads();  // buffer buf is read; the next issue may overwrite it
     }
-    if (h == 1)
+    if (NH == 2) {
+      if (h == 1)
 #pragma unroll
-      for (int q = 0; q < RG; ++q) half[k * (RG + 1) + q] = acc[q];
-    __syncthreads();
+        for (int q = 0; q < RG; ++q) half[k * (RG + 1) + q] = acc[q];
+      __syncthreads();
+    }
     if (h == 0 && k < bw)
 #pragma unroll
       for (int q = 0; q < RG; ++q)
-        if (q < nr) aadd(&tf[k * MAXR + rg + q], acc[q] + half[k * (RG + 1) + q]);
+        if (q < nr) aadd(&tf[k * MAXR + rg + q], acc[q] + (NH == 2 ? half[k * (RG + 1) + q] : ACC(0)));
+    __syncthreads();
+  }
+}
+
+template <typename T, typename ACC, bool BWD>
+__global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks,
+                                                 LsArgs<T, ACC> a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  diag_body<T, ACC, BWD, true>(tasks[blockIdx.x], blockIdx.y, a, dsm);
+}
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ tasks,
+                                                  LsArgs<T, ACC> a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  upd_body<T, ACC, 512, true>(tasks[blockIdx.x], a, dsm);
+}
+template <typename T, typename ACC>
+__global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ tasks,
+                                                  LsArgs<T, ACC> a) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  red_body<T, ACC, 512, true>(tasks[blockIdx.x], a, dsm);
+}
+
+// 16-byte asynchronous copy global -> shared (both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// The contribution-row kernels read L in 16-byte pieces of a column: every
+// front's storage starts on a 64-element boundary with a leading dimension
+// that is a multiple of 4, so a piece that starts on a row divisible by 4 is
+// 16-byte aligned (and lies inside the column's padded length).
+constexpr int RF_KU = 8;   // columns of L in flight per thread (forward)
+constexpr int RB_SR = 16;  // rows per pipeline slice (backward)
+template <typename T> constexpr int rb_nst() { return sizeof(T) == 8 ? 3 : 4; }
+// padded column run of a slice: 16-byte aligned, and lanes RB_LP apart hit
+// distinct banks with 16-byte reads
+template <typename T> constexpr int rb_lp() { return RB_SR + 16 / (int)sizeof(T); }
+template <typename T> struct Pair;
+template <> struct Pair<float> {
+  using V = float2;
+};
+template <> struct Pair<double> {
+  using V = double2;
+};
+
+// Contribution rows (i >= n) of a front, forward: x(rls[i], :) -= L(i, c0:c0+bw)
+// y with y = x(rls[c0:c0+bw], :), the front's solved pivot rows, for the rows
+// [r0, r0 + 2 RECT_FWD_T) of the task (r0 divisible by 4; rows below n in
+// the first tile are skipped).  Thread t owns the adjacent rows r0 + 2t and
+// r0 + 2t + 1 and reads them from each column as one 8-byte (FP32) or
+// 16-byte (FP64) load straight into registers, the next RF_KU columns in
+// flight while the current ones are multiplied; the task's block of y (RQ
+// right-hand sides per pass) is staged in shared memory and read as 16-byte
+// vectors that serve both rows.  Sibling fronts of a level share ancestor
+// rows, so the results are added with atomics.  Dynamic shared memory:
+// rect_fwd_smem(kpad), kpad >= every task's bw rounded up to RF_KU.
+template <typename T, typename ACC, int RQ>
+__global__ void __launch_bounds__(RECT_FWD_T) k_rect_fwd(const LTask* __restrict__ tasks,
+                                                         LsArgs<T, ACC> a) {
+  using V = typename Vec4<ACC>::V;
+  using P2 = typename Pair<T>::V;
+  constexpr int VW = Vec4<ACC>::W, KU = RF_KU;
+  static_assert(RQ % VW == 0, "right-hand sides per pass");
+  extern __shared__ __align__(16) unsigned char dsm[];
+  int* rc = reinterpret_cast<int*>(dsm);        // [BW2] pivot rows of the block
+  ACC* yb = reinterpret_cast<ACC*>(rc + BW2);   // [kpad][RQ]
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  const int* rl = a.rlist + f.rl;
+  const int tid = threadIdx.x, bw = t.bw, i0 = t.r0 + 2 * tid;
+  const bool live0 = i0 >= f.n && i0 < f.m, live1 = i0 + 1 >= f.n && i0 + 1 < f.m;
+  const bool any = i0 < f.m;  // rows beyond m: padding of the column, never used
+  const int dst0 = live0 ? rl[i0] : 0, dst1 = live1 ? rl[i0 + 1] : 0;
+  const P2* Lp = reinterpret_cast<const P2*>(a.arena + f.off + (int64_t)t.c0 * f.ld + (any ? i0 : t.r0));
+  const int64_t lds = f.ld / 2;  // column stride in pairs
+  const int kpad = (bw + KU - 1) / KU * KU;
+  for (int k = tid; k < bw; k += RECT_FWD_T) rc[k] = rl[t.c0 + k];
+  for (int rg = 0; rg < a.nrhs; rg += RQ) {
+    const int nr = min(RQ, a.nrhs - rg);
+    __syncthreads();  // rc written; the previous pass's block is no longer read
+    for (int e = tid; e < kpad * RQ; e += RECT_FWD_T) {
+      const int q = e % RQ, k = e / RQ;
+      if (k < bw && q < nr) cp_async(&yb[e], &a.x[(int64_t)(rg + q) * a.n + rc[k]]);
+      else yb[e] = ACC(0);
+    }
+    P2 ln[KU];
+#pragma unroll
+    for (int u = 0; u < KU; ++u) ln[u] = (any && u < bw) ? Lp[u * lds] : P2{};
+    cp_async_wait_all();
+    __syncthreads();
+    ACC acc0[RQ], acc1[RQ];
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) acc0[q] = acc1[q] = ACC(0);
+    for (int k0 = 0; k0 < bw; k0 += KU) {
+      P2 lc[KU];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) lc[u] = ln[u];
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        const int k = k0 + KU + u;
+        ln[u] = (any && k < bw) ? Lp[(int64_t)k * lds] : P2{};
+      }
+#pragma unroll
+      for (int u = 0; u < KU; ++u) {
+        const ACC l0 = (ACC)lc[u].x, l1 = (ACC)lc[u].y;
+        const V* yv = reinterpret_cast<const V*>(yb + (k0 + u) * RQ);
+#pragma unroll
+        for (int q = 0; q < RQ / VW; ++q) {
+          const V y4 = yv[q];
+          if constexpr (VW == 4) {
+            acc0[4 * q + 0] += l0 * y4.x;
+            acc0[4 * q + 1] += l0 * y4.y;
+            acc0[4 * q + 2] += l0 * y4.z;
+            acc0[4 * q + 3] += l0 * y4.w;
+            acc1[4 * q + 0] += l1 * y4.x;
+            acc1[4 * q + 1] += l1 * y4.y;
+            acc1[4 * q + 2] += l1 * y4.z;
+            acc1[4 * q + 3] += l1 * y4.w;
+          } else {
+            acc0[2 * q + 0] += l0 * y4.x;
+            acc0[2 * q + 1] += l0 * y4.y;
+            acc1[2 * q + 0] += l1 * y4.x;
+            acc1[2 * q + 1] += l1 * y4.y;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < RQ; ++q)
+      if (q < nr) {
+        if (live0) aadd(&a.x[(int64_t)(rg + q) * a.n + dst0], -acc0[q]);
+        if (live1) aadd(&a.x[(int64_t)(rg + q) * a.n + dst1], -acc1[q]);
+      }
+  }
+}
+
+// Contribution rows of a front, backward: t(k, :) = sum_i L(i, c0 + k)
+// x(rls[i], :) over the rows [r0, r0 + RECT_BWD_ROWS) of the task (r0
+// divisible by 4; rows below n are skipped), added into tacc at the block's
+// pivot rows rls[c0 + k] (tacc is laid out like x; the pivot rows' gather
+// reads and clears it).  RB_SR-row slices of the tile of L (up to
+// RECT_BWD_COLS columns, each column a padded run of RB_SR rows so the
+// 16-byte reads of a warp are conflict-free) and of x are copied to shared
+// memory asynchronously, several slices in flight.  Thread (column pair p,
+// row half h) owns columns p and p + RECT_BWD_COLS / 2, so each 16-byte read
+// of x serves two columns; the halves are reduced through shared memory,
+// one set of atomics per task.
+template <typename T, typename ACC, int RQ>
+__global__ void __launch_bounds__(RECT_BWD_T) k_rect_bwd(const LTask* __restrict__ tasks,
+                                                         LsArgs<T, ACC> a) {
+  using V = typename Vec4<ACC>::V;
+  constexpr int VW = Vec4<ACC>::W, SR = RB_SR, KC = RECT_BWD_COLS, NT = RECT_BWD_T;
+  constexpr int NP = KC / 2, HR = SR / 2;  // column pairs; rows of a slice per half
+  constexpr int NST = rb_nst<T>(), LP = rb_lp<T>(), CH = 16 / sizeof(T);
+  static_assert(RQ % VW == 0 && NT == 2 * NP && HR % CH == 0, "thread layout");
+  extern __shared__ __align__(16) unsigned char dsm[];
+  T* Ls = reinterpret_cast<T*>(dsm);                        // [NST][KC][LP]
+  ACC* xt = reinterpret_cast<ACC*>(Ls + NST * KC * LP);     // [NST][SR][RQ]
+  ACC* half = xt + NST * SR * RQ;                           // [KC][RQ + 1]
+  int* rr = reinterpret_cast<int*>(half + KC * (RQ + 1));  // [RECT_BWD_ROWS]
+  const LTask t = tasks[blockIdx.x];
+  const FrontDesc f = a.fr[t.f];
+  const T* Lc = a.arena + f.off + (int64_t)t.c0 * f.ld + t.r0;
+  const int* rl = a.rlist + f.rl;
+  const int bw = t.bw, tid = threadIdx.x, p = tid % NP, h = tid / NP;
+  const int rows = min(RECT_BWD_ROWS, f.m - t.r0), nst = (rows + SR - 1) / SR;
+  const int rlo = f.n - t.r0;  // rows of the tile below this one are pivot rows: skipped
+  for (int ii = tid; ii < rows; ii += NT) rr[ii] = rl[t.r0 + ii];
+  auto issue = [&](int st, int rg, int nr) {
+    T* d = Ls + (st % NST) * KC * LP;
+    for (int e = tid; e < KC * SR / CH; e += NT) {
+      const int kk = e / (SR / CH), row = (e % (SR / CH)) * CH, grow = st * SR + row;
+      T* dp = d + kk * LP + row;
+      if (kk < bw && grow < rows) cp_async16(dp, Lc + (int64_t)kk * f.ld + grow);
+      else *reinterpret_cast<float4*>(dp) = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    ACC* dx = xt + (st % NST) * SR * RQ;
+    for (int e = tid; e < SR * RQ; e += NT) {
+      const int r = e % RQ, ii = e / RQ, grow = st * SR + ii;
+      if (grow >= rlo && grow < rows && r < nr)
+        cp_async(&dx[e], &a.x[(int64_t)(rg + r) * a.n + rr[grow]]);
+      else dx[e] = ACC(0);
+    }
+  };
+  for (int rg = 0; rg < a.nrhs; rg += RQ) {
+    const int nr = min(RQ, a.nrhs - rg);
+    __syncthreads();  // rr written; the previous pass's buffers are no longer read
+#pragma unroll
+    for (int st = 0; st < NST - 1; ++st) {
+      if (st < nst) issue(st, rg, nr);
+      cp_async_commit();
+    }
+    ACC acc0[RQ], acc1[RQ];
+#pragma unroll
+    for (int q = 0; q < RQ; ++q) acc0[q] = acc1[q] = ACC(0);
+    for (int s = 0; s < nst; ++s) {
+      cp_async_wait<NST - 2>();
+      __syncthreads();  // slice s landed for all; slice s - 1's buffers are free
+      if (s + NST - 1 < nst) issue(s + NST - 1, rg, nr);
+      cp_async_commit();
+      const T* l0p = Ls + (s % NST) * KC * LP + p * LP + h * HR;
+      const T* l1p = l0p + NP * LP;
+      const ACC* xb = xt + (s % NST) * SR * RQ + h * HR * RQ;
+#pragma unroll
+      for (int i4 = 0; i4 < HR; i4 += CH) {
+        ACC l0[CH], l1[CH];
+        if constexpr (CH == 4) {
+          const float4 v0 = *reinterpret_cast<const float4*>(l0p + i4);
+          const float4 v1 = *reinterpret_cast<const float4*>(l1p + i4);
+          l0[0] = v0.x; l0[1] = v0.y; l0[2] = v0.z; l0[3] = v0.w;
+          l1[0] = v1.x; l1[1] = v1.y; l1[2] = v1.z; l1[3] = v1.w;
+        } else {
+          const double2 v0 = *reinterpret_cast<const double2*>(l0p + i4);
+          const double2 v1 = *reinterpret_cast<const double2*>(l1p + i4);
+          l0[0] = v0.x; l0[1] = v0.y;
+          l1[0] = v1.x; l1[1] = v1.y;
+        }
+#pragma unroll
+        for (int u = 0; u < CH; ++u) {
+          const V* xv = reinterpret_cast<const V*>(xb + (i4 + u) * RQ);
+#pragma unroll
+          for (int q = 0; q < RQ / VW; ++q) {
+            const V x4 = xv[q];
+            if constexpr (VW == 4) {
+              acc0[4 * q + 0] += l0[u] * x4.x;
+              acc0[4 * q + 1] += l0[u] * x4.y;
+              acc0[4 * q + 2] += l0[u] * x4.z;
+              acc0[4 * q + 3] += l0[u] * x4.w;
+              acc1[4 * q + 0] += l1[u] * x4.x;
+              acc1[4 * q + 1] += l1[u] * x4.y;
+              acc1[4 * q + 2] += l1[u] * x4.z;
+              acc1[4 * q + 3] += l1[u] * x4.w;
+            } else {
+              acc0[2 * q + 0] += l0[u] * x4.x;
+              acc0[2 * q + 1] += l0[u] * x4.y;
+              acc1[2 * q + 0] += l1[u] * x4.x;
+              acc1[2 * q + 1] += l1[u] * x4.y;
+            }
+          }
+        }
+      }
+    }
+    cp_async_wait<0>();
+    if (h == 1)
+#pragma unroll
+      for (int q = 0; q < RQ; ++q) {
+        half[p * (RQ + 1) + q] = acc0[q];
+        half[(p + NP) * (RQ + 1) + q] = acc1[q];
+      }
+    __syncthreads();
+    if (h == 0) {
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int k = p + c * NP;
+        if (k < bw) {
+          const int64_t pr = rl[t.c0 + k];
+#pragma unroll
+          for (int q = 0; q < RQ; ++q)
+            if (q < nr)
+              aadd(&a.tacc[(int64_t)(rg + q) * a.n + pr],
+                   (c == 0 ? acc0[q] : acc1[q]) + half[k * (RQ + 1) + q]);
+        }
+      }
+    }
   }
 }
 
 inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs); }
 
-// dynamic shared memory of the staged solve-step kernels
-template <typename T> constexpr size_t diag_mv_smem() {
-  return sizeof(T) * DMV_ROWS * BW2 + sizeof(T) * 256 * (RGn<T>::v + 1);
+// dynamic shared memory of the contribution-row kernels
+template <typename T, typename ACC, int RQ> constexpr size_t rect_fwd_smem(int kpad) {
+  return sizeof(int) * BW2 + sizeof(ACC) * (size_t)kpad * RQ;
 }
-template <typename T> constexpr size_t fwd_upd_smem() {
-  return sizeof(T) * 32 * BW2 + sizeof(T) * 16 * 32 * (RGn<T>::v + 1);
+template <typename T, typename ACC, int RQ> constexpr size_t rect_bwd_smem() {
+  return sizeof(T) * rb_nst<T>() * RECT_BWD_COLS * rb_lp<T>() +
+         sizeof(ACC) * (rb_nst<T>() * RB_SR * RQ + RECT_BWD_COLS * (RQ + 1)) +
+         sizeof(int) * RECT_BWD_ROWS;
 }
-template <typename T> constexpr size_t bwd_cb_smem() {
-  return sizeof(T) * 2 * 32 * (BW2 + 1) + sizeof(T) * (2 * 32 * RGn<T>::v + BW2 * (RGn<T>::v + 1));
-}
-template <typename T> constexpr size_t bwd_red_smem() {
-  return sizeof(T) * BRED_ROWS * (BW2 + 1) + sizeof(T) * BW2 * (RGn<T>::v + 1);
-}
-
 }  // namespace
 
 template <typename T, typename ACC>
@@ -1243,33 +1262,18 @@ void launch_solve_fwd(const T* arena, const FrontDesc* fr, int nfronts, const in
                                               unit_diag);
 }
 
-template <typename ACC>
-size_t small_solve_smem(int maxm, int nrhs) {
-  return (size_t)maxm * nrhs * sizeof(ACC) + (size_t)maxm * sizeof(int);
-}
-
 template <typename T, typename ACC>
-bool launch_solve_small(bool fwd, const T* arena, const FrontDesc* fr, int nfronts,
-                        const int* rlist, ACC* x, int n, int nrhs, int maxm, bool unit_diag,
-                        cudaStream_t s) {
-  const size_t sm = small_solve_smem<ACC>(maxm, nrhs);
-  if (sm > SMALL_SOLVE_SMEM || nrhs > MAXR) return false;
-  if (nfronts <= 0) return true;
-  if (fwd)
-    k_solve_fwd_s<T, ACC><<<nfronts, 256, sm, s>>>(arena, fr, rlist, x, n, nrhs, unit_diag);
-  else
-    k_solve_bwd_s<T, ACC><<<nfronts, 256, sm, s>>>(arena, fr, rlist, x, n, nrhs, unit_diag);
-  return true;
-}
-
-template <typename T, typename ACC>
-void launch_solve_bwd(const T* arena, const FrontDesc* fr, int nfronts, const int* rlist,
-                      ACC* x, int n, int nrhs, ACC* scratch, const int64_t* scr_off,
+void launch_small_tri(bool fwd, const T* arena, const FrontDesc* fr, int nfronts,
+                      const int* rlist, ACC* x, ACC* tacc, int n, int nrhs, int maxn,
                       bool unit_diag, cudaStream_t s) {
   if (nfronts <= 0) return;
   if (nrhs > MAXR) throw CudaError("solve: more than 32 right-hand sides per launch");
-  k_solve_bwd<T, ACC><<<nfronts, 256, 0, s>>>(arena, fr, rlist, x, n, nrhs, scratch, scr_off,
-                                              unit_diag);
+  const size_t sm = (size_t)maxn * nrhs * sizeof(ACC) + (size_t)maxn * sizeof(int);
+  if (sm > TRI_SMEM) throw CudaError("solve: small front with too many pivot rows");
+  if (fwd)
+    k_tri<T, ACC, false><<<nfronts, 256, sm, s>>>(arena, fr, rlist, x, tacc, n, nrhs, unit_diag);
+  else
+    k_tri<T, ACC, true><<<nfronts, 256, sm, s>>>(arena, fr, rlist, x, tacc, n, nrhs, unit_diag);
 }
 
 template <typename ACC>
@@ -1333,7 +1337,8 @@ void launch_axpy_inplace(double* x, int ldx, const double* d, int n, int nrhs, c
 }
 
 template <typename T, typename ACC>
-void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cudaStream_t s) {
+void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, int aux,
+                   cudaStream_t s) {
   if (ntask <= 0) return;
   if (a.nrhs > MAXR) throw CudaError("solve: more than 32 right-hand sides per launch");
   switch (kind) {
@@ -1346,23 +1351,34 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, cu
       k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
     case LS_FWD_DIAG2:
-      launch_pdl(k_diag_mv<T, ACC, false>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s,
+      launch_pdl(k_diag_mv<T, ACC, false>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T, ACC>(), s,
                  tasks, a);
       break;
     case LS_FWD_UPD2:
-      launch_pdl(k_fwd_upd3<T, ACC>, dim3(ntask), 512, fwd_upd_smem<T>(), s, tasks, a);
+      launch_pdl(k_fwd_upd3<T, ACC>, dim3(ntask), 512, upd_smem<T, ACC, 512>(), s, tasks, a);
       break;
-    case LS_BWD_CB:
-      k_bwd_cb<T, ACC><<<ntask, 512, bwd_cb_smem<T>(), s>>>(tasks, a);
+    case LS_RECT_FWD: {
+      // aux: the widest task's columns rounded up to the pipeline slice
+      const int kpad = std::min(std::max(aux, RF_KU), BW2);
+      if (a.nrhs <= 4)
+        k_rect_fwd<T, ACC, 4><<<ntask, RECT_FWD_T, rect_fwd_smem<T, ACC, 4>(kpad), s>>>(tasks, a);
+      else
+        k_rect_fwd<T, ACC, RQ_MID<ACC>>
+            <<<ntask, RECT_FWD_T, rect_fwd_smem<T, ACC, RQ_MID<ACC>>(kpad), s>>>(tasks, a);
       break;
-    case LS_FWD_ROWS:
-      k_fwd_rows<T, ACC><<<ntask, LSOLVE_ROWS_T, 0, s>>>(tasks, a);
+    }
+    case LS_RECT_BWD:
+      if (a.nrhs <= 4)
+        k_rect_bwd<T, ACC, 4><<<ntask, RECT_BWD_T, rect_bwd_smem<T, ACC, 4>(), s>>>(tasks, a);
+      else
+        k_rect_bwd<T, ACC, RQ_MID<ACC>>
+            <<<ntask, RECT_BWD_T, rect_bwd_smem<T, ACC, RQ_MID<ACC>>(), s>>>(tasks, a);
       break;
     case LS_BWD_RED2:
-      launch_pdl(k_bwd_red3<T, ACC>, dim3(ntask), 512, bwd_red_smem<T>(), s, tasks, a);
+      launch_pdl(k_bwd_red3<T, ACC>, dim3(ntask), 512, red_smem<T, ACC>(), s, tasks, a);
       break;
     case LS_BWD_DIAG2:
-      launch_pdl(k_diag_mv<T, ACC, true>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T>(), s,
+      launch_pdl(k_diag_mv<T, ACC, true>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T, ACC>(), s,
                  tasks, a);
       break;
   }
@@ -1375,24 +1391,32 @@ void launch_inv_diag(const T* arena, const FrontDesc* fr, const LTask* tasks, in
   k_inv_diag<T><<<ntask, LB, 0, s>>>(arena, fr, tasks, inv, inv_off, unit);
 }
 
+template <typename T, int RQ>
+void set_rect_smem() {
+  SG_CUDA(cudaFuncSetAttribute(k_rect_fwd<T, T, RQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)rect_fwd_smem<T, T, RQ>(BW2)));
+  SG_CUDA(cudaFuncSetAttribute(k_rect_bwd<T, T, RQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)rect_bwd_smem<T, T, RQ>()));
+}
+
 template <typename T>
 void prepare_solve_kernels() {
   SG_CUDA(cudaFuncSetAttribute(k_inv256<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(2 * 64 * 65 * sizeof(T))));
   SG_CUDA(cudaFuncSetAttribute(k_diag_mv<T, T, false>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T, T>()));
   SG_CUDA(cudaFuncSetAttribute(k_diag_mv<T, T, true>,
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T>()));
-  SG_CUDA(cudaFuncSetAttribute(k_solve_fwd_s<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)SMALL_SOLVE_SMEM));
-  SG_CUDA(cudaFuncSetAttribute(k_solve_bwd_s<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)SMALL_SOLVE_SMEM));
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T, T>()));
+  SG_CUDA(cudaFuncSetAttribute(k_tri<T, T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)TRI_SMEM));
+  SG_CUDA(cudaFuncSetAttribute(k_tri<T, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)TRI_SMEM));
+  set_rect_smem<T, 4>();
+  set_rect_smem<T, RQ_MID<T>>();
   SG_CUDA(cudaFuncSetAttribute(k_fwd_upd3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)fwd_upd_smem<T>()));
+                               (int)upd_smem<T, T, 512>()));
   SG_CUDA(cudaFuncSetAttribute(k_bwd_red3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)bwd_red_smem<T>()));
-  SG_CUDA(cudaFuncSetAttribute(k_bwd_cb<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)bwd_cb_smem<T>()));
+                               (int)red_smem<T, T>()));
 }
 
 template <typename T>
@@ -1412,9 +1436,9 @@ template void launch_inv256<double>(const double*, const FrontDesc*, const LTask
                                     const double*, const int64_t*, double*, double*,
                                     const int64_t*, cudaStream_t);
 
-template void launch_lsolve<float, float>(int, const LTask*, int, LsArgs<float, float>,
+template void launch_lsolve<float, float>(int, const LTask*, int, LsArgs<float, float>, int,
                                           cudaStream_t);
-template void launch_lsolve<double, double>(int, const LTask*, int, LsArgs<double, double>,
+template void launch_lsolve<double, double>(int, const LTask*, int, LsArgs<double, double>, int,
                                             cudaStream_t);
 template void launch_inv_diag<float>(const float*, const FrontDesc*, const LTask*, int, float*,
                                      const int64_t*, bool, cudaStream_t);
@@ -1423,21 +1447,15 @@ template void launch_inv_diag<double>(const double*, const FrontDesc*, const LTa
 template void launch_solve_fwd<float, float>(const float*, const FrontDesc*, int, const int*,
                                              float*, int, int, float*, const int64_t*, bool,
                                              cudaStream_t);
-template void launch_solve_bwd<float, float>(const float*, const FrontDesc*, int, const int*,
-                                             float*, int, int, float*, const int64_t*, bool,
-                                             cudaStream_t);
 template void launch_solve_fwd<double, double>(const double*, const FrontDesc*, int,
                                                const int*, double*, int, int, double*,
                                                const int64_t*, bool, cudaStream_t);
-template void launch_solve_bwd<double, double>(const double*, const FrontDesc*, int,
-                                               const int*, double*, int, int, double*,
-                                               const int64_t*, bool, cudaStream_t);
-template bool launch_solve_small<float, float>(bool, const float*, const FrontDesc*, int,
-                                               const int*, float*, int, int, int, bool,
+template void launch_small_tri<float, float>(bool, const float*, const FrontDesc*, int,
+                                             const int*, float*, float*, int, int, int, bool,
+                                             cudaStream_t);
+template void launch_small_tri<double, double>(bool, const double*, const FrontDesc*, int,
+                                               const int*, double*, double*, int, int, int, bool,
                                                cudaStream_t);
-template bool launch_solve_small<double, double>(bool, const double*, const FrontDesc*, int,
-                                                 const int*, double*, int, int, int, bool,
-                                                 cudaStream_t);
 template void launch_permute_in<float>(const double*, int, float*, const int*, const double*,
                                        int, int, cudaStream_t);
 template void launch_permute_in<double>(const double*, int, double*, const int*, const double*,

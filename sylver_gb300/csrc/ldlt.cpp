@@ -617,7 +617,7 @@ static void ldlt_solve_t(FKeep& fk, int job, ACC* xp, int nrhs, cudaStream_t s) 
   const int* var = L.dvar.as<int>();
   using T = ACC;  // factors and accumulation share the factor precision
   const T* A = fk.arena.as<T>();
-  fk.splan.ensure_tt(sizeof(ACC), L.scratch_rows * std::min(nrhs, 32));
+  fk.splan.ensure_tt(sizeof(ACC), L.scratch_rows * std::min(nrhs, 32), n);
   fk.replay(job, nrhs, xp, s, [&]() {
     for (int r0 = 0; r0 < nrhs; r0 += 32) {
       int nr = std::min(32, nrhs - r0);

@@ -769,12 +769,39 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
     v.nfront = L.f1 - L.f0;
     v.nsmall = 0;
     while (v.nsmall < v.nfront && !is_large(hfr[L.f0 + v.nsmall])) v.nsmall++;
-    for (int f = 0; f < v.nsmall; ++f) v.small_maxm = std::max(v.small_maxm, hfr[L.f0 + f].m);
+    for (int f = 0; f < v.nsmall; ++f) v.small_maxn = std::max(v.small_maxn, hfr[L.f0 + f].n);
     max_large = std::max(max_large, v.nfront);
     auto push = [&](std::vector<SOp>& ops, int kind, int64_t a) {
       int64_t b = (int64_t)htasks.size();
       if (b > a) ops.push_back({kind, a, b});
     };
+    // contribution rows of every front of the level, one launch per
+    // direction: forward after all pivot rows are solved, backward before
+    // (tiles start on a row divisible by 4, for 16-byte copies of L; the
+    // kernels skip the first tile's rows below n)
+    auto rect = [&](std::vector<SOp>& ops, bool fwd) {
+      int64_t a = (int64_t)htasks.size();
+      const int cw = fwd ? LSOLVE_BW2 : RECT_BWD_COLS;
+      const int rh = fwd ? 2 * RECT_FWD_T : RECT_BWD_ROWS;
+      int wmax = 0;
+      for (int f = 0; f < v.nfront; ++f) {
+        const FrontDesc& d = hfr[L.f0 + f];
+        if (d.m <= d.n) continue;
+        for (int c0 = 0; c0 < d.n; c0 += cw) {
+          const int bw = std::min(cw, d.n - c0);
+          wmax = std::max(wmax, bw);
+          for (int r0 = d.n & ~3; r0 < d.m; r0 += rh) htasks.push_back({f, c0, bw, r0, 0, 0});
+        }
+      }
+      push(ops, fwd ? LS_RECT_FWD : LS_RECT_BWD, a);
+      if (!ops.empty() && ops.back().kind == (fwd ? LS_RECT_FWD : LS_RECT_BWD))
+        ops.back().aux = round_up(wmax, 16);
+    };
+    rect(v.bwd, false);
+    if (v.nsmall > 0) {
+      v.fwd.push_back({LS_SMALL_TRI, 0, 0});
+      v.bwd.push_back({LS_SMALL_TRI, 0, 0});
+    }
     if (v.nsmall < v.nfront) {
       int maxb = 0;
       for (int f = v.nsmall; f < v.nfront; ++f) {
@@ -796,7 +823,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
       auto rows = [&](std::vector<SOp>& ops, int kind) {
         int64_t a = (int64_t)htasks.size();
         for (int f = v.nsmall; f < v.nfront; ++f)
-          for (int r0 = 0; r0 < hfr[L.f0 + f].m; r0 += 256) htasks.push_back({f, 0, 0, r0, 0, 0});
+          for (int r0 = 0; r0 < hfr[L.f0 + f].n; r0 += 256) htasks.push_back({f, 0, 0, r0, 0, 0});
         push(ops, kind, a);
       };
       rows(v.fwd, LS_GATHER_FWD);
@@ -804,21 +831,9 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
       int maxb2 = 0;
       for (int f = v.nsmall; f < v.nfront; ++f)
         maxb2 = std::max(maxb2, (hfr[L.f0 + f].n + LB2 - 1) / LB2);
-      // block steps: forward, over all rows below the block; backward, over
-      // the fully-summed rows (< n) only
+      // block steps over the fully-summed rows (< n) below the block
       auto step = [&](std::vector<SOp>& ops, int kind, int b, bool diag) {
         int64_t a = (int64_t)htasks.size();
-        if (kind == LS_FWD_UPD2) {
-          // steps with rows for at least two one-row-per-thread CTAs per SM
-          // use that update; the k-split update keeps the top levels busy
-          int64_t rows = 0;
-          for (int f = v.nsmall; f < v.nfront; ++f) {
-            const FrontDesc& d = hfr[L.f0 + f];
-            const int c1 = std::min(d.n, (b + 1) * LB2);
-            if (b * LB2 < d.n) rows += d.m - c1;
-          }
-          if (rows >= (int64_t)2 * 152 * LSOLVE_ROWS_T) kind = LS_FWD_ROWS;
-        }
         for (int f = v.nsmall; f < v.nfront; ++f) {
           const FrontDesc& d = hfr[L.f0 + f];
           int c0 = b * LB2;
@@ -826,9 +841,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           int bw = std::min(LB2, d.n - c0), c1 = c0 + bw;
           if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
           else if (kind == LS_FWD_UPD2)
-            for (int r0 = c1; r0 < d.m; r0 += LSOLVE_UPD_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
-          else if (kind == LS_FWD_ROWS)
-            for (int r0 = c1; r0 < d.m; r0 += LSOLVE_ROWS_T) htasks.push_back({f, c0, bw, r0, 0, 0});
+            for (int r0 = c1; r0 < d.n; r0 += LSOLVE_UPD_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
           else
             for (int r0 = c1; r0 < d.n; r0 += LSOLVE_RED_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
         }
@@ -840,23 +853,13 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
       }
       rows(v.fwd, LS_SCATTER_FWD);
       rows(v.bwd, LS_GATHER_BWD);
-      {
-        // contribution rows' share of every block, before the block steps
-        int64_t a = (int64_t)htasks.size();
-        for (int f = v.nsmall; f < v.nfront; ++f) {
-          const FrontDesc& d = hfr[L.f0 + f];
-          for (int c0 = 0; c0 < d.n; c0 += LB2)
-            for (int r0 = d.n; r0 < d.m; r0 += LSOLVE_CB_ROWS)
-              htasks.push_back({f, c0, std::min(LB2, d.n - c0), r0, 0, 0});
-        }
-        push(v.bwd, LS_BWD_CB, a);
-      }
       for (int b = maxb2 - 1; b >= 0; --b) {
         step(v.bwd, LS_BWD_RED2, b, false);
         step(v.bwd, LS_BWD_DIAG2, b, true);
       }
       rows(v.bwd, LS_SCATTER_BWD);
     }
+    rect(v.fwd, true);
     lv.push_back(std::move(v));
   }
   tasks.upload(htasks, s);
@@ -864,8 +867,6 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
   inv_off.upload(hinv_off, s);
   invt2.upload(hinv2, s);
   inv2_off.upload(hinv2_off, s);
-  cnt.ensure((size_t)std::max(max_large, 1) * sizeof(unsigned));
-  SG_CUDA(cudaMemsetAsync(cnt.p, 0, cnt.bytes, s));
 }
 
 template <typename T>
@@ -884,16 +885,17 @@ template void SolvePlan::compute_inverses<float>(const float*, const FrontDesc*,
 template void SolvePlan::compute_inverses<double>(const double*, const FrontDesc*, bool,
                                                   cudaStream_t);
 
-void SolvePlan::ensure_tt(size_t elem, int64_t scratch_elems) {
+void SolvePlan::ensure_tt(size_t elem, int64_t scratch_elems, int n) {
   const void* before = tt.p;
   tt.ensure((size_t)std::max(max_large, 1) * 2 * LSOLVE_BW2 * 32 * elem);
   // the backward steps leave the accumulators zero; a new buffer starts zero
   if (tt.p != before) SG_CUDA(cudaMemset(tt.p, 0, tt.bytes));
   ys.ensure((size_t)std::max<int64_t>(scratch_elems, 1) * elem);
-  // one 256 x 32 block of contribution-row sums per solve block (the gather
-  // of each backward level clears the blocks it uses)
-  tcb.ensure((size_t)std::max<int64_t>(inv2_elems / (LSOLVE_BW2 * LSOLVE_BW2), 1) * LSOLVE_BW2 *
-             32 * elem);
+  // contribution rows' share of the pivot rows, laid out like x (32
+  // right-hand sides); each backward sweep's consumers clear what they read
+  const void* tbefore = tacc.p;
+  tacc.ensure((size_t)std::max(n, 1) * 32 * elem);
+  if (tacc.p != tbefore) SG_CUDA(cudaMemset(tacc.p, 0, tacc.bytes));
 }
 
 template <typename T, typename ACC>
@@ -903,22 +905,19 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
   auto level = [&](const Lv& v) {
     const FrontDesc* fr = dfr + v.f0;
     const int64_t* sc = dscr + v.f0;
-    if (v.nsmall > 0) {
-      if (!launch_solve_small<T, ACC>(fwd, arena, fr, v.nsmall, rlist, x, n, nrhs, v.small_maxm,
-                                      unit, s)) {
-        if (fwd) launch_solve_fwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc,
-                                          unit, s);
-        else launch_solve_bwd<T, ACC>(arena, fr, v.nsmall, rlist, x, n, nrhs, scratch, sc, unit,
-                                      s);
-      }
-      if (prof) mark(fwd ? 0 : 1, s);
-    }
     LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),
-                     inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), cnt.as<unsigned>(),
-                     inv2.as<T>(), inv2_off.as<int64_t>() + v.f0, inv2t.as<T>(),
-                     tcb.as<ACC>()};
-    for (const SOp& op : fwd ? v.fwd : v.bwd) {
-      launch_lsolve<T, ACC>(op.kind, tasks.as<LTask>() + op.a, (int)(op.b - op.a), a, s);
+                     inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), inv2.as<T>(),
+                     inv2_off.as<int64_t>() + v.f0, inv2t.as<T>(), tacc.as<ACC>()};
+    const std::vector<SOp>& ops = fwd ? v.fwd : v.bwd;
+    for (size_t k = 0; k < ops.size(); ++k) {
+      const SOp& op = ops[k];
+      if (op.kind == LS_SMALL_TRI) {
+        launch_small_tri<T, ACC>(fwd, arena, fr, v.nsmall, rlist, x, tacc.as<ACC>(), n, nrhs,
+                                 v.small_maxn, unit, s);
+        if (prof) mark(fwd ? 0 : 1, s);
+        continue;
+      }
+      launch_lsolve<T, ACC>(op.kind, tasks.as<LTask>() + op.a, (int)(op.b - op.a), a, op.aux, s);
       if (prof) mark(2 + op.kind, s);
     }
   };
@@ -936,7 +935,7 @@ void SolvePlan::mark(int kind, cudaStream_t s) {
 }
 
 int FKeep::profile_solve(int nrhs, double* ms, long* nl, cudaStream_t s) {
-  for (int k = 0; k < 12; ++k) {
+  for (int k = 0; k < 16; ++k) {
     ms[k] = 0.0;
     nl[k] = 0;
   }
@@ -946,7 +945,7 @@ int FKeep::profile_solve(int nrhs, double* ms, long* nl, cudaStream_t s) {
   xp.ensure(std::max<size_t>((size_t)n * nrhs * es, 1));
   SG_CUDA(cudaMemsetAsync(xp.p, 0, (size_t)n * nrhs * es, s));
   scratch.ensure(std::max<int64_t>(scratch_rows * nrhs, 1) * es);
-  splan.ensure_tt(es, scratch_rows * nrhs);
+  splan.ensure_tt(es, scratch_rows * nrhs, n);
   std::vector<std::pair<int, cudaEvent_t>> ev;
   splan.prof = &ev;
   try {
@@ -972,7 +971,7 @@ int FKeep::profile_solve(int nrhs, double* ms, long* nl, cudaStream_t s) {
     float t = 0.f;
     cudaEventElapsedTime(&t, ev[q - 1].second, ev[q].second);
     const int k = ev[q].first;
-    if (k >= 0 && k < 12) {
+    if (k >= 0 && k < 16) {
       ms[k] += t;
       nl[k] += 1;
     }
@@ -997,7 +996,7 @@ void FKeep::solve_pivot_order(int job, void* xpv, int nrhs, cudaStream_t s) {
   scratch.ensure(std::max<int64_t>(scratch_rows * std::min(nrhs, 32), 1) * sizeof(ACC));
   bool fwd = job == 0 || job == 1;
   bool bwd = job == 0 || job == 3 || job == 4;
-  splan.ensure_tt(sizeof(ACC), scratch_rows * std::min(nrhs, 32));
+  splan.ensure_tt(sizeof(ACC), scratch_rows * std::min(nrhs, 32), n);
   replay(job, nrhs, xpd, s, [&]() {
     for (int r0 = 0; r0 < nrhs; r0 += 32) {
       int nr = std::min(32, nrhs - r0);

@@ -123,17 +123,20 @@ struct Level {
   int f0 = 0, f1 = 0;  // fronts [f0, f1) of the level-ordered front table
 };
 
-// Solve schedule over a level-ordered front table: per level the small
-// fronts (one CTA each) come first, then the large fronts, which run blocked
-// multi-CTA sweeps.
+// Solve schedule over a level-ordered front table.  Per level, the pivot
+// rows of the small fronts (one CTA each, on chip) and of the large fronts
+// (blocked multi-CTA sweeps) are solved; the contribution rows of all fronts
+// of the level are one row-parallel launch per direction (forward after the
+// pivot rows, backward before them).
 struct SolvePlan {
   struct SOp {
     int kind;      // LsKind
     int64_t a, b;  // task range
+    int aux = 0;   // LS_RECT_FWD: widest task's columns, rounded up to 16
   };
   struct Lv {
     int f0 = 0, nsmall = 0, nfront = 0;
-    int small_maxm = 0;  // most rows of the level's small fronts
+    int small_maxn = 0;  // most pivot rows of the level's small fronts
     std::vector<SOp> fwd, bwd;
   };
   std::vector<Lv> lv;
@@ -144,7 +147,7 @@ struct SolvePlan {
   std::vector<LTask> hinv2;       // 256-column diagonal blocks (f = level-ordered index)
   std::vector<int64_t> hinv2_off;
   int64_t inv2_elems = 0;
-  DevMem tasks, tt, cnt, ys, inv, invt, inv_off, inv2, inv2t, invt2, inv2_off, tcb;
+  DevMem tasks, tt, ys, inv, invt, inv_off, inv2, inv2t, invt2, inv2_off, tacc;
   int max_large = 0;
   // Invert every diagonal block of the large fronts (after a factorization).
   template <typename T>
@@ -156,7 +159,7 @@ struct SolvePlan {
                                       const std::vector<Level>& levels);
   void build_tasks(const std::vector<FrontDesc>& hfr, const std::vector<Level>& levels,
                    cudaStream_t s);
-  void ensure_tt(size_t elem, int64_t scratch_elems);
+  void ensure_tt(size_t elem, int64_t scratch_elems, int n);
   template <typename T, typename ACC>
   void run(bool fwd, const T* arena, const FrontDesc* dfr, const int* rlist, ACC* x, int n,
            int nrhs, ACC* scratch, const int64_t* dscr, bool unit, cudaStream_t s);
@@ -265,7 +268,13 @@ struct FKeep {
       }
     cudaGraph_t gr;
     SG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    body();
+    try {
+      body();
+    } catch (...) {
+      // leave the stream out of capture mode before reporting the error
+      if (cudaStreamEndCapture(s, &gr) == cudaSuccess && gr) cudaGraphDestroy(gr);
+      throw;
+    }
     SG_CUDA(cudaStreamEndCapture(s, &gr));
     cudaGraphExec_t ex;
     SG_CUDA(cudaGraphInstantiate(&ex, gr, 0));
