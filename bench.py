@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--ldlt-k", type=int, default=48)
     ap.add_argument("--cpu-sample-k", type=int, default=0,
                     help="grid edge of the CPU baseline sample (0: auto)")
+    ap.add_argument("--cpu-1core-k", type=int, default=40,
+                    help="grid edge of the one-core sequential-BLAS CPU sample (0: skip)")
     return ap.parse_args()
 
 
@@ -305,6 +307,22 @@ def run_ours(args, rank, ws):
         fp64 = {"s_per_step": round(t64, 4), "gflops": round(flops / t64 / 1e9, 1),
                 "ir_iters": it64.value, "bwd_err": be64.value,
                 "fp32_speedup": round(t64 / (t_dev / args.steps), 2)}
+        # roofline of the FP64 path's dominant kernel against the measured
+        # FP64 FMA rate of this GPU (fma chains timed with CUDA events)
+        ms64 = np.zeros(12); cnt64 = np.zeros(12, dtype=np.int64); fl64 = np.zeros(12)
+        lib.sylver_gb300_profile_factor(f3, None, ms64.ctypes.data_as(P), cnt64.ctypes.data_as(P),
+                                        fl64.ctypes.data_as(P))
+        peak64 = ctypes.c_double()
+        lib.sylver_gb300_fp64_fma_rate(ctypes.byref(peak64))
+        d64 = int(np.argmax(ms64))
+        ach64 = fl64[d64] / (ms64[d64] * 1e-3) / 1e12 if ms64[d64] > 0 else 0.0
+        fp64["roofline"] = {
+            "kernel": sg.Factor.KINDS[d64], "bound": "fp64 pipe",
+            "achieved": round(ach64, 4), "peak": round(peak64.value, 4), "unit": "TFLOP/s",
+            "frac": round(ach64 / peak64.value, 3) if peak64.value > 0 else None,
+            "peak_source": "measured: independent fma chains on every SM, CUDA events",
+            "share_of_profiled_factorization": round(float(ms64[d64] / max(ms64.sum(), 1e-9)), 3),
+            "factor_rate_tflops": round(float(fl64.sum() / (ms64.sum() * 1e-3) / 1e12), 4)}
         lib.spldlt_free_fkeep(ctypes.byref(f3))
 
     ldlt = ldlt_leg(args, lib, stream) if (rank == 0 and not args.no_ldlt) else None
@@ -445,10 +463,47 @@ def cpu_baseline(args, gpu_flops):
     x = x + o.solve(prob.rhs - full @ x)
     t = time.perf_counter() - t0
     be = float(w.backward_error(full, x, prob.rhs).max())
-    return {"value": round(an.inform.num_flops / t / 1e9, 2), "unit": "GFLOP/s", "cores": cores,
-            "kind": "port", "seconds": round(t, 3), "bwd_err": be,
-            "sample": f"one factor+solve+1 IR of lognormal27 {k}^3 (n={prob.a.n}, "
-                      f"nrhs={args.nrhs}), FP64, OpenBLAS {cores} threads"}
+    out = {"value": round(an.inform.num_flops / t / 1e9, 2), "unit": "GFLOP/s", "cores": cores,
+           "kind": "port", "seconds": round(t, 3), "bwd_err": be,
+           "sample": f"one factor+solve+1 IR of lognormal27 {k}^3 (n={prob.a.n}, "
+                     f"nrhs={args.nrhs}), FP64, OpenBLAS {cores} threads",
+           "host": host_cpu()}
+    # one core, sequential BLAS, on a smaller grid of the same family (the
+    # full grid would take minutes on one core)
+    if args.cpu_1core_k > 0:
+        oracle.set_threads(1)
+        p1 = workload(args.cpu_1core_k, args.nrhs)
+        an1 = sg.Analysis(p1.a.n, p1.a.ptr, p1.a.row, order=p1.order)
+        full1 = p1.a.to_scipy_full()
+        t0 = time.perf_counter()
+        o1 = oracle.OracleFactor(True, an1.symbolic(), p1.a.val)
+        x1 = o1.solve(p1.rhs)
+        x1 = x1 + o1.solve(p1.rhs - full1 @ x1)
+        t1 = time.perf_counter() - t0
+        oracle.set_threads(cores)
+        out["one_core"] = {
+            "value": round(an1.inform.num_flops / t1 / 1e9, 2), "unit": "GFLOP/s", "cores": 1,
+            "seconds": round(t1, 3), "bwd_err": float(w.backward_error(full1, x1, p1.rhs).max()),
+            "sample": f"one factor+solve+1 IR of lognormal27 {args.cpu_1core_k}^3 "
+                      f"(n={p1.a.n}, nrhs={args.nrhs}), FP64, OpenBLAS 1 thread (sequential)"}
+    return out
+
+
+def host_cpu():
+    """Model, architecture and logical CPU count of the host (lscpu when
+    present, else /proc/cpuinfo)."""
+    import subprocess
+    info = {"logical_cpus": os.cpu_count()}
+    try:
+        txt = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in txt.splitlines():
+            key, _, val = line.partition(":")
+            if key.strip() in ("Architecture", "Model name", "Thread(s) per core",
+                               "Core(s) per socket", "Socket(s)", "CPU max MHz"):
+                info[key.strip()] = val.strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return info
 
 
 def run_reference(args, rank, ws):

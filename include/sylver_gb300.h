@@ -273,6 +273,13 @@ int sylver_gb300_fkeep_diag(void const* fkeep, double* d, int* piv_order);
  * No reference counterpart; for tests. */
 int sylver_gb300_fkeep_fronts(void const* fkeep, int* m, int* n, int* nelim);
 
+/* Bytes of the factor storage (the front arena: every front's L, and D for
+ * LDL^T, in the factor precision); with dst non-null and cap at least that
+ * size the storage is copied there (host memory).  Returns the size, or -1
+ * for a null fkeep.  No reference counterpart; for tests (bitwise
+ * reproducibility of the factors). */
+long sylver_gb300_fkeep_factor_bytes(void const* fkeep, void* dst, long cap);
+
 /* The CUDA stream (cudaStream_t) all library work is issued on; callers that
  * time with CUDA events record them on this stream. */
 void* sylver_gb300_stream(void);
@@ -312,6 +319,12 @@ int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches
  * update on a synthetic rows x k panel and report max|C - C_ref| / max|C_ref|
  * against an FP64 host product.  Returns 0 or a reference flag. */
 int sylver_gb300_tc_selfcheck(int rows, int k, double* max_rel_err);
+
+/* Diagnostic: the device's FP64 fused multiply-add rate in TFLOP/s, from one
+ * timed launch of independent fma chains on every SM (CUDA events, after a
+ * warm-up launch); the denominator of the FP64 path's roofline.  Changes no
+ * device setting.  No reference counterpart. */
+int sylver_gb300_fp64_fma_rate(double* tflops);
 
 /* Counters of the last factorization on fkeep (kernel launches, levels). */
 int sylver_gb300_fkeep_counters(void const* fkeep, long* kernel_launches, int* nlevels,

@@ -127,7 +127,8 @@ EXPORTS = (
     "sylver_gb300_akeep_arrays", "sylver_gb300_fkeep_diag", "sylver_gb300_fkeep_counters",
     "sylver_gb300_fkeep_fronts", "sylver_gb300_akeep_scaling", "sylver_gb300_profile_levels",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
-    "sylver_gb300_tc_selfcheck", "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
+    "sylver_gb300_tc_selfcheck", "sylver_gb300_fp64_fma_rate", "sylver_gb300_fkeep_factor_bytes",
+    "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
     "sylver_gb300_get_schedule", "sylver_gb300_profile_solve", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
     "sylver_gb300_mlp_num_params", "sylver_gb300_mlp_set_params", "sylver_gb300_mlp_get_params",
     "sylver_gb300_mlp_forward", "sylver_gb300_mlp_loss_grad", "sylver_gb300_mlp_train",
@@ -177,6 +178,8 @@ def load(path: str | None = None):
         "sylver_gb300_profile_factor": (I, [P, P, P, P, P]),
         "sylver_gb300_profile_solve": (I, [P, I, P, P]),
         "sylver_gb300_tc_selfcheck": (I, [I, I, ctypes.POINTER(D)]),
+        "sylver_gb300_fp64_fma_rate": (I, [ctypes.POINTER(D)]),
+        "sylver_gb300_fkeep_factor_bytes": (L, [P, P, L]),
         "sylver_gb300_solve_history": (I, [P, P, I]),
         "sylver_gb300_set_schedule": (None, [ctypes.POINTER(Schedule)]),
         "sylver_gb300_get_schedule": (None, [ctypes.POINTER(Schedule)]),

@@ -456,6 +456,20 @@ int sylver_gb300_fkeep_fronts(void const* fkeep, int* m, int* n, int* nelim) {
   return ldlt_export_fronts(*fk, m, n, nelim);
 }
 
+long sylver_gb300_fkeep_factor_bytes(void const* fkeep, void* dst, long cap) {
+  const FKeep* fk = static_cast<const FKeep*>(fkeep);
+  if (!fk) return -1;
+  const long bytes = (long)fk->arena.bytes;
+  if (dst && cap >= bytes && bytes > 0) {
+    Runtime& rt = Runtime::get();
+    if (cudaMemcpyAsync(dst, fk->arena.p, (size_t)bytes, cudaMemcpyDeviceToHost, rt.stream) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(rt.stream) != cudaSuccess)
+      return -1;
+  }
+  return bytes;
+}
+
 void* sylver_gb300_stream(void) {
   Runtime& rt = Runtime::get();
   rt.init();

@@ -187,6 +187,11 @@ void launch_zero_lower(T* arena, const ZeroTask* t, int ntask, cudaStream_t s);
 template <typename T>
 void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
                    int64_t count, bool atomic, cudaStream_t s);
+// Groups g of items [grp[g], grp[g + 1]) that land in one parent column, in
+// child order; one warp per group, no atomics (maps must keep row order).
+template <typename T>
+void launch_extend_add_grouped(T* arena, const ChildDesc* cd, const EaItem* items,
+                               const int* grp, const int* maps, int ngroups, cudaStream_t s);
 // atomic = false: at most one child per parent in this launch (see kernel).
 template <typename T>
 void launch_extend_add(T* arena, const ChildDesc* cd, const EaItem* items, const int* maps,
@@ -256,6 +261,7 @@ constexpr int LSOLVE_BW2 = 256;  // columns per solve step
 constexpr int LSOLVE_UPD_ROWS = 32;  // rows per forward-update CTA
 constexpr int LSOLVE_RED_ROWS = 64;  // rows per backward-reduction CTA
 constexpr int RECT_FWD_T = 128;      // threads of an LS_RECT_FWD task (two contribution rows each)
+constexpr int RECT_FWD_COLS = 128;   // pivot columns per LS_RECT_FWD task (partial sums add atomically)
 constexpr int RECT_BWD_COLS = 128;   // pivot columns per LS_RECT_BWD task
 constexpr int RECT_BWD_T = 128;      // threads of an LS_RECT_BWD task (two columns each, two row halves)
 constexpr int RECT_BWD_ROWS = 256;   // contribution rows per LS_RECT_BWD task

@@ -10,6 +10,8 @@
 //   factorize_diag_block + solve_block + update_block + update_diag_block
 //                                     src/kernels/factor.hxx:56-260,
 //                                     src/factor.hxx:19-148
+#include <type_traits>
+
 #include "device.hpp"
 #include "tile_update.cuh"
 
@@ -51,27 +53,101 @@ __global__ void k_init_a(T* __restrict__ arena, const double* __restrict__ val,
 // Two children of one parent may hit the same parent entry: with `atomic`
 // the launch may hold several children of a parent; without it the caller
 // gives each launch at most one child per parent (children in a fixed order
-// across launches), which makes the sums deterministic.
+// across launches), which makes the sums deterministic.  The column is read
+// in 16-byte pieces: front storage starts on a 64-element boundary with a
+// leading dimension divisible by 4, so the pieces are aligned from the
+// first aligned row on (the rows before it, at most three, are read singly),
+// and a piece never reaches past the column's padded length.
+template <typename T>
+__device__ __forceinline__ void ea_column(T* __restrict__ arena, const ChildDesc& c,
+                                          const int* __restrict__ maps, int j, int lane,
+                                          bool atomic) {
+  constexpr int V = 16 / sizeof(T);
+  using Vec = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+  const int* map = maps + c.map_off;
+  const int pj = map[j];
+  const int64_t s0 = c.cb_off + (int64_t)j * c.ld_c;  // element index of cb(0, j)
+  const T* src = arena + s0;
+  T* dst = arena + c.p_off;
+  auto addr = [&](int pi) {
+    const int r = max(pi, pj), cc = min(pi, pj);
+    return dst + (int64_t)cc * c.ld_p + r;
+  };
+  const int mis = (int)((s0 + j) % V);
+  const int ia = j + (mis ? V - mis : 0);  // first row >= j on a 16-byte boundary
+  if (j + lane < min(ia, c.mc)) {
+    T* d = addr(map[j + lane]);
+    if (atomic) atomic_add(d, src[j + lane]);
+    else *d += src[j + lane];
+  }
+  // EB pieces per lane per round: every load of the round (the column, its
+  // map entries, then the parent entries) is issued before the first store
+  constexpr int EB = 2;
+  for (int i0 = ia + lane * V; i0 < c.mc; i0 += 32 * V * EB) {
+    T e[EB][V];
+    int pi[EB][V];
+#pragma unroll
+    for (int b = 0; b < EB; ++b) {
+      const int i = i0 + b * 32 * V;
+      if (i < c.mc) {
+        const Vec v = *reinterpret_cast<const Vec*>(src + i);
+        if constexpr (V == 4) {
+          e[b][0] = v.x; e[b][1] = v.y; e[b][2] = v.z; e[b][3] = v.w;
+        } else {
+          e[b][0] = v.x; e[b][1] = v.y;
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < V; ++u) pi[b][u] = (i + u < c.mc) ? map[i + u] : -1;
+    }
+    if (atomic) {
+#pragma unroll
+      for (int b = 0; b < EB; ++b)
+#pragma unroll
+        for (int u = 0; u < V; ++u)
+          if (pi[b][u] >= 0) atomic_add(addr(pi[b][u]), e[b][u]);
+    } else {
+      T old[EB][V];
+#pragma unroll
+      for (int b = 0; b < EB; ++b)
+#pragma unroll
+        for (int u = 0; u < V; ++u) old[b][u] = pi[b][u] >= 0 ? *addr(pi[b][u]) : T(0);
+#pragma unroll
+      for (int b = 0; b < EB; ++b)
+#pragma unroll
+        for (int u = 0; u < V; ++u)
+          if (pi[b][u] >= 0) *addr(pi[b][u]) = old[b][u] + e[b][u];
+    }
+  }
+}
+
 template <typename T>
 __global__ void k_extend_add(T* __restrict__ arena, const ChildDesc* __restrict__ cd,
                              const EaItem* __restrict__ items, const int* __restrict__ maps,
                              int nitems, bool atomic) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= nitems) return;
-  EaItem it = items[warp];
-  ChildDesc c = cd[it.child];
-  const int* map = maps + c.map_off;
-  int j = it.col;
-  const int pj = map[j];
-  const T* src = arena + c.cb_off + (int64_t)j * c.ld_c;
-  T* dst = arena + c.p_off;
-  for (int i = j + lane; i < c.mc; i += 32) {
-    const int pi = map[i];
-    const int r = max(pi, pj), cc = min(pi, pj);
-    T* d = dst + (int64_t)cc * c.ld_p + r;
-    if (atomic) atomic_add(d, src[i]);
-    else *d += src[i];
+  const EaItem it = items[warp];
+  ea_column<T>(arena, cd[it.child], maps, it.col, threadIdx.x & 31, atomic);
+}
+
+// One warp per parent column: the CB columns of the front's children that
+// map to it (group g: items [grp[g], grp[g + 1]), in child order) are added
+// one after another, so every parent entry receives its children's sums in a
+// fixed order without atomics.  Needs maps that keep row order (a child
+// column then lands in one parent column).
+template <typename T>
+__global__ void k_extend_add_grouped(T* __restrict__ arena, const ChildDesc* __restrict__ cd,
+                                     const EaItem* __restrict__ items,
+                                     const int* __restrict__ grp, const int* __restrict__ maps,
+                                     int ngroups) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= ngroups) return;
+  const int lane = threadIdx.x & 31;
+  for (int q = grp[warp]; q < grp[warp + 1]; ++q) {
+    const EaItem it = items[q];
+    ea_column<T>(arena, cd[it.child], maps, it.col, lane, false);
+    __syncwarp();  // this column's additions land before the next child's
   }
 }
 
@@ -246,6 +322,14 @@ void launch_extend_add(T* arena, const ChildDesc* cd, const EaItem* items, const
 }
 
 template <typename T>
+void launch_extend_add_grouped(T* arena, const ChildDesc* cd, const EaItem* items,
+                               const int* grp, const int* maps, int ngroups, cudaStream_t s) {
+  if (ngroups <= 0) return;
+  int blocks = (ngroups + 7) / 8;
+  k_extend_add_grouped<T><<<blocks, 256, 0, s>>>(arena, cd, items, grp, maps, ngroups);
+}
+
+template <typename T>
 static size_t panel_smem() {
   constexpr int NB = Tiles<T>::NB, RT = Tiles<T>::RT;
   return sizeof(T) * ((size_t)NB * (NB + 1) + (size_t)NB * (RT + 1));
@@ -298,6 +382,8 @@ void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStr
                                  bool, cudaStream_t);                                       \
   template void launch_extend_add<T>(T*, const ChildDesc*, const EaItem*, const int*, int,   \
                                      cudaStream_t, bool);                                   \
+  template void launch_extend_add_grouped<T>(T*, const ChildDesc*, const EaItem*, const int*, \
+                                             const int*, int, cudaStream_t);                \
   template void launch_small_chol<T>(T*, const SmallTask*, int, int, unsigned*, cudaStream_t); \
   template void launch_diag_chol<T>(T*, const PanelTask*, int, unsigned*, cudaStream_t);     \
   template void launch_panel_trsm<T>(T*, const PanelTask*, int, cudaStream_t);               \

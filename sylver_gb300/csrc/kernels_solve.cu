@@ -1005,7 +1005,7 @@ template <int N> __device__ __forceinline__ void cp_async_wait() {
 // 16-byte aligned (and lies inside the column's padded length).
 constexpr int RF_KU = 8;   // columns of L in flight per thread (forward)
 constexpr int RB_SR = 16;  // rows per pipeline slice (backward)
-template <typename T> constexpr int rb_nst() { return sizeof(T) == 8 ? 3 : 4; }
+template <typename T> constexpr int rb_nst() { return 3; }
 // padded column run of a slice: 16-byte aligned, and lanes RB_LP apart hit
 // distinct banks with 16-byte reads
 template <typename T> constexpr int rb_lp() { return RB_SR + 16 / (int)sizeof(T); }

@@ -267,6 +267,7 @@ void FKeep::plan_cholesky() {
   // per-level launches
   std::vector<ChildDesc> cds;
   std::vector<EaItem> items;
+  std::vector<int> eagrp;  // first item of each extend-add group (grouped levels)
   std::vector<int> maps;
   std::vector<SmallTask> smalls;
   std::vector<PanelTask> panels, diags;
@@ -287,12 +288,23 @@ void FKeep::plan_cholesky() {
   ops.push_back({Op::INIT, 0, ninit, 0});
   op_level.assign(ops.size(), -1);
   for (auto& L : levels) {
-    // extend-add of children into this level's fronts
-    int64_t i0 = (int64_t)items.size();
+    // extend-add of children into this level's fronts, in child order and
+    // without atomics (the factors are bitwise reproducible): one warp per
+    // parent column adds the children's columns that land there one after
+    // another (one launch per level); should a child's row map not keep row
+    // order, one launch per child rank (the r-th child of every front)
+    std::vector<std::vector<EaItem>> by_rank;
+    struct Dest {
+      int p, pc, rank;
+      EaItem it;
+    };
+    std::vector<Dest> dests;
+    bool ordered = true;
     for (int k = L.f0; k < L.f1; ++k) {
       int p = order[k];
       for (int64_t q = st.rptr[p] - 1; q < st.rptr[p + 1] - 1; ++q)
         pos[st.rlist[q] - 1] = (int)(q - (st.rptr[p] - 1));
+      int rank = 0;
       for (int c : st.children[p]) {
         int mc = st.nrow[c] - st.ncol[c];
         if (mc <= 0) continue;
@@ -306,10 +318,33 @@ void FKeep::plan_cholesky() {
         for (int i = 0; i < mc; ++i) maps.push_back(pos[st.rlist[st.rptr[c] - 1 + st.ncol[c] + i] - 1]);
         int ci = (int)cds.size();
         cds.push_back(cd);
-        for (int j = 0; j < mc; ++j) items.push_back({ci, j});
+        if ((int)by_rank.size() <= rank) by_rank.resize(rank + 1);
+        for (int j = 0; j < mc; ++j) {
+          by_rank[rank].push_back({ci, j});
+          dests.push_back({k, maps[cd.map_off + j], rank, {ci, j}});
+          if (j > 0 && maps[cd.map_off + j] <= maps[cd.map_off + j - 1]) ordered = false;
+        }
+        ++rank;
       }
     }
-    if ((int64_t)items.size() > i0) ops.push_back({Op::EA, i0, (int64_t)items.size(), 0});
+    if (ordered && !dests.empty()) {
+      std::stable_sort(dests.begin(), dests.end(), [](const Dest& x, const Dest& y) {
+        return x.p != y.p ? x.p < y.p : (x.pc != y.pc ? x.pc < y.pc : x.rank < y.rank);
+      });
+      const int64_t g0 = (int64_t)eagrp.size();
+      for (size_t q = 0; q < dests.size(); ++q) {
+        if (q == 0 || dests[q].p != dests[q - 1].p || dests[q].pc != dests[q - 1].pc)
+          eagrp.push_back((int)items.size());
+        items.push_back(dests[q].it);
+      }
+      ops.push_back({Op::EAG, g0, (int64_t)eagrp.size(), 0});
+    } else {
+      for (const auto& rk : by_rank) {
+        const int64_t i0 = (int64_t)items.size();
+        items.insert(items.end(), rk.begin(), rk.end());
+        ops.push_back({Op::EA, i0, (int64_t)items.size(), 0});
+      }
+    }
     // small fronts: one CTA each
     int64_t s0 = (int64_t)smalls.size();
     int maxm = 0;
@@ -521,6 +556,8 @@ void FKeep::plan_cholesky() {
   cdesc.upload(cds, s);
   eaitems.upload(items, s);
   eamaps.upload(maps, s);
+  eagrp.push_back((int)items.size());  // end of the last group
+  eagroups.upload(eagrp, s);
   small.upload(smalls, s);
   panel.upload(panels, s);
   diagt.upload(diags, s);
@@ -597,7 +634,11 @@ void FKeep::run_ops(cudaStream_t s) {
         break;
       case Op::EA:
         launch_extend_add<T>(A, cdesc.as<ChildDesc>(), eaitems.as<EaItem>() + op.a,
-                             eamaps.as<int>(), (int)cnt, s);
+                             eamaps.as<int>(), (int)cnt, s, false);
+        break;
+      case Op::EAG:
+        launch_extend_add_grouped<T>(A, cdesc.as<ChildDesc>(), eaitems.as<EaItem>(),
+                                     eagroups.as<int>() + op.a, eamaps.as<int>(), (int)cnt, s);
         break;
       case Op::SMALL:
         launch_small_chol<T>(A, small.as<SmallTask>() + op.a, (int)cnt, op.aux, stp, s);
@@ -728,7 +769,7 @@ int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, c
   for (size_t q = 0; q < all.size(); ++q) {
     float t = 0.f;
     cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
-    int k = (int)all[q].kind;
+    int k = all[q].kind == Op::EAG ? (int)Op::EA : (int)all[q].kind;  // both extend-add
     ms[k] += t;
     nl[k] += 1;
     flops[k] += op_flops.empty() ? 0.0 : op_flops[q];
@@ -781,7 +822,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
     // kernels skip the first tile's rows below n)
     auto rect = [&](std::vector<SOp>& ops, bool fwd) {
       int64_t a = (int64_t)htasks.size();
-      const int cw = fwd ? LSOLVE_BW2 : RECT_BWD_COLS;
+      const int cw = fwd ? RECT_FWD_COLS : RECT_BWD_COLS;
       const int rh = fwd ? 2 * RECT_FWD_T : RECT_BWD_ROWS;
       int wmax = 0;
       for (int f = 0; f < v.nfront; ++f) {

@@ -114,7 +114,7 @@ struct AKeep {
 
 // One kernel launch of the factor schedule.
 struct Op {
-  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV, SPLIT, TCUPD, BDIAG, BPANEL } kind;
+  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV, SPLIT, TCUPD, BDIAG, BPANEL, EAG } kind;
   int64_t a = 0, b = 0;  // task range [a, b)
   int aux = 0;           // SMALL: max front rows; SPLIT/TCUPD: tensor-core level
 };
@@ -226,7 +226,7 @@ struct FKeep {
 
   // device data
   DevMem arena, val, cval, faval, frow, fcol, fidx, srcptr, src, status, anorm;
-  DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, small, panel, upd, diagt, zerot;
+  DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, eagroups, small, panel, upd, diagt, zerot;
   int nzero = 0;
   DevMem dfr, dscr, rlist0, perm0;
   DevMem xp, scratch, bcopy, resid, norms;

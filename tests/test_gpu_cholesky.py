@@ -242,3 +242,28 @@ def test_solve_rhs_counts_match_oracle(sylver, orc, gpu, nrhs):
     x32 = f32.solve(rhs)
     assert w.backward_error(p.a.to_scipy_full(), x32, rhs).max() <= 1e-14
 
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_factors_bitwise_reproducible(sylver, gpu, precision):
+    """The extend-add sums each parent entry's children in child order (one
+    launch per child rank, no atomics), so factorizing the same values twice
+    into the same factor storage gives the same bits, FP64 and FP32 (the
+    tensor-core updates included)."""
+    import ctypes
+    p = w.lognormal27(20, nrhs=1)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    f = sylver.Factor(an, True, p.a.val, precision=precision)
+    assert f.flag == 0
+    lib = sylver.load()
+    nb = lib.sylver_gb300_fkeep_factor_bytes(f.fkeep, None, 0)
+    assert nb > 0
+    first = np.empty(nb, np.uint8)
+    assert lib.sylver_gb300_fkeep_factor_bytes(f.fkeep, first.ctypes.data_as(ctypes.c_void_p),
+                                               nb) == nb
+    for _ in range(2):
+        assert f.refactor(p.a.val, precision=precision) == 0
+        again = np.empty(nb, np.uint8)
+        assert lib.sylver_gb300_fkeep_factor_bytes(
+            f.fkeep, again.ctypes.data_as(ctypes.c_void_p), nb) == nb
+        assert np.array_equal(first, again)
