@@ -273,11 +273,13 @@ int sylver_gb300_fkeep_diag(void const* fkeep, double* d, int* piv_order);
  * No reference counterpart; for tests. */
 int sylver_gb300_fkeep_fronts(void const* fkeep, int* m, int* n, int* nelim);
 
-/* Bytes of the factor storage (the front arena: every front's L, and D for
- * LDL^T, in the factor precision); with dst non-null and cap at least that
- * size the storage is copied there (host memory).  Returns the size, or -1
- * for a null fkeep.  No reference counterpart; for tests (bitwise
- * reproducibility of the factors). */
+/* Bytes of the factor storage in the factor precision: the front arena
+ * (every front's block), or for an LDL^T factorization whose front blocks
+ * would not fit in device memory the compact store of the fronts' factor
+ * columns; with dst non-null and cap at least that size the storage is
+ * copied there (host memory).  Returns the size, or -1 for a null fkeep.
+ * No reference counterpart; for tests (bitwise reproducibility of the
+ * factors). */
 long sylver_gb300_fkeep_factor_bytes(void const* fkeep, void* dst, long cap);
 
 /* The CUDA stream (cudaStream_t) all library work is issued on; callers that
@@ -370,6 +372,13 @@ typedef struct {
                             (default 4).  Within a group each panel but the last updates only
                             the group's remaining columns; the columns past the group get one
                             tensor-core update with K = group x panel width */
+  int front_memory;      /* front storage economy: 0 when needed (all front blocks would take
+                            more than half of the device memory), 1 always, negative never.
+                            Cholesky: contribution blocks given back to later fronts once the
+                            parent's level has assembled them (each level zeroed just before it);
+                            LDL^T: each level's factor columns copied to a compact store and
+                            whole blocks given back (LDL^T always gives contribution blocks
+                            back) */
 } sylver_gb300_schedule_t;
 
 /* Set the schedule used by factorizations planned afterwards (a new fkeep);

@@ -90,7 +90,8 @@ class Schedule(ctypes.Structure):
     """sylver_gb300_schedule_t: kernel-path choices (0 = default)."""
     _fields_ = [("small_front_rows", ctypes.c_int), ("tc_min_cb_rows", ctypes.c_int),
                 ("solve_large_cols", ctypes.c_int), ("ldlt_tpp_cols", ctypes.c_int),
-                ("fs_panel_cols", ctypes.c_int), ("fs_panel_group", ctypes.c_int)]
+                ("fs_panel_cols", ctypes.c_int), ("fs_panel_group", ctypes.c_int),
+                ("front_memory", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

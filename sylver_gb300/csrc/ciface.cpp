@@ -459,10 +459,10 @@ int sylver_gb300_fkeep_fronts(void const* fkeep, int* m, int* n, int* nelim) {
 long sylver_gb300_fkeep_factor_bytes(void const* fkeep, void* dst, long cap) {
   const FKeep* fk = static_cast<const FKeep*>(fkeep);
   if (!fk) return -1;
-  const long bytes = (long)fk->arena.bytes;
+  const long bytes = (long)fk->factor_bytes();
   if (dst && cap >= bytes && bytes > 0) {
     Runtime& rt = Runtime::get();
-    if (cudaMemcpyAsync(dst, fk->arena.p, (size_t)bytes, cudaMemcpyDeviceToHost, rt.stream) !=
+    if (cudaMemcpyAsync(dst, fk->factor_base(), (size_t)bytes, cudaMemcpyDeviceToHost, rt.stream) !=
             cudaSuccess ||
         cudaStreamSynchronize(rt.stream) != cudaSuccess)
       return -1;
@@ -675,6 +675,7 @@ void sylver_gb300_set_schedule(sylver_gb300_schedule_t const* s) {
   c.ldlt_tpp_cols = s->ldlt_tpp_cols;
   c.fs_panel_cols = s->fs_panel_cols;
   c.fs_panel_group = s->fs_panel_group;
+  c.front_memory = s->front_memory;
 }
 
 void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
@@ -686,6 +687,7 @@ void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
   s->ldlt_tpp_cols = c.ldlt_tpp_cols;
   s->fs_panel_cols = c.fs_panel_cols;
   s->fs_panel_group = c.fs_panel_group;
+  s->front_memory = c.front_memory;
 }
 
 }  // extern "C"

@@ -184,6 +184,19 @@ template <typename T>
 void prepare_factor_kernels();
 template <typename T>
 void launch_zero_lower(T* arena, const ZeroTask* t, int ntask, cudaStream_t s);
+// arena[off, off + len) <- 0 for each span (off, len multiples of 64 elements)
+struct ZeroSpan {
+  int64_t off, len;
+};
+template <typename T>
+void launch_zero_spans(T* arena, const ZeroSpan* t, int ntask, cudaStream_t s);
+// dst[d, d + len) <- src[o, o + len) for each span (multiples of 4 elements,
+// 16-byte aligned)
+struct CopySpan {
+  int64_t src, dst, len;
+};
+template <typename T>
+void launch_copy_spans(T* dst, const T* src, const CopySpan* t, int ntask, cudaStream_t s);
 template <typename T>
 void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
                    int64_t count, bool atomic, cudaStream_t s);

@@ -35,6 +35,29 @@ __global__ void __launch_bounds__(256) k_zero_lower(T* __restrict__ arena,
   }
 }
 
+// Whole spans of the arena <- 0 (front blocks placed where contribution
+// blocks were given back), 16-byte stores; one CTA per span.
+template <typename T>
+__global__ void __launch_bounds__(256) k_zero_spans(T* __restrict__ arena,
+                                                    const ZeroSpan* __restrict__ spans) {
+  const ZeroSpan z = spans[blockIdx.x];
+  float4* p = reinterpret_cast<float4*>(arena + z.off);
+  const int64_t n4 = z.len * (int64_t)sizeof(T) / 16;
+  for (int64_t i = threadIdx.x; i < n4; i += 256) p[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// Copies of whole spans (a front's factor columns into the compact factor
+// store), 16-byte loads and stores; one CTA per span.
+template <typename T>
+__global__ void __launch_bounds__(256) k_copy_spans(T* __restrict__ dst, const T* __restrict__ src,
+                                                    const CopySpan* __restrict__ spans) {
+  const CopySpan c = spans[blockIdx.x];
+  const float4* s4 = reinterpret_cast<const float4*>(src + c.src);
+  float4* d4 = reinterpret_cast<float4*>(dst + c.dst);
+  const int64_t n4 = c.len * (int64_t)sizeof(T) / 16;
+  for (int64_t i = threadIdx.x; i < n4; i += 256) d4[i] = s4[i];
+}
+
 // arena[dst[k]] (+)= val[src[k]]  -- assembly of original entries.
 template <typename T>
 __global__ void k_init_a(T* __restrict__ arena, const double* __restrict__ val,
@@ -306,6 +329,18 @@ void launch_zero_lower(T* arena, const ZeroTask* t, int ntask, cudaStream_t s) {
 }
 
 template <typename T>
+void launch_zero_spans(T* arena, const ZeroSpan* t, int ntask, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_zero_spans<T><<<ntask, 256, 0, s>>>(arena, t);
+}
+
+template <typename T>
+void launch_copy_spans(T* dst, const T* src, const CopySpan* t, int ntask, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_copy_spans<T><<<ntask, 256, 0, s>>>(dst, src, t);
+}
+
+template <typename T>
 void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_t* dst,
                    int64_t count, bool atomic, cudaStream_t s) {
   if (count <= 0) return;
@@ -378,6 +413,8 @@ void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStr
 #define SG_INST(T)                                                                          \
   template void prepare_factor_kernels<T>();                                                 \
   template void launch_zero_lower<T>(T*, const ZeroTask*, int, cudaStream_t);                \
+  template void launch_zero_spans<T>(T*, const ZeroSpan*, int, cudaStream_t);                \
+  template void launch_copy_spans<T>(T*, const T*, const CopySpan*, int, cudaStream_t);       \
   template void launch_init_a<T>(T*, const double*, const int64_t*, const int64_t*, int64_t, \
                                  bool, cudaStream_t);                                       \
   template void launch_extend_add<T>(T*, const ChildDesc*, const EaItem*, const int*, int,   \

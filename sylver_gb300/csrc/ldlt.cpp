@@ -30,6 +30,7 @@
 #include <numeric>
 #include <type_traits>
 
+#include "arena_alloc.hpp"
 #include "ldlt_dev.hpp"
 #include "tc.hpp"
 
@@ -40,11 +41,24 @@ struct LdltState {
   std::vector<int> m, n, nelim, ld, var_off;
   std::vector<int64_t> off, d_off;
   std::vector<std::vector<int>> var;  // host copy after factorization
-  int64_t arena_used = 0, var_used = 0, d_used = 0;
+  int64_t var_used = 0, d_used = 0;
+  // front blocks in the arena: contribution blocks are given back once the
+  // parent's level has assembled them (`pending`: the fronts whose blocks
+  // the last level read)
+  ArenaAlloc alloc;
+  std::vector<int> pending;
+  // arena high-water marks from the symbolic sizes: contribution blocks
+  // given back (in place) or whole blocks given back with the factor
+  // columns copied out; elements of factor columns (symbolic)
+  int64_t hw_inplace = 0, hw_copyout = 0, fsym = 0;
+  bool copyout = false;
+  std::vector<int64_t> foff;  // copy-out: offset of each front's factor columns
+  int64_t fused = 0;
+  DevMem cspans;
   DevMem dvar, dall, blk, bdinv, lperm, state, mvvar;
   DevMem fr, fr2, cmap, cmap2, up, sc, sc2;  // per-level descriptors + scratch
   DevMem tcsplit, tctask, tcplanes;          // FP32 contribution blocks on the tensor cores
-  DevMem ea_cd, ea_items, ea_maps, am_src, am_dst;
+  DevMem ea_cd, ea_items, ea_maps, am_src, am_dst, zspans;
   // solve
   DevMem sfr, sscr, sdoff;
   std::vector<FrontDesc> hsfr;
@@ -103,10 +117,35 @@ void plan_ldlt(FKeep& fk) {
   for (int i = 0; i < st.n; ++i) p0[i] = st.perm[i];
   fk.perm0.upload(p0, Runtime::get().stream);
   fk.num_flops = st.num_flops;
-  // arena: symbolic size plus headroom for delays; grows when a level needs
-  int64_t sym = 0;
-  for (int s = 0; s < ns; ++s) sym += round_up64((int64_t)round_up(st.nrow[s], 4) * st.nrow[s], 64);
-  fk.arena_elems = sym + sym / 8 + 1024;
+  // arena: the high-water mark of the front blocks with contribution blocks
+  // given back after the parent's level (symbolic sizes, no delays), plus
+  // headroom for delays; it grows when a level needs more.  The same with
+  // whole blocks given back (factor columns copied out) for fronts that
+  // would not fit that way.
+  LdltState& L = *fk.ldlt;
+  for (int whole = 0; whole < 2; ++whole) {
+    ArenaAlloc sim;
+    std::vector<int64_t> soff(ns, 0);
+    std::vector<int> pend;
+    for (const Level& lev : fk.levels) {
+      for (int c : pend) {
+        const int64_t ldc = round_up(std::max(st.nrow[c], 1), 4);
+        int64_t a = soff[c], b = soff[c] + ArenaAlloc::round64(ldc * st.nrow[c]);
+        if (!whole) cb_span(soff[c], ldc, st.nrow[c], st.ncol[c], &a, &b);
+        sim.release(a, b);
+      }
+      pend.clear();
+      for (int k = lev.f0; k < lev.f1; ++k) {
+        const int s = fk.order[k];
+        const int64_t lds = round_up(std::max(st.nrow[s], 1), 4);
+        soff[s] = sim.alloc(lds * st.nrow[s]);
+        for (int c : st.children[s]) pend.push_back(c);
+        if (whole) L.fsym += ArenaAlloc::round64(lds * st.ncol[s]);
+      }
+    }
+    (whole ? L.hw_copyout : L.hw_inplace) = sim.high_water();
+  }
+  fk.arena_elems = L.hw_inplace + L.hw_inplace / 8 + 1024;
 }
 
 namespace {
@@ -136,7 +175,35 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   L.off.assign(ns, 0);
   L.d_off.assign(ns, 0);
   L.var.assign(ns, {});
-  L.arena_used = L.var_used = L.d_used = 0;
+  L.var_used = L.d_used = 0;
+  L.alloc.reset();
+  L.pending.clear();
+  // fronts kept in place unless their blocks would take more than half of
+  // the device memory that way; then the factor columns are copied out to a
+  // compact store after each level and whole blocks are given back
+  {
+    size_t freeb = 0, totb = 0;
+    SG_CUDA(cudaMemGetInfo(&freeb, &totb));
+    const double avail = (double)freeb + (double)fk.arena.bytes + (double)fk.fstore.bytes;
+    const int fsch = Schedule::current().front_memory;
+    L.copyout = fsch > 0 ||
+                (fsch == 0 && (double)(L.hw_inplace + L.hw_inplace / 8) * sizeof(T) > 0.5 * avail);
+    fk.fcopy = L.copyout;
+    if (L.copyout) {
+      fk.arena_elems = L.hw_copyout + L.hw_copyout / 8 + 1024;
+      const int64_t fe = L.fsym + L.fsym / 4 + 1024;
+      if (fk.fstore.bytes < (size_t)fe * sizeof(T)) {
+        fk.fstore.release();
+        fk.fstore.ensure((size_t)fe * sizeof(T));
+      }
+      L.foff.assign(ns, 0);
+      L.fused = 0;
+    } else {
+      fk.fstore.release();
+      fk.arena_elems = std::max(fk.arena_elems, L.hw_inplace + L.hw_inplace / 8 + 1024);
+    }
+  }
+  if (L.copyout && fk.arena.bytes > (size_t)fk.arena_elems * sizeof(T) * 2) fk.arena.release();
   fk.arena.ensure((size_t)fk.arena_elems * sizeof(T));
   unsigned* status = fk.status.as<unsigned>();
   SG_CUDA(cudaMemsetAsync(status, 0, sizeof(unsigned), s));
@@ -150,8 +217,16 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   for (const Level& lev : fk.levels) {
     std::vector<int> F(fk.order.begin() + lev.f0, fk.order.begin() + lev.f1);
     const int nslot = (int)F.size();
-    // ---- sizes, variable lists, storage
-    int64_t lvl_off0 = L.arena_used;
+    // ---- sizes, variable lists, storage: the contribution blocks the last
+    // level assembled are given back first (that level has completed: its
+    // host synchronisation), then this level's fronts are placed
+    for (int c : L.pending) {
+      int64_t a = L.off[c], b = L.off[c] + round_up64((int64_t)L.ld[c] * L.m[c], 64);
+      if (!L.copyout) cb_span(L.off[c], L.ld[c], L.m[c], L.nelim[c], &a, &b);
+      L.alloc.release(a, b);
+    }
+    L.pending.clear();
+    std::vector<ZeroSpan> zsp;
     std::vector<int> hvar_lvl;
     for (int s2 : F) {
       int sncol = st.ncol[s2], snrow = st.nrow[s2];
@@ -160,8 +235,11 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
       L.n[s2] = sncol + ndin;
       L.m[s2] = snrow + ndin;
       L.ld[s2] = round_up(std::max(L.m[s2], 1), 4);
-      L.off[s2] = L.arena_used;
-      L.arena_used += round_up64((int64_t)L.ld[s2] * L.m[s2], 64);
+      const int64_t blk = round_up64((int64_t)L.ld[s2] * L.m[s2], 64);
+      L.off[s2] = L.alloc.alloc(blk);
+      for (int64_t z = 0; z < blk; z += (int64_t)1 << 20)
+        zsp.push_back({L.off[s2] + z, std::min<int64_t>((int64_t)1 << 20, blk - z)});
+      for (int c : st.children[s2]) L.pending.push_back(c);
       L.d_off[s2] = L.d_used;
       L.d_used += 2 * (int64_t)std::max(L.n[s2], 1);
       L.var_off[s2] = (int)L.var_used;
@@ -176,8 +254,8 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
       hvar_lvl.insert(hvar_lvl.end(), v.begin(), v.end());
       fk.maxfront = std::max(fk.maxfront, L.m[s2]);
     }
-    if (L.arena_used > fk.arena_elems) {
-      int64_t ne = std::max(L.arena_used, fk.arena_elems + fk.arena_elems / 4);
+    if (L.alloc.top() > fk.arena_elems) {
+      int64_t ne = std::max(L.alloc.top(), fk.arena_elems + fk.arena_elems / 4);
       grow(fk.arena, (size_t)ne * sizeof(T), s);
       fk.arena_elems = ne;
     }
@@ -188,7 +266,8 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
     if (!hvar_lvl.empty())
       SG_CUDA(cudaMemcpyAsync(dvar + L.var_off[F[0]], hvar_lvl.data(),
                               hvar_lvl.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    SG_CUDA(cudaMemsetAsync(A + lvl_off0, 0, (size_t)(L.arena_used - lvl_off0) * sizeof(T), s));
+    put(L.zspans, zsp, s);
+    launch_zero_spans<T>(A, L.zspans.as<ZeroSpan>(), (int)zsp.size(), s);
     SG_CUDA(cudaMemsetAsync(L.dall.as<double>() + L.d_off[F[0]], 0,
                             (size_t)(L.d_used - L.d_off[F[0]]) * sizeof(double), s));
     // ---- original entries (rows below the own columns shift by ndelay_in)
@@ -410,6 +489,23 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
       }
       fk.num_delay += nn - t2;
     }
+    // ---- copy-out: the level's factor columns to the compact store (the
+    // blocks are given back whole once the parents have assembled them)
+    if (L.copyout) {
+      std::vector<CopySpan> cs;
+      for (int s2 : F) {
+        const int64_t len = (int64_t)L.ld[s2] * L.nelim[s2];
+        L.foff[s2] = L.fused;
+        L.fused += round_up64(len, 64);
+        for (int64_t z = 0; z < len; z += (int64_t)1 << 20)
+          cs.push_back({L.off[s2] + z, L.foff[s2] + z, std::min<int64_t>((int64_t)1 << 20, len - z)});
+      }
+      if ((size_t)L.fused * sizeof(T) > fk.fstore.bytes)
+        grow(fk.fstore, (size_t)L.fused * sizeof(T), s);
+      put(L.cspans, cs, s);
+      launch_copy_spans<T>(fk.fstore.as<T>(), fk.arena.as<T>(), L.cspans.as<CopySpan>(),
+                           (int)cs.size(), s);
+    }
     // ---- contribution blocks: CB -= (L D) L^T over all eliminated columns
     // (form_contrib).  FP32 fronts with enough contribution rows run it on the
     // tensor cores: L and L*D of the contribution rows are split into 3xBF16
@@ -544,7 +640,8 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   std::vector<FrontDesc> tmp(ns);
   for (int k = 0; k < ns; ++k) {
     int s2 = fk.order[k];
-    tmp[k] = FrontDesc{L.off[s2], L.ld[s2], L.m[s2], L.nelim[s2], L.var_off[s2], 0};
+    tmp[k] = FrontDesc{L.copyout ? L.foff[s2] : L.off[s2], L.ld[s2], L.m[s2], L.nelim[s2],
+                       L.var_off[s2], 0};
   }
   std::vector<int> pm = SolvePlan::small_first(tmp, fk.levels);
   for (int k = 0; k < ns; ++k) {
@@ -565,7 +662,8 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   put(L.sscr, L.hsscr, s);
   put(L.sdoff, L.hsdoff, s);
   fk.splan.build_tasks(L.hsfr, fk.levels, s);
-  fk.splan.compute_inverses<T>(fk.arena.as<T>(), L.sfr.as<FrontDesc>(), true, s);
+  fk.splan.compute_inverses<T>(static_cast<const T*>(fk.factor_base()), L.sfr.as<FrontDesc>(),
+                              true, s);
   SG_CUDA(cudaStreamSynchronize(s));
   return fk.flag;
 }
@@ -616,7 +714,7 @@ static void ldlt_solve_t(FKeep& fk, int job, ACC* xp, int nrhs, cudaStream_t s) 
   const int64_t* dof = L.sdoff.as<int64_t>();
   const int* var = L.dvar.as<int>();
   using T = ACC;  // factors and accumulation share the factor precision
-  const T* A = fk.arena.as<T>();
+  const T* A = static_cast<const T*>(fk.factor_base());
   fk.splan.ensure_tt(sizeof(ACC), L.scratch_rows * std::min(nrhs, 32), n);
   fk.replay(job, nrhs, xp, s, [&]() {
     for (int r0 = 0; r0 < nrhs; r0 += 32) {

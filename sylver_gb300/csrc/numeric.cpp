@@ -7,6 +7,7 @@
 // covers all fronts of a level, so independent subtrees share kernels and the
 // whole posdef factorization is one captured CUDA graph.
 #include "numeric.hpp"
+#include "arena_alloc.hpp"
 #include "ldlt.hpp"
 #include "../../include/sylver_gb300.h"
 
@@ -193,51 +194,86 @@ void FKeep::plan_cholesky() {
       levels[l].f1 = cnt[l + 1];
     }
   }
+  // front blocks: one after another when they all fit in half of the device
+  // memory (zeroed and initialised by one launch each at the start);
+  // otherwise placed level by level with the contribution blocks a level
+  // assembled given back before the next level is placed (the schedule runs
+  // the levels in order on one stream, so each level's zeroing, just before
+  // it, comes after that assembly)
   off.assign(ns, 0);
   ld.assign(ns, 0);
-  int64_t cur = 0;
-  for (int k = 0; k < ns; ++k) {
-    int s = order[k];
-    int m = st.nrow[s];
-    ld[s] = round_up(std::max(m, 1), 4);
-    off[s] = cur;
-    cur += round_up64((int64_t)ld[s] * m, 64);
+  int64_t blocks = 0;
+  for (int s = 0; s < ns; ++s)
+    blocks += ArenaAlloc::round64((int64_t)round_up(std::max(st.nrow[s], 1), 4) * st.nrow[s]);
+  size_t freeb = 0, totb = 0;
+  SG_CUDA(cudaMemGetInfo(&freeb, &totb));
+  const int fmem = sched.front_memory;
+  reuse_blocks = fmem > 0 || (fmem == 0 && (double)blocks * (f32 ? sizeof(float) : sizeof(double)) >
+                                               0.5 * (double)totb);
+  {
+    ArenaAlloc al;
+    std::vector<int> pend;
+    for (const Level& L : levels) {
+      for (int c : pend) {
+        int64_t a, b;
+        cb_span(off[c], ld[c], st.nrow[c], st.ncol[c], &a, &b);
+        al.release(a, b);
+      }
+      pend.clear();
+      for (int k = L.f0; k < L.f1; ++k) {
+        const int s = order[k], m = st.nrow[s];
+        ld[s] = round_up(std::max(m, 1), 4);
+        off[s] = al.alloc((int64_t)ld[s] * m);
+        if (reuse_blocks)
+          for (int c : st.children[s]) pend.push_back(c);
+      }
+    }
+    arena_elems = std::max<int64_t>(al.high_water(), 1);
   }
-  arena_elems = std::max<int64_t>(cur, 1);
   // zeroing tasks: each front's lower triangle in column ranges of about 64K
-  // entries
+  // entries, level by level (zlv[l] = first task of level l)
   std::vector<ZeroTask> zt;
-  for (int k = 0; k < ns; ++k) {
-    const int s = order[k], m = st.nrow[s];
-    int j0 = 0;
-    while (j0 < m) {
-      int64_t acc = 0;
-      int j1 = j0;
-      while (j1 < m && acc < 65536) acc += m - j1++;
-      zt.push_back({off[s], ld[s], m, j0, j1});
-      j0 = j1;
+  std::vector<int64_t> zlv(levels.size() + 1, 0), ilv(levels.size() + 1, 0);
+  for (size_t l = 0; l < levels.size(); ++l) {
+    zlv[l] = (int64_t)zt.size();
+    for (int k = levels[l].f0; k < levels[l].f1; ++k) {
+      const int s = order[k], m = st.nrow[s];
+      int j0 = 0;
+      while (j0 < m) {
+        int64_t acc = 0;
+        int j1 = j0;
+        while (j1 < m && acc < 65536) acc += m - j1++;
+        zt.push_back({off[s], ld[s], m, j0, j1});
+        j0 = j1;
+      }
     }
   }
+  zlv[levels.size()] = (int64_t)zt.size();
   nzero = (int)zt.size();
 
-  // A -> arena map
+  // A -> arena map, level by level (ilv[l] = first entry of level l)
   std::vector<int64_t> asrc, adst;
   asrc.reserve(st.nlist.size() / 2);
   adst.reserve(st.nlist.size() / 2);
   init_atomic = false;
-  for (int s = 0; s < ns; ++s) {
-    int nrow = st.nrow[s];
-    int64_t prev = -1;
-    for (int64_t k = st.nptr[s] - 1; k < st.nptr[s + 1] - 1; ++k) {
-      int64_t src = st.nlist[2 * k] - 1, dest = st.nlist[2 * k + 1] - 1;
-      int64_t c = dest / nrow, r = dest % nrow;
-      asrc.push_back(src);
-      adst.push_back(off[s] + c * ld[s] + r);
-      if (dest == prev) init_atomic = true;
-      prev = dest;
+  for (size_t l = 0; l < levels.size(); ++l) {
+    ilv[l] = (int64_t)asrc.size();
+    for (int kk = levels[l].f0; kk < levels[l].f1; ++kk) {
+      const int s = order[kk];
+      int nrow = st.nrow[s];
+      int64_t prev = -1;
+      for (int64_t k = st.nptr[s] - 1; k < st.nptr[s + 1] - 1; ++k) {
+        int64_t src = st.nlist[2 * k] - 1, dest = st.nlist[2 * k + 1] - 1;
+        int64_t c = dest / nrow, r = dest % nrow;
+        asrc.push_back(src);
+        adst.push_back(off[s] + c * ld[s] + r);
+        if (dest == prev) init_atomic = true;
+        prev = dest;
+      }
     }
   }
   ninit = (int64_t)asrc.size();
+  ilv[levels.size()] = ninit;
 
   // rlist (0-based) and solve descriptors in level order, small fronts first
   std::vector<int> rl0(st.rlist.size());
@@ -284,10 +320,15 @@ void FKeep::plan_cholesky() {
   std::vector<int> pos(st.n, -1);
   ops.clear();
   op_level.clear();
-  ops.push_back({Op::MEMSET, 0, 0, 0});
-  ops.push_back({Op::INIT, 0, ninit, 0});
-  op_level.assign(ops.size(), -1);
   for (auto& L : levels) {
+    // the level's front blocks <- 0, then the original entries (every
+    // level's at once before the first when no block is reused)
+    const size_t l = &L - levels.data();
+    const size_t l1 = reuse_blocks ? l + 1 : levels.size();
+    if (reuse_blocks || l == 0) {
+      if (zlv[l1] > zlv[l]) ops.push_back({Op::MEMSET, zlv[l], zlv[l1], 0});
+      if (ilv[l1] > ilv[l]) ops.push_back({Op::INIT, ilv[l], ilv[l1], 0});
+    }
     // extend-add of children into this level's fronts, in child order and
     // without atomics (the factors are bitwise reproducible): one warp per
     // parent column adds the children's columns that land there one after
@@ -589,7 +630,9 @@ void FKeep::upload_static(cudaStream_t s) {
   faval.ensure(std::max<size_t>(1, a.fcol.size()) * sizeof(double));
   status.ensure(sizeof(unsigned));
   anorm.ensure(sizeof(double));
-  arena.ensure((size_t)arena_elems * (precision == 1 ? sizeof(float) : sizeof(double)));
+  // (LDL^T sizes its arena at factor time, when it knows whether the
+  // factor columns go to the compact store)
+  if (!ldlt) arena.ensure((size_t)arena_elems * (precision == 1 ? sizeof(float) : sizeof(double)));
   if (posdef) {
     // the inverses are formed inside the captured factor graph: allocate now
     const size_t es = precision == 1 ? sizeof(float) : sizeof(double);
@@ -626,11 +669,11 @@ void FKeep::run_ops(cudaStream_t s) {
     int64_t cnt = op.b - op.a;
     switch (op.kind) {
       case Op::MEMSET:
-        launch_zero_lower<T>(A, zerot.as<ZeroTask>(), nzero, s);
+        launch_zero_lower<T>(A, zerot.as<ZeroTask>() + op.a, (int)cnt, s);
         break;
       case Op::INIT:
-        launch_init_a<T>(A, val.as<double>(), amap_src.as<int64_t>(), amap_dst.as<int64_t>(),
-                         ninit, init_atomic, s);
+        launch_init_a<T>(A, val.as<double>(), amap_src.as<int64_t>() + op.a,
+                         amap_dst.as<int64_t>() + op.a, cnt, init_atomic, s);
         break;
       case Op::EA:
         launch_extend_add<T>(A, cdesc.as<ChildDesc>(), eaitems.as<EaItem>() + op.a,

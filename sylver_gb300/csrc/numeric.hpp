@@ -58,6 +58,7 @@ struct Schedule {
   int fs_panel_cols = 0;     // FP32 Cholesky: outer panel width of the blocked large-front
                              // path (multiple of 64, <= 256; <0: 64-column SIMT steps)
   int fs_panel_group = 0;    // FP32 Cholesky: outer panels per trailing fully-summed update
+  int front_memory = 0;      // front storage economy: 1 always, < 0 never, 0 when needed
   static Schedule& current();
   // default 96 rows: measured faster than the FP32 cap of 128 on 40^3, 56^3 and
   // 80^3 log-normal 27-point matrices (schedule sweeps of the learned scheduler)
@@ -223,9 +224,19 @@ struct FKeep {
   std::vector<int> op_level;         // level of each op (-1: whole-factor set-up / inverses)
   bool init_atomic = false;
   int64_t ninit = 0;
+  // Cholesky: front blocks placed with contribution blocks given back (when
+  // all blocks would take more than half of the device memory)
+  bool reuse_blocks = false;
 
   // device data
   DevMem arena, val, cval, faval, frow, fcol, fidx, srcptr, src, status, anorm;
+  // LDL^T with the factor columns copied out of the front blocks (set when
+  // the fronts' blocks would not fit with only their contribution blocks
+  // given back): the solves read the compact store instead of the arena
+  DevMem fstore;
+  bool fcopy = false;
+  const void* factor_base() const { return fcopy ? fstore.p : arena.p; }
+  size_t factor_bytes() const { return fcopy ? fstore.bytes : arena.bytes; }
   DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, eagroups, small, panel, upd, diagt, zerot;
   int nzero = 0;
   DevMem dfr, dscr, rlist0, perm0;

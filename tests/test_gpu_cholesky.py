@@ -267,3 +267,27 @@ def test_factors_bitwise_reproducible(sylver, gpu, precision):
         assert lib.sylver_gb300_fkeep_factor_bytes(
             f.fkeep, again.ctypes.data_as(ctypes.c_void_p), nb) == nb
         assert np.array_equal(first, again)
+
+
+def test_front_memory_economy_matches(sylver, orc, gpu):
+    """Front storage economy forced on (schedule front_memory = 1: contribution
+    blocks given back to later fronts once the parent's level has assembled
+    them, every level zeroed and initialised just before it, the mode large
+    problems take automatically): the same solutions as the default layout,
+    FP64 against the oracle and FP32 with refinement."""
+    p = w.lognormal27(20, nrhs=2)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    ref = sylver.Factor(an, True, p.a.val).solve(p.rhs)
+    o = orc.OracleFactor(True, an.symbolic(), p.a.val)
+    xo = o.solve(p.rhs)
+    try:
+        sylver.set_schedule(front_memory=1)
+        f = sylver.Factor(an, True, p.a.val)
+        x = f.solve(p.rhs)
+        f32 = sylver.Factor(an, True, p.a.val, precision=sylver.FP32, ir_max_iter=10)
+        x32 = f32.solve(p.rhs)
+    finally:
+        sylver.set_schedule()
+    assert np.abs(x - ref).max() <= 1e-12 * np.abs(ref).max()
+    assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
+    assert w.backward_error(p.a.to_scipy_full(), x32, p.rhs).max() <= 1e-14

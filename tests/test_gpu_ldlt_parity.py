@@ -225,3 +225,58 @@ def test_config1_laplace2d_100(sylver, orc, gpu, precision):
     xo = o.solve(p.rhs)
     assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
     assert np.abs(x - p.x_true.reshape(x.shape)).max() <= 1e-10
+
+
+@pytest.mark.parametrize("name", ["dense_indef_delays_96", "kkt_4", "shifted_laplace3d_9"])
+def test_factor_copyout_exact(sylver, orc, gpu, name):
+    """The compact factor store (schedule front_memory = 1: each level's
+    factor columns copied out of the front blocks, whole blocks given back
+    after the parents' assembly, the mode large-contribution-block matrices
+    take automatically) changes where L lives, not the arithmetic: the same
+    exact agreement with the oracle, and the same solutions (to rounding)."""
+    g = load_golden(name)
+    a = w.SymMatrix(g["n"], g["ptr"], g["row"], g["val"])
+    try:
+        sylver.set_schedule(front_memory=1)
+        tree, o, _ = check_exact(sylver, orc, a, g["order"],
+                                 rhs=None if g["flag"] == 7 else g["rhs"])
+        tree.close()
+    finally:
+        sylver.set_schedule()
+    p = w.shifted_laplace3d(12, nrhs=2)
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
+    ref = sylver.Factor(an, False, p.a.val).solve(p.rhs)
+    try:
+        sylver.set_schedule(front_memory=1)
+        for prec in (sylver.FP64, sylver.FP32):
+            f = sylver.Factor(an, False, p.a.val, precision=prec, ir_max_iter=10)
+            x = f.solve(p.rhs)
+            if prec == sylver.FP64:  # (the solves' atomic sums are not order-fixed)
+                assert np.abs(x - ref).max() <= 1e-12 * np.abs(ref).max()
+            assert w.backward_error(p.a.to_scipy_full(), x, p.rhs).max() <= 1e-14
+    finally:
+        sylver.set_schedule()
+
+
+def test_config5_kkt_full_size(sylver, gpu):
+    """Saddle point [[H, B^T], [B, -1e-8 I]] with H the 7-point Laplacian on
+    40^3 (n = 80,000) under the matching-based ordering with its scaling:
+    a ~1,000-deep chain of fronts with up to 35,061 rows and 30-50 pivots
+    each, whose blocks would need 6.5 TB in place -- the factor columns go to
+    the compact store and whole blocks are given back.  FP64 and FP32 with
+    refinement: Haynsworth inertia, backward error <= 1e-14."""
+    p = w.kkt(40, nrhs=1)
+    o = sylver.default_options()
+    o.ordering = 2
+    o.scaling = 3
+    an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, options=o, val=p.a.val)
+    assert an.flag >= 0 and an.inform.maxfront > 30000
+    full = p.a.to_scipy_full()
+    xs = {}
+    for prec in (sylver.FP32, sylver.FP64):
+        f = sylver.Factor(an, False, p.a.val, precision=prec, ir_max_iter=10, options=o)
+        assert f.flag == 0, f.inform.as_dict()
+        assert f.inform.num_neg == p.inertia[0]
+        assert f.inform.matrix_rank == p.a.n
+        xs[prec] = f.solve(p.rhs)
+        assert w.backward_error(full, xs[prec], p.rhs).max() <= 1e-14
