@@ -270,7 +270,8 @@ enum LsKind {
   LS_SMALL_TRI  // the level's small fronts (launch_small_tri)
 };
 constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
-constexpr int LSOLVE_BW2 = 256;  // columns per solve step
+constexpr int LSOLVE_BW2 = 256;  // columns per solve step (diagonal block with an explicit inverse)
+constexpr int LSOLVE_TW = 256;   // columns of the L tiles of the update and reduction tasks
 constexpr int LSOLVE_UPD_ROWS = 32;  // rows per forward-update CTA
 constexpr int LSOLVE_RED_ROWS = 64;  // rows per backward-reduction CTA
 constexpr int RECT_FWD_T = 128;      // threads of an LS_RECT_FWD task (two contribution rows each)
@@ -300,22 +301,23 @@ struct LsArgs {
   const T* inv;
   const int64_t* inv_off;
   ACC* tt;
-  const T* inv2;            // 256x256 inverses of the solve-step diagonal blocks
+  const T* inv2;            // LSOLVE_BW2-square inverses of the solve-step diagonal blocks
   const int64_t* inv2_off;  // per front of the level
   const T* inv2t;           // the same inverses transposed (row-major)
   // contribution rows' share of the backward reduction, laid out like x
   // (n x nrhs, column stride n); zero between backward sweeps
   ACC* tacc;
 };
-// Inverse of each 256-column diagonal block from its 64x64 inverses: task
-// (front f, c0, bw), output at inv2 + inv2_off[f] + (c0/256)*256*256
-// (column-major) and, transposed, at the same offset of inv2t.
+// Inverse of each solve-step diagonal block (LSOLVE_BW2 columns) from its
+// 64x64 inverses: task (front f, c0, bw), output at inv2 + inv2_off[f] +
+// (c0/LSOLVE_BW2)*LSOLVE_BW2^2 (column-major) and, transposed, at the same
+// offset of inv2t.
 template <typename T>
 void prepare_solve_kernels();
 template <typename T>
-void launch_inv256(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
-                   const T* inv64, const int64_t* inv_off, T* inv2, T* inv2t,
-                   const int64_t* inv2_off, cudaStream_t s);
+void launch_inv_block(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+                      const T* inv64, const int64_t* inv_off, T* inv2, T* inv2t,
+                      const int64_t* inv2_off, cudaStream_t s);
 template <typename T, typename ACC>
 void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, int aux,
                    cudaStream_t s);

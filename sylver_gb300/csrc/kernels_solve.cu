@@ -571,20 +571,24 @@ __global__ void __launch_bounds__(LB) k_inv_diag(const T* __restrict__ arena,
   for (int e = j; e < LB * LB; e += LB) out[e] = Xs[e / LB][e % LB];
 }
 
-// Block steps of BW2 = 256 columns.  Each diagonal block has an explicit
-// inverse (built once per factorization from its four 64x64 inverses), so a
-// step is one parallel mat-vec on the diagonal block plus one update (forward)
-// or reduction (backward) of the rows below, spread over many small CTAs.
-constexpr int BW2 = LSOLVE_BW2;
+// Block steps of SW = LSOLVE_BW2 columns.  Each diagonal block has an
+// explicit inverse (built once per factorization from its 64x64 inverses), so
+// a step is one parallel mat-vec on the diagonal block plus one update
+// (forward) or reduction (backward) of the rows below, spread over many small
+// CTAs whose L tiles are TW = 256 columns wide.  (Steps of 512 columns halve
+// the number of dependent launches but measured no faster: the wider
+// mat-vec takes twice as long and the larger inverses cost more to build.)
+constexpr int SW = LSOLVE_BW2;
+constexpr int TW = 256;
 constexpr int DMV_ROWS = 8;   // rows of the diagonal mat-vec per CTA (32 CTAs per block)
 constexpr int BRED_ROWS = LSOLVE_RED_ROWS;  // rows per backward-reduction CTA
 template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
 
-// X = inverse of the 256-column diagonal block (column-major, ld 256, lower):
-// X_jj = Inv64_j and X_ij = -Inv64_i * sum_{k=j}^{i-1} L_ik X_kj for i > j,
-// with 64x64 blocks; identity beyond bw.
+// X = inverse of the SW-column diagonal block of a step (column-major, ld SW,
+// lower): X_jj = Inv64_j and X_ij = -Inv64_i * sum_{k=j}^{i-1} L_ik X_kj for
+// i > j, with 64x64 blocks; identity beyond bw.
 template <typename T>
-__global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
+__global__ void __launch_bounds__(256) k_inv_block(const T* __restrict__ arena,
                                                 const FrontDesc* __restrict__ fr,
                                                 const LTask* __restrict__ tasks,
                                                 const T* __restrict__ inv64,
@@ -599,15 +603,15 @@ __global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
   const FrontDesc f = fr[t.f];
   const T* L = arena + f.off;
   const int c0 = t.c0, bw = t.bw, tid = threadIdx.x;
-  T* X = inv2 + inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
+  T* X = inv2 + inv2_off[t.f] + (int64_t)(c0 / SW) * SW * SW;
   const T* I64 = inv64 + inv_off[t.f] + (int64_t)(c0 / LB) * LB * LB;
   const int nb = (bw + LB - 1) / LB;
-  for (int e = tid; e < BW2 * BW2; e += blockDim.x) X[e] = T(0);
+  for (int e = tid; e < SW * SW; e += blockDim.x) X[e] = T(0);
   __syncthreads();
-  for (int j = 0; j < 4; ++j)
+  for (int j = 0; j < SW / LB; ++j)
     for (int e = tid; e < LB * LB; e += blockDim.x) {
       int i = e % LB, k = e / LB;
-      X[(int64_t)(LB * j + k) * BW2 + LB * j + i] =
+      X[(int64_t)(LB * j + k) * SW + LB * j + i] =
           (j < nb) ? I64[(int64_t)j * LB * LB + k * LB + i] : T(i == k ? 1 : 0);
     }
   __syncthreads();
@@ -622,7 +626,7 @@ __global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
           int rr = e % LB, kk = e / LB;
           int grow = LB * i + rr, gcol = LB * k + kk;
           As[kk * 65 + rr] = (grow < bw && gcol < bw) ? L[(int64_t)(c0 + gcol) * f.ld + c0 + grow] : T(0);
-          Bs[rr * 65 + kk] = X[(int64_t)(LB * j + rr) * BW2 + LB * k + kk];  // B(kk, rr) = X_kj
+          Bs[rr * 65 + kk] = X[(int64_t)(LB * j + rr) * SW + LB * k + kk];  // B(kk, rr) = X_kj
         }
         __syncthreads();
 #pragma unroll 8
@@ -650,21 +654,21 @@ __global__ void __launch_bounds__(256) k_inv256(const T* __restrict__ arena,
         for (int q = 0; q < 16; ++q) acc[q] += a * Bs[(cq * 16 + q) * 65 + kk];
       }
 #pragma unroll
-      for (int q = 0; q < 16; ++q) X[(int64_t)(LB * j + cq * 16 + q) * BW2 + LB * i + r] = -acc[q];
+      for (int q = 0; q < 16; ++q) X[(int64_t)(LB * j + cq * 16 + q) * SW + LB * i + r] = -acc[q];
       __syncthreads();
     }
   // transposed copy, XT[k*256 + i] = X(k, i), through 64 x 64 shared tiles
-  T* XT = inv2t + inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
-  for (int bj = 0; bj < BW2 / LB; ++bj)
-    for (int bi = 0; bi < BW2 / LB; ++bi) {
+  T* XT = inv2t + inv2_off[t.f] + (int64_t)(c0 / SW) * SW * SW;
+  for (int bj = 0; bj < SW / LB; ++bj)
+    for (int bi = 0; bi < SW / LB; ++bi) {
       for (int e = tid; e < LB * LB; e += blockDim.x) {
         const int rr = e % LB, kk = e / LB;  // X(LB*bi + rr, LB*bj + kk)
-        As[kk * 65 + rr] = X[(int64_t)(LB * bj + kk) * BW2 + LB * bi + rr];
+        As[kk * 65 + rr] = X[(int64_t)(LB * bj + kk) * SW + LB * bi + rr];
       }
       __syncthreads();
       for (int e = tid; e < LB * LB; e += blockDim.x) {
         const int kk = e % LB, rr = e / LB;  // XT(LB*bj + kk, LB*bi + rr)
-        XT[(int64_t)(LB * bi + rr) * BW2 + LB * bj + kk] = As[kk * 65 + rr];
+        XT[(int64_t)(LB * bi + rr) * SW + LB * bj + kk] = As[kk * 65 + rr];
       }
       __syncthreads();
     }
@@ -692,8 +696,8 @@ template <> struct Vec4<double> {
 // block's reduction fills.  With PDL the inverse slice is staged before the
 // wait for the previous launch.
 template <typename T, typename ACC> constexpr size_t diag_mv_smem() {
-  return sizeof(T) * DMV_ROWS * BW2 +
-         sizeof(ACC) * ((256 / DMV_ROWS) * DMV_ROWS * (RGn<ACC>::v + 1) + BW2 * RGn<ACC>::v);
+  return sizeof(T) * DMV_ROWS * SW +
+         sizeof(ACC) * ((256 / DMV_ROWS) * DMV_ROWS * (RGn<ACC>::v + 1) + SW * RGn<ACC>::v);
 }
 template <typename T, typename ACC, bool BWD, bool PDL>
 __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<T, ACC>& a,
@@ -704,19 +708,19 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   T* Ms = reinterpret_cast<T*>(dsm);  // Ms[(k - klo)*DR + il] = M(i0 + il, k)
-  ACC* part = reinterpret_cast<ACC*>(dsm + sizeof(T) * DR * BW2);  // [NG][DR][RG + 1]
-  ACC* vb = part + NG * DR * (RG + 1);                               // [BW2][RG]
+  ACC* part = reinterpret_cast<ACC*>(dsm + sizeof(T) * DR * SW);  // [NG][DR][RG + 1]
+  ACC* vb = part + NG * DR * (RG + 1);                               // [SW][RG]
   const FrontDesc f = a.fr[t.f];
   const int c0 = t.c0, bw = t.bw, i0 = DR * sub;
   const int tid = threadIdx.x, il = tid % DR, g = tid / DR, i = i0 + il;
   const int64_t m = f.m;
   ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  const int64_t moff = a.inv2_off[t.f] + (int64_t)(c0 / BW2) * BW2 * BW2;
+  const int64_t moff = a.inv2_off[t.f] + (int64_t)(c0 / SW) * SW * SW;
   const T* M = (BWD ? a.inv2t : a.inv2) + moff;
-  ACC* tf = a.tt + (int64_t)t.f * 2 * BW2 * MAXR;
-  ACC* tcur = tf + ((c0 / BW2) & 1) * BW2 * MAXR;
-  ACC* tnext = tf + (((c0 / BW2) + 1) & 1) * BW2 * MAXR;
+  ACC* tf = a.tt + (int64_t)t.f * 2 * SW * MAXR;
+  ACC* tcur = tf + ((c0 / SW) & 1) * SW * MAXR;
+  ACC* tnext = tf + (((c0 / SW) + 1) & 1) * SW * MAXR;
   // entries k of v (and columns of the matrix slice) this task needs
   const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + DR), nk = khi - klo;
   __syncthreads();  // the previous task's shared data is no longer read
@@ -725,7 +729,7 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
     // the task's slice of the inverse, one wave of asynchronous copies
     for (int e = tid; e < nk * DR; e += 256) {
       const int rr = e % DR, k = klo + e / DR;
-      cp_async(&Ms[e], &M[(int64_t)k * BW2 + i0 + rr]);
+      cp_async(&Ms[e], &M[(int64_t)k * SW + i0 + rr]);
     }
   }
   if (PDL) pdl_wait();
@@ -735,7 +739,7 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
     __syncthreads();
     {
       // all loads of the slab issued before any is used (nk * RG <= 256 NL)
-      constexpr int NL = BW2 * RG / 256;
+      constexpr int NL = SW * RG / 256;
       ACC v[NL];
 #pragma unroll
       for (int u = 0; u < NL; ++u) {
@@ -801,18 +805,18 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
 // 32 x 256 tile of L is staged in shared memory by one wave of asynchronous
 // copies; y is read as 16-byte vectors (one broadcast per warp).
 template <typename T, typename ACC, int NT> constexpr size_t upd_smem() {
-  return sizeof(T) * 32 * BW2 +
-         sizeof(ACC) * ((NT / 32) * 32 * (RGn<ACC>::v + 1) + BW2 * RGn<ACC>::v);
+  return sizeof(T) * 32 * TW +
+         sizeof(ACC) * ((NT / 32) * 32 * (RGn<ACC>::v + 1) + TW * RGn<ACC>::v);
 }
 template <typename T, typename ACC, int NT, bool PDL>
 __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a,
                                          unsigned char* dsm) {
-  constexpr int RG = RGn<ACC>::v, NGU = NT / 32, KPG = BW2 / NGU;
+  constexpr int RG = RGn<ACC>::v, NGU = NT / 32, KPG = TW / NGU;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   T* Lt = reinterpret_cast<T*>(dsm);  // Lt[k*32 + rr] = L(r0 + rr, c0 + k)
-  ACC* red = reinterpret_cast<ACC*>(dsm + sizeof(T) * 32 * BW2);  // [NGU][32][RG + 1]
-  ACC* yb = red + NGU * 32 * (RG + 1);                              // [BW2][RG]
+  ACC* red = reinterpret_cast<ACC*>(dsm + sizeof(T) * 32 * TW);  // [NGU][32][RG + 1]
+  ACC* yb = red + NGU * 32 * (RG + 1);                              // [TW][RG]
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
   const int tid = threadIdx.x, rr = tid % 32, g = tid / 32;
@@ -826,27 +830,27 @@ __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
-    for (int c0 = cfirst; c0 < clast; c0 += BW2) {
-      const int bw = min(BW2, clast - c0);
+    for (int c0 = cfirst; c0 < clast; c0 += TW) {
+      const int bw = min(TW, clast - c0);
       __syncthreads();  // the previous block's tiles are no longer read
-      for (int e = tid; e < BW2 * 32; e += NT) {
+      for (int e = tid; e < TW * 32; e += NT) {
         const int r2 = e & 31, k = e >> 5;
         if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
         else Lt[e] = T(0);
       }
       if (PDL) pdl_wait();
       {
-        constexpr int NL = BW2 * RG / NT;
+        constexpr int NL = TW * RG / NT;
         ACC v[NL];
 #pragma unroll
         for (int u = 0; u < NL; ++u) {
-          const int e = tid + NT * u, k = e % BW2, r = e / BW2;
+          const int e = tid + NT * u, k = e % TW, r = e / TW;
           v[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
         }
 #pragma unroll
         for (int u = 0; u < NL; ++u) {
           const int e = tid + NT * u;
-          yb[(e % BW2) * RG + e / BW2] = v[u];
+          yb[(e % TW) * RG + e / TW] = v[u];
         }
       }
       cp_async_wait_all();
@@ -896,22 +900,23 @@ __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a
 // contribution rows' share was put into tacc by k_rect_bwd and taken out by
 // the gather.
 template <typename T, typename ACC> constexpr size_t red_smem() {
-  return sizeof(T) * 32 * (BW2 + 1) + sizeof(ACC) * (BW2 * (RGn<ACC>::v + 1) + 32 * RGn<ACC>::v);
+  return sizeof(T) * 32 * (TW + 1) + sizeof(ACC) * (TW * (RGn<ACC>::v + 1) + 32 * RGn<ACC>::v);
 }
 template <typename T, typename ACC, int NT, bool PDL>
 __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a,
                                          unsigned char* dsm) {
-  constexpr int RG = RGn<ACC>::v, SR = 32, NH = NT / BW2;
+  constexpr int RG = RGn<ACC>::v, SR = 32, NH = NT / TW;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
-  T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(BW2+1) + k] = L(s0 + ii, c0 + k)
-  ACC* half = reinterpret_cast<ACC*>(dsm + sizeof(T) * SR * (BW2 + 1));  // [BW2][RG + 1]
-  ACC* xt = half + BW2 * (RG + 1);                                         // [SR][RG]
+  T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(TW+1) + k] = L(s0 + ii, c0 + k)
+  ACC* half = reinterpret_cast<ACC*>(dsm + sizeof(T) * SR * (TW + 1));  // [TW][RG + 1]
+  ACC* xt = half + TW * (RG + 1);                                         // [SR][RG]
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
-  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, k = tid % BW2, h = tid / BW2;
+  const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, k = tid % TW, h = tid / TW;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
-  ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / BW2) & 1)) * BW2 * MAXR;
+  // the accumulator of the step block holding columns [c0, c0 + bw)
+  ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / SW) & 1)) * SW * MAXR + (int64_t)(c0 % SW) * MAXR;
   const int rend = min(t.r0 + BRED_ROWS, f.n);
   __syncthreads();  // the previous task's shared data is no longer read
   if (PDL) pdl_trigger();
@@ -923,9 +928,9 @@ __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a
     for (int s0 = t.r0; s0 < rend; s0 += SR) {
       const int nrow = min(SR, rend - s0);
       __syncthreads();  // the previous sub-tile is no longer read
-      for (int e = tid; e < SR * BW2; e += NT) {
+      for (int e = tid; e < SR * TW; e += NT) {
         const int ii = e % SR, kk = e / SR;
-        T* dst = &Lt[ii * (BW2 + 1) + kk];
+        T* dst = &Lt[ii * (TW + 1) + kk];
         if (ii < nrow && kk < bw) cp_async(dst, &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]);
         else *dst = T(0);
       }
@@ -939,7 +944,7 @@ __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a
 #pragma unroll 8
       for (int i2 = 0; i2 < SR / NH; ++i2) {
         const int ii = h * (SR / NH) + i2;
-        const ACC l = (ACC)Lt[ii * (BW2 + 1) + k];
+        const ACC l = (ACC)Lt[ii * (TW + 1) + k];
         const V* xv = reinterpret_cast<const V*>(&xt[ii * RG]);
 #pragma unroll
         for (int q = 0; q < RG / VW; ++q) {
@@ -1036,8 +1041,8 @@ __global__ void __launch_bounds__(RECT_FWD_T) k_rect_fwd(const LTask* __restrict
   constexpr int VW = Vec4<ACC>::W, KU = RF_KU;
   static_assert(RQ % VW == 0, "right-hand sides per pass");
   extern __shared__ __align__(16) unsigned char dsm[];
-  int* rc = reinterpret_cast<int*>(dsm);        // [BW2] pivot rows of the block
-  ACC* yb = reinterpret_cast<ACC*>(rc + BW2);   // [kpad][RQ]
+  int* rc = reinterpret_cast<int*>(dsm);        // [TW] pivot rows of the block
+  ACC* yb = reinterpret_cast<ACC*>(rc + TW);   // [kpad][RQ]
   const LTask t = tasks[blockIdx.x];
   const FrontDesc f = a.fr[t.f];
   const int* rl = a.rlist + f.rl;
@@ -1243,7 +1248,7 @@ inline int nblocks(int64_t count, int bs) { return (int)((count + bs - 1) / bs);
 
 // dynamic shared memory of the contribution-row kernels
 template <typename T, typename ACC, int RQ> constexpr size_t rect_fwd_smem(int kpad) {
-  return sizeof(int) * BW2 + sizeof(ACC) * (size_t)kpad * RQ;
+  return sizeof(int) * TW + sizeof(ACC) * (size_t)kpad * RQ;
 }
 template <typename T, typename ACC, int RQ> constexpr size_t rect_bwd_smem() {
   return sizeof(T) * rb_nst<T>() * RECT_BWD_COLS * rb_lp<T>() +
@@ -1351,7 +1356,7 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, in
       k_lscatter<T, ACC><<<ntask, 256, 0, s>>>(tasks, a, kind == LS_SCATTER_FWD);
       break;
     case LS_FWD_DIAG2:
-      launch_pdl(k_diag_mv<T, ACC, false>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T, ACC>(), s,
+      launch_pdl(k_diag_mv<T, ACC, false>, dim3(ntask, SW / DMV_ROWS), 256, diag_mv_smem<T, ACC>(), s,
                  tasks, a);
       break;
     case LS_FWD_UPD2:
@@ -1359,7 +1364,7 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, in
       break;
     case LS_RECT_FWD: {
       // aux: the widest task's columns rounded up to the pipeline slice
-      const int kpad = std::min(std::max(aux, RF_KU), BW2);
+      const int kpad = std::min(std::max(aux, RF_KU), TW);
       if (a.nrhs <= 4)
         k_rect_fwd<T, ACC, 4><<<ntask, RECT_FWD_T, rect_fwd_smem<T, ACC, 4>(kpad), s>>>(tasks, a);
       else
@@ -1378,7 +1383,7 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, in
       launch_pdl(k_bwd_red3<T, ACC>, dim3(ntask), 512, red_smem<T, ACC>(), s, tasks, a);
       break;
     case LS_BWD_DIAG2:
-      launch_pdl(k_diag_mv<T, ACC, true>, dim3(ntask, BW2 / DMV_ROWS), 256, diag_mv_smem<T, ACC>(), s,
+      launch_pdl(k_diag_mv<T, ACC, true>, dim3(ntask, SW / DMV_ROWS), 256, diag_mv_smem<T, ACC>(), s,
                  tasks, a);
       break;
   }
@@ -1394,14 +1399,14 @@ void launch_inv_diag(const T* arena, const FrontDesc* fr, const LTask* tasks, in
 template <typename T, int RQ>
 void set_rect_smem() {
   SG_CUDA(cudaFuncSetAttribute(k_rect_fwd<T, T, RQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)rect_fwd_smem<T, T, RQ>(BW2)));
+                               (int)rect_fwd_smem<T, T, RQ>(TW)));
   SG_CUDA(cudaFuncSetAttribute(k_rect_bwd<T, T, RQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)rect_bwd_smem<T, T, RQ>()));
 }
 
 template <typename T>
 void prepare_solve_kernels() {
-  SG_CUDA(cudaFuncSetAttribute(k_inv256<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  SG_CUDA(cudaFuncSetAttribute(k_inv_block<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(2 * 64 * 65 * sizeof(T))));
   SG_CUDA(cudaFuncSetAttribute(k_diag_mv<T, T, false>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_mv_smem<T, T>()));
@@ -1420,19 +1425,19 @@ void prepare_solve_kernels() {
 }
 
 template <typename T>
-void launch_inv256(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
+void launch_inv_block(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
                    const T* inv64, const int64_t* inv_off, T* inv2, T* inv2t,
                    const int64_t* inv2_off, cudaStream_t s) {
   if (ntask <= 0) return;
-  k_inv256<T><<<ntask, 256, 2 * 64 * 65 * sizeof(T), s>>>(arena, fr, tasks, inv64, inv_off,
+  k_inv_block<T><<<ntask, 256, 2 * 64 * 65 * sizeof(T), s>>>(arena, fr, tasks, inv64, inv_off,
                                                            inv2, inv2t, inv2_off);
 }
 template void prepare_solve_kernels<float>();
 template void prepare_solve_kernels<double>();
-template void launch_inv256<float>(const float*, const FrontDesc*, const LTask*, int,
+template void launch_inv_block<float>(const float*, const FrontDesc*, const LTask*, int,
                                    const float*, const int64_t*, float*, float*,
                                    const int64_t*, cudaStream_t);
-template void launch_inv256<double>(const double*, const FrontDesc*, const LTask*, int,
+template void launch_inv_block<double>(const double*, const FrontDesc*, const LTask*, int,
                                     const double*, const int64_t*, double*, double*,
                                     const int64_t*, cudaStream_t);
 

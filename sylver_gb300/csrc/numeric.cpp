@@ -926,8 +926,10 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           if (diag) htasks.push_back({f, c0, bw, 0, 0, 0});
           else if (kind == LS_FWD_UPD2)
             for (int r0 = c1; r0 < d.n; r0 += LSOLVE_UPD_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
-          else
-            for (int r0 = c1; r0 < d.n; r0 += LSOLVE_RED_ROWS) htasks.push_back({f, c0, bw, r0, 0, 0});
+          else  // reductions in column tiles of LSOLVE_TW (one accumulator row per column)
+            for (int h0 = c0; h0 < c1; h0 += LSOLVE_TW)
+              for (int r0 = c1; r0 < d.n; r0 += LSOLVE_RED_ROWS)
+                htasks.push_back({f, h0, std::min(LSOLVE_TW, c1 - h0), r0, 0, 0});
         }
         push(ops, kind, a);
       };
@@ -960,7 +962,7 @@ void SolvePlan::compute_inverses(const T* arena, const FrontDesc* dfr, bool unit
   inv2t.ensure((size_t)std::max<int64_t>(inv2_elems, 1) * sizeof(T));
   launch_inv_diag<T>(arena, dfr, invt.as<LTask>(), (int)hinv.size(), inv.as<T>(),
                      inv_off.as<int64_t>(), unit, s);
-  launch_inv256<T>(arena, dfr, invt2.as<LTask>(), (int)hinv2.size(), inv.as<T>(),
+  launch_inv_block<T>(arena, dfr, invt2.as<LTask>(), (int)hinv2.size(), inv.as<T>(),
                    inv_off.as<int64_t>(), inv2.as<T>(), inv2t.as<T>(), inv2_off.as<int64_t>(),
                    s);
 }
