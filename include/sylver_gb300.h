@@ -313,14 +313,23 @@ int sylver_gb300_profile_levels(void* fkeep, double const* val_dev, double* leve
  * other launches (k: 0/1 gather forward/backward, 2/3 scatter forward/
  * backward, 4 diagonal block forward, 5 rows below forward, 6 rows below
  * backward, 7 diagonal block backward, 8 contribution rows backward, 9
- * contribution rows forward).  Arrays hold 16 entries.  Returns 0, or -98 for an LDL^T factor or nrhs outside
- * 1..32.  No reference counterpart. */
+ * contribution rows forward, 11/12 a level's block steps as one dataflow
+ * launch forward/backward).  Arrays hold 16 entries.  Returns 0, or -98 for
+ * an LDL^T factor or nrhs outside 1..32.  No reference counterpart. */
 int sylver_gb300_profile_solve(void* fkeep, int nrhs, double* ms, long* launches);
 
 /* Diagnostic: run the tensor-core (tcgen05, 3xBF16) contribution-block
  * update on a synthetic rows x k panel and report max|C - C_ref| / max|C_ref|
  * against an FP64 host product.  Returns 0 or a reference flag. */
 int sylver_gb300_tc_selfcheck(int rows, int k, double* max_rel_err);
+
+/* Diagnostic: the bounded wait of the dataflow solve sweep on a synthetic
+ * one-task sweep.  starve != 0: the task waits on a counter nothing sets, so
+ * the wait must give up (ST_TIMEOUT, 32, in *status) and the launch finish;
+ * starve == 0: the counter is set first and *status must be 0.  *seconds:
+ * the launch's wall time.  Faults and hangs nothing; changes no device
+ * setting.  Returns 0 or a reference flag.  No reference counterpart. */
+int sylver_gb300_dataflow_selftest(int starve, unsigned* status, double* seconds);
 
 /* Diagnostic: the device's FP64 fused multiply-add rate in TFLOP/s, from one
  * timed launch of independent fma chains on every SM (CUDA events, after a
@@ -379,6 +388,9 @@ typedef struct {
                             LDL^T: each level's factor columns copied to a compact store and
                             whole blocks given back (LDL^T always gives contribution blocks
                             back) */
+  int solve_dataflow;    /* solves: the block steps of a level's large fronts as one launch of
+                            persistent CTAs that hand each step to the next through counters
+                            (0 or positive, default), or one launch per block step (negative) */
 } sylver_gb300_schedule_t;
 
 /* Set the schedule used by factorizations planned afterwards (a new fkeep);

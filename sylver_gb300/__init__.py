@@ -91,7 +91,7 @@ class Schedule(ctypes.Structure):
     _fields_ = [("small_front_rows", ctypes.c_int), ("tc_min_cb_rows", ctypes.c_int),
                 ("solve_large_cols", ctypes.c_int), ("ldlt_tpp_cols", ctypes.c_int),
                 ("fs_panel_cols", ctypes.c_int), ("fs_panel_group", ctypes.c_int),
-                ("front_memory", ctypes.c_int)]
+                ("front_memory", ctypes.c_int), ("solve_dataflow", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -129,6 +129,7 @@ EXPORTS = (
     "sylver_gb300_fkeep_fronts", "sylver_gb300_akeep_scaling", "sylver_gb300_profile_levels",
     "sylver_gb300_stream", "sylver_gb300_profile_factor", "spldlt_tree_solve_fwd_noalloc_dbl",
     "sylver_gb300_tc_selfcheck", "sylver_gb300_fp64_fma_rate", "sylver_gb300_fkeep_factor_bytes",
+    "sylver_gb300_dataflow_selftest",
     "sylver_gb300_solve_history", "sylver_gb300_set_schedule",
     "sylver_gb300_get_schedule", "sylver_gb300_profile_solve", "sylver_gb300_mlp_create", "sylver_gb300_mlp_free",
     "sylver_gb300_mlp_num_params", "sylver_gb300_mlp_set_params", "sylver_gb300_mlp_get_params",
@@ -179,6 +180,7 @@ def load(path: str | None = None):
         "sylver_gb300_profile_factor": (I, [P, P, P, P, P]),
         "sylver_gb300_profile_solve": (I, [P, I, P, P]),
         "sylver_gb300_tc_selfcheck": (I, [I, I, ctypes.POINTER(D)]),
+        "sylver_gb300_dataflow_selftest": (I, [I, ctypes.POINTER(ctypes.c_uint), ctypes.POINTER(D)]),
         "sylver_gb300_fp64_fma_rate": (I, [ctypes.POINTER(D)]),
         "sylver_gb300_fkeep_factor_bytes": (L, [P, P, L]),
         "sylver_gb300_solve_history": (I, [P, P, I]),
@@ -360,7 +362,7 @@ class Factor:
 
     SOLVE_KINDS = ("small_fwd", "small_bwd", "gather_fwd", "gather_bwd", "scatter_fwd",
                    "scatter_bwd", "diag_fwd", "rows_fwd", "rows_bwd", "diag_bwd", "cb_bwd",
-                   "cb_fwd")
+                   "cb_fwd", "unused", "chain_fwd", "chain_bwd")
 
     def profile_solve(self, nrhs=16):
         """Per-kernel-kind timing of one forward + backward sweep (no graph)."""

@@ -676,6 +676,7 @@ void sylver_gb300_set_schedule(sylver_gb300_schedule_t const* s) {
   c.fs_panel_cols = s->fs_panel_cols;
   c.fs_panel_group = s->fs_panel_group;
   c.front_memory = s->front_memory;
+  c.solve_dataflow = s->solve_dataflow;
 }
 
 void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
@@ -688,6 +689,7 @@ void sylver_gb300_get_schedule(sylver_gb300_schedule_t* s) {
   s->fs_panel_cols = c.fs_panel_cols;
   s->fs_panel_group = c.fs_panel_group;
   s->front_memory = c.front_memory;
+  s->solve_dataflow = c.solve_dataflow;
 }
 
 }  // extern "C"

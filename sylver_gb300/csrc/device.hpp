@@ -51,6 +51,17 @@ __device__ __forceinline__ void cp_async(T* smem, const T* gmem) {
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
 }
+// 16-byte asynchronous copy global -> shared (both addresses 16-byte
+// aligned), and the commit / wait of groups of copies (the wait returns once
+// at most N of the thread's committed groups are still in flight).
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
 // Programmatic dependent launch (kernels launched with launch_pdl): the
 // trigger lets the next launch of the stream start at once; the wait blocks
 // until the previous grid has completed and its writes are visible.  Every
@@ -267,7 +278,41 @@ enum LsKind {
   LS_FWD_DIAG2, LS_FWD_UPD2, LS_BWD_RED2, LS_BWD_DIAG2,
   LS_RECT_BWD,  // contribution rows' share of every pivot row, before the level (backward)
   LS_RECT_FWD,  // contribution rows' update from all pivot rows, after the level (forward)
-  LS_SMALL_TRI  // the level's small fronts (launch_small_tri)
+  LS_SMALL_TRI,  // the level's small fronts (launch_small_tri)
+  LS_CHAIN_FWD,  // the large fronts' block steps of a level as one dataflow launch (launch_chain)
+  LS_CHAIN_BWD
+};
+// One task of a dataflow sweep (launch_chain, FP32 factors): the large
+// fronts' block steps of one level in one launch.  CTAs take tasks in list
+// order (an atomic ticket); the list is a topological order of the
+// dependencies, so a task waits only on tasks taken earlier by running CTAs.
+// Before reading data an earlier task writes, a task waits until counters
+// [w0, w0 + nw) are all >= need0 and counter w1 (if >= 0) is >= need1; when
+// done it adds one to counter sig.  Counter 0 of a level is the ticket.
+// With the products P_ib = L_ib X_b (formed after the factorization) no
+// diagonal mat-vec sits on the chain of block steps:
+//   DF_UPD_FWD   x_i -= P_ib x_b, rows [r0, r0 + 32) below block b, once x_b
+//                is final (the rows of block b + 1 first: the chain)
+//   DF_DIAG_FWD  y_b = X_b x_b (x_b final), output rows [sub*16, +16)
+//   DF_DIAG_BWD  u_b = X_b^T x_b for every block, first
+//   DF_RED_BWD   z_j = u_j - t_j for rows [r0, r0 + 32) of block j, then
+//                t_b += P_jb^T z_j (sub = 1: b = j - 1, the task that also
+//                stores z_j in the xs slab)
+//   DF_FIN_BWD   z_0 = u_0 - t_0, rows [r0, r0 + 32)
+// P_ib sits at pofs in LsArgs::pmat, column-major with leading dimension ldp
+// (rows from the first row below the block).
+enum DfKind { DF_DIAG_FWD, DF_UPD_FWD, DF_RED_BWD, DF_DIAG_BWD, DF_FIN_BWD };
+struct DfTask {
+  int kind, f, c0, bw, r0, sub;
+  int w0, nw, need0, w1, need1, sig;
+  int ldp, pad;
+  int64_t pofs;
+};
+// Formation of P_ib = L_ib X_b: rows [r0, r0 + 64) (from c1, the first row
+// below the block [c0, c1)) of front f's block, into pmat + pofs (ld ldp).
+struct PTask {
+  int f, c0, c1, r0, ldp, pad;
+  int64_t pofs;
 };
 constexpr int LSOLVE_BW = 64;    // inverted diagonal sub-blocks
 constexpr int LSOLVE_BW2 = 256;  // columns per solve step (diagonal block with an explicit inverse)
@@ -287,7 +332,9 @@ constexpr int RECT_BWD_ROWS = 256;   // contribution rows per LS_RECT_BWD task
 // Buffers of the large-front sweeps, per level: xs/ys slabs (scratch, ys),
 // explicit inverses of the 64x64 diagonal blocks (inv + inv_off[f] + block
 // index), tt: two 256 x 32 accumulators per front (backward steps alternate
-// between them; the backward gather clears both).
+// between them; the backward gather clears both), entry (column k, right-hand
+// side r) at r * 256 + k, so that a warp's atomic additions for 32
+// consecutive columns fall in one cache line.
 template <typename T, typename ACC>
 struct LsArgs {
   const T* arena;
@@ -307,6 +354,17 @@ struct LsArgs {
   // contribution rows' share of the backward reduction, laid out like x
   // (n x nrhs, column stride n); zero between backward sweeps
   ACC* tacc;
+  // dataflow sweeps (null otherwise): the level's counters, per front of
+  // the level its counter range (offset, count) and the offset of its
+  // per-block backward accumulators in tt (256 x 32 per 256-column block);
+  // the gathers clear both
+  int* dfc;
+  const int2* dfo;
+  const int64_t* ttoff;
+  // dataflow sweeps (FP32): the products P_ib = L_ib X_b; pmode: the
+  // backward sweep leaves z in the xs slab for the scatter
+  const T* pmat;
+  int pmode;
 };
 // Inverse of each solve-step diagonal block (LSOLVE_BW2 columns) from its
 // 64x64 inverses: task (front f, c0, bw), output at inv2 + inv2_off[f] +
@@ -321,6 +379,15 @@ void launch_inv_block(const T* arena, const FrontDesc* fr, const LTask* tasks, i
 template <typename T, typename ACC>
 void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, int aux,
                    cudaStream_t s);
+// Dataflow sweep over the large fronts of one level (a.dfc: its counters,
+// zeroed by the gather before it): persistent CTAs, at most one per task.
+// A wait that runs past its bound sets ST_TIMEOUT in *err and the task goes
+// on (its result is then wrong, and the caller reports the error).
+void launch_chain(bool bwd, const DfTask* tasks, int ntask, LsArgs<float, float> a, unsigned* err,
+                  cudaStream_t s);
+// P_ib = L_ib X_b for every task (FP32; X from inv2t, row-major).
+void launch_form_p(const float* arena, const FrontDesc* fr, const PTask* tasks, int ntask,
+                   const float* inv2t, const int64_t* inv2_off, float* pmat, cudaStream_t s);
 // Explicit inverse of each diagonal block: task (front f, c0, bw), output at
 // inv + inv_off[f] + (c0/64)*64*64, column-major 64 x 64, identity padded.
 template <typename T>

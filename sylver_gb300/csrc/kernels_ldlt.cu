@@ -114,6 +114,7 @@ __global__ void __launch_bounds__(128) k_app_diag(T* __restrict__ arena, T* __re
   if (tid < 2 * BW) dv[tid] = 0.0;
   __syncthreads();
   if (warp == 0) {
+    __syncwarp();  // reconverge after the lane-dependent staging loop
     // symmetric swap of candidates x < y (lower storage), rows [0, R)
     auto swap_xy = [&](int x, int y) {
       if (x == y) return;

@@ -90,6 +90,7 @@ __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
     // diagonal block: one right-hand side per warp at a time
     for (int r = warp; r < nrhs; r += nwarps) {
       ACC v = (lane < bw) ? xs[(int64_t)r * m + c0 + lane] : ACC(0);
+      __syncwarp();  // converged before the shuffle chain
       for (int kk = 0; kk < bw; ++kk) {
         const ACC vk = __shfl_sync(0xffffffffu, v, kk) * rdg[kk];
         if (lane == kk) v = vk;
@@ -254,6 +255,7 @@ __global__ void __launch_bounds__(256) k_tri(const T* __restrict__ arena,
           if (two) w -= tt[lane][r2];
         }
       }
+      __syncwarp();  // converged before the shuffle chain
       if (!BWD) {
         for (int kk = 0; kk < bw; ++kk) {
           const ACC vk = __shfl_sync(0xffffffffu, v, kk) * rdg[kk];
@@ -492,7 +494,19 @@ constexpr int LB = LSOLVE_BW;
 template <typename T, typename ACC>
 __device__ __forceinline__ void gather_body(const LTask& t, const LsArgs<T, ACC>& a, bool fwd) {
   const FrontDesc f = a.fr[t.f];
-  if (!fwd && t.r0 == 0) {
+  if (a.dfc != nullptr) {
+    // dataflow sweep next: its counters (the ticket with the first task) and,
+    // backward, the accumulator of the 256-column block holding these rows
+    if (t.r0 == 0) {
+      const int2 o = a.dfo[t.f];
+      for (int e = threadIdx.x; e < o.y; e += blockDim.x) a.dfc[o.x + e] = 0;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.dfc[0] = 0;
+    if (!fwd) {
+      ACC* tb = a.tt + a.ttoff[t.f] + (int64_t)(t.r0 / LSOLVE_BW2) * LSOLVE_BW2 * MAXR;
+      for (int e = threadIdx.x; e < LSOLVE_BW2 * MAXR; e += blockDim.x) tb[e] = ACC(0);
+    }
+  } else if (!fwd && t.r0 == 0) {
     ACC* tf = a.tt + (int64_t)t.f * 2 * LSOLVE_BW2 * MAXR;
     for (int e = threadIdx.x; e < 2 * LSOLVE_BW2 * MAXR; e += blockDim.x) tf[e] = ACC(0);
   }
@@ -518,12 +532,13 @@ __device__ __forceinline__ void gather_body(const LTask& t, const LsArgs<T, ACC>
 
 // Scatter of the solved pivot rows (ys) of a large front back to x.
 template <typename T, typename ACC>
-__device__ __forceinline__ void scatter_body(const LTask& t, const LsArgs<T, ACC>& a) {
+__device__ __forceinline__ void scatter_body(const LTask& t, const LsArgs<T, ACC>& a, bool fwd) {
   const FrontDesc f = a.fr[t.f];
   const int i = t.r0 + threadIdx.x;
   if (threadIdx.x >= 256 || i >= f.n) return;
   const int v = a.rlist[f.rl + i];
-  const ACC* src = a.ys + a.scr_off[t.f] * a.nrhs + i;
+  // the backward sweep with P leaves z in the xs slab
+  const ACC* src = (a.pmode && !fwd ? a.scratch : a.ys) + a.scr_off[t.f] * a.nrhs + i;
   ACC val[MAXR];
 #pragma unroll
   for (int r = 0; r < MAXR; ++r) val[r] = r < a.nrhs ? src[(int64_t)r * f.m] : ACC(0);
@@ -539,7 +554,7 @@ __global__ void k_lgather(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, boo
 
 template <typename T, typename ACC>
 __global__ void k_lscatter(const LTask* __restrict__ tasks, LsArgs<T, ACC> a, bool fwd) {
-  scatter_body<T, ACC>(tasks[blockIdx.x], a);
+  scatter_body<T, ACC>(tasks[blockIdx.x], a, fwd);
 }
 
 // X = L^-1 for one diagonal block, thread j computes column j; L is read
@@ -583,6 +598,11 @@ constexpr int TW = 256;
 constexpr int DMV_ROWS = 8;   // rows of the diagonal mat-vec per CTA (32 CTAs per block)
 constexpr int BRED_ROWS = LSOLVE_RED_ROWS;  // rows per backward-reduction CTA
 template <typename ACC> struct RGn { static constexpr int v = sizeof(ACC) == 8 ? 8 : 16; };
+// Row stride of the [k][RG] right-hand-side slabs in shared memory: padded by
+// 16 bytes so that the transposing stores (consecutive lanes, consecutive k)
+// spread over the banks (4-way instead of 16-way conflicts for FP32) while
+// rows stay 16-byte aligned for the vector reads.
+template <typename ACC> struct RGP { static constexpr int v = RGn<ACC>::v + 16 / (int)sizeof(ACC); };
 
 // X = inverse of the SW-column diagonal block of a step (column-major, ld SW,
 // lower): X_jj = Inv64_j and X_ij = -Inv64_i * sum_{k=j}^{i-1} L_ik X_kj for
@@ -674,6 +694,78 @@ __global__ void __launch_bounds__(256) k_inv_block(const T* __restrict__ arena,
     }
 }
 
+// P_ib = L_ib X_b (FP32), 64 rows per task: thread (rows 4tr .. 4tr + 3,
+// columns 16tc .. 16tc + 15); the inner index in chunks of 32 staged by
+// 16-byte copies (columns of L, rows of X from its row-major copy).  X_b is
+// lower triangular, so chunk [i0, i0 + 32) adds nothing to columns > i0 + 31.
+__global__ void __launch_bounds__(256) k_form_p(const float* __restrict__ arena,
+                                                const FrontDesc* __restrict__ fr,
+                                                const PTask* __restrict__ tasks,
+                                                const float* __restrict__ inv2t,
+                                                const int64_t* __restrict__ inv2_off,
+                                                float* __restrict__ pmat) {
+  __shared__ __align__(16) float As[32][64];   // As[i][r] = L(r0 + r, c0 + i0 + i)
+  __shared__ __align__(16) float Bs[32][SW];   // Bs[i][k] = X(i0 + i, k)
+  const PTask t = tasks[blockIdx.x];
+  const FrontDesc f = fr[t.f];
+  const float* L = arena + f.off;
+  const float* XT = inv2t + inv2_off[t.f] + (int64_t)(t.c0 / SW) * SW * SW;
+  const int tid = threadIdx.x, tr = tid & 15, tc = tid >> 4;
+  const int nr = min(64, f.n - t.r0);
+  float acc[4][16];
+#pragma unroll
+  for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+    for (int jj = 0; jj < 16; ++jj) acc[ii][jj] = 0.f;
+  for (int i0 = 0; i0 < SW; i0 += 32) {
+    __syncthreads();  // the previous chunk is no longer read
+    for (int e = tid; e < 32 * 16; e += 256) {
+      const int i = e / 16, r4 = 4 * (e % 16);
+      float* dst = &As[i][r4];
+      const float* src = &L[(int64_t)(t.c0 + i0 + i) * f.ld + t.r0 + r4];
+      if (r4 + 4 <= nr) {
+        cp_async16(dst, src);
+      } else {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) dst[u] = (r4 + u < nr) ? src[u] : 0.f;
+      }
+    }
+    for (int e = tid; e < 32 * (SW / 4); e += 256) {
+      const int i = e / (SW / 4), k4 = 4 * (e % (SW / 4));
+      cp_async16(&Bs[i][k4], &XT[(int64_t)(i0 + i) * SW + k4]);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    if (16 * tc > i0 + 31) continue;
+#pragma unroll 4
+    for (int i = 0; i < 32; ++i) {
+      const float4 a4 = *reinterpret_cast<const float4*>(&As[i][4 * tr]);
+      const float av[4] = {a4.x, a4.y, a4.z, a4.w};
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        const float4 b4 = *reinterpret_cast<const float4*>(&Bs[i][16 * tc + 4 * m]);
+        const float bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+        for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[ii][4 * m + q] = fmaf(av[ii], bv[q], acc[ii][4 * m + q]);
+      }
+    }
+  }
+  float* out = pmat + t.pofs + (t.r0 - t.c1) + 4 * tr;
+#pragma unroll
+  for (int jj = 0; jj < 16; ++jj) {
+    float* o = out + (int64_t)(16 * tc + jj) * t.ldp;
+    if (4 * tr + 4 <= nr) {
+      *reinterpret_cast<float4*>(o) = make_float4(acc[0][jj], acc[1][jj], acc[2][jj], acc[3][jj]);
+    } else {
+#pragma unroll
+      for (int ii = 0; ii < 4; ++ii)
+        if (4 * tr + ii < nr) o[ii] = acc[ii][jj];
+    }
+  }
+}
+
 template <typename ACC> struct Vec4;
 template <> struct Vec4<float> {
   using V = float4;
@@ -695,15 +787,32 @@ template <> struct Vec4<double> {
 // accumulator (c0/256)&1 and clears the other one, which the next (lower)
 // block's reduction fills.  With PDL the inverse slice is staged before the
 // wait for the previous launch.
-template <typename T, typename ACC> constexpr size_t diag_mv_smem() {
-  return sizeof(T) * DMV_ROWS * SW +
-         sizeof(ACC) * ((256 / DMV_ROWS) * DMV_ROWS * (RGn<ACC>::v + 1) + SW * RGn<ACC>::v);
+template <typename T, typename ACC, int DR = DMV_ROWS> constexpr size_t diag_mv_smem() {
+  return sizeof(T) * DR * SW +
+         sizeof(ACC) * ((256 / DR) * DR * (RGn<ACC>::v + 1) + SW * RGP<ACC>::v);
 }
-template <typename T, typename ACC, bool BWD, bool PDL>
+// MODE 0: one launch per step (programmatic dependent launch, two backward
+// accumulators per front used in turn); MODE 1: a task of a dataflow sweep
+// with the products P_ib = L_ib X_b (no accumulator in the diagonal tasks).
+// wait() is called by every thread before the first read of data an earlier
+// step wrote; those reads bypass L1 (__ldcg), since in a dataflow sweep the
+// writer is another CTA of the same launch.
+struct PdlWait {
+  __device__ void operator()() const { pdl_wait(); }
+};
+// MODE 1: where a task's product tile comes from (P's rows start at the first
+// row below the block), and whether a backward reduction task also stores
+// the z rows it forms
+template <typename T> struct PSrc {
+  const T* base = nullptr;
+  int64_t ld = 0;
+  bool writer = false;
+};
+template <typename T, typename ACC, bool BWD, int DR, int MODE, typename W>
 __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<T, ACC>& a,
-                                          unsigned char* dsm) {
-  constexpr int RG = RGn<ACC>::v;
-  constexpr int DR = DMV_ROWS;  // output rows per task; 256 / DR k-phases per row
+                                          unsigned char* dsm, const W& wait) {
+  constexpr int RG = RGn<ACC>::v, RS = RGP<ACC>::v;
+  // DR output rows per task; 256 / DR k-phases per row
   constexpr int NG = 256 / DR;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
@@ -724,15 +833,16 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
   // entries k of v (and columns of the matrix slice) this task needs
   const int klo = BWD ? i0 : 0, khi = BWD ? bw : min(bw, i0 + DR), nk = khi - klo;
   __syncthreads();  // the previous task's shared data is no longer read
-  if (PDL) pdl_trigger();
+  if (MODE == 0) pdl_trigger();
   if (i0 < bw) {
     // the task's slice of the inverse, one wave of asynchronous copies
-    for (int e = tid; e < nk * DR; e += 256) {
-      const int rr = e % DR, k = klo + e / DR;
-      cp_async(&Ms[e], &M[(int64_t)k * SW + i0 + rr]);
+    constexpr int E = 16 / (int)sizeof(T), DQ = DR / E;  // 16-byte pieces per column
+    for (int e = tid; e < nk * DQ; e += 256) {
+      const int rr = E * (e % DQ), k = klo + e / DQ;
+      cp_async16(&Ms[(k - klo) * DR + rr], &M[(int64_t)k * SW + i0 + rr]);
     }
   }
-  if (PDL) pdl_wait();
+  wait();
   // rows beyond the block: nothing to compute (uniform per task)
   for (int rg = 0; rg < (i0 < bw ? a.nrhs : 0); rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
@@ -747,14 +857,14 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
         const int k = klo + e % max(nk, 1), r = e / max(nk, 1);
         v[u] = ACC(0);
         if (e < nk * RG && r < nr) {
-          v[u] = xs[(int64_t)(rg + r) * m + c0 + k];
-          if (BWD) v[u] -= tcur[k * MAXR + rg + r];
+          v[u] = __ldcg(&xs[(int64_t)(rg + r) * m + c0 + k]);
+          if (BWD && MODE == 0) v[u] -= __ldcg(&tcur[(int64_t)(rg + r) * SW + k]);
         }
       }
 #pragma unroll
       for (int u = 0; u < NL; ++u) {
         const int e = tid + 256 * u;
-        if (e < nk * RG) vb[(klo + e % nk) * RG + e / nk] = v[u];
+        if (e < nk * RG) vb[(klo + e % nk) * RS + e / nk] = v[u];
       }
     }
     cp_async_wait_all();
@@ -767,7 +877,7 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
 #pragma unroll 4
       for (int k = k0 + ((g - k0) % NG + NG) % NG; k < k1; k += NG) {
         const ACC l = (ACC)Ms[(k - klo) * DR + il];
-        const V* vv = reinterpret_cast<const V*>(vb + k * RG);
+        const V* vv = reinterpret_cast<const V*>(vb + k * RS);
 #pragma unroll
         for (int q = 0; q < RG / VW; ++q) {
           const V x4 = vv[q];
@@ -796,8 +906,8 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
       }
     }
   }
-  if (BWD)
-    for (int e = tid; e < DR * MAXR; e += 256) tnext[i0 * MAXR + e] = ACC(0);
+  if (BWD && MODE == 0)
+    for (int e = tid; e < DR * MAXR; e += 256) tnext[(int64_t)(e / DR) * SW + i0 + e % DR] = ACC(0);
 }
 
 // Fully-summed rows [r0, r0+32) (< n) below the block: xs_i -= L_i,blk y_blk;
@@ -806,12 +916,13 @@ __device__ __forceinline__ void diag_body(const LTask& t, int sub, const LsArgs<
 // copies; y is read as 16-byte vectors (one broadcast per warp).
 template <typename T, typename ACC, int NT> constexpr size_t upd_smem() {
   return sizeof(T) * 32 * TW +
-         sizeof(ACC) * ((NT / 32) * 32 * (RGn<ACC>::v + 1) + TW * RGn<ACC>::v);
+         sizeof(ACC) * ((NT / 32) * 32 * (RGn<ACC>::v + 1) + TW * RGP<ACC>::v);
 }
-template <typename T, typename ACC, int NT, bool PDL>
+template <typename T, typename ACC, int NT, int MODE, typename W>
 __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a,
-                                         unsigned char* dsm) {
-  constexpr int RG = RGn<ACC>::v, NGU = NT / 32, KPG = TW / NGU;
+                                         unsigned char* dsm, const W& wait,
+                                         const PSrc<T>& ps = PSrc<T>{}) {
+  constexpr int RG = RGn<ACC>::v, RS = RGP<ACC>::v, NGU = NT / 32, KPG = TW / NGU;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   T* Lt = reinterpret_cast<T*>(dsm);  // Lt[k*32 + rr] = L(r0 + rr, c0 + k)
@@ -824,33 +935,60 @@ __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   const int nrow = min(32, f.n - t.r0);  // fully-summed rows only
   const int cfirst = t.c0, clast = t.c0 + t.bw;
-  if (PDL) pdl_trigger();
+  // the product's tile: L(r0 + rr, c0 + k), or with MODE 1 P(r0 + rr, k)
+  const T* tb = MODE == 1 ? ps.base + (t.r0 - cfirst - SW) : L + (int64_t)cfirst * f.ld + t.r0;
+  const int64_t tld = MODE == 1 ? ps.ld : (int64_t)f.ld;
+  // ... times y_b, or with MODE 1 the block's final x_b
+  const ACC* yin = MODE == 1 ? xs : ysl;
+  __syncthreads();  // the previous task's shared data is no longer read
+  if (MODE == 0) pdl_trigger();
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     ACC acc[RG];
 #pragma unroll
     for (int q = 0; q < RG; ++q) acc[q] = ACC(0);
+    // the rows' current values, read as soon as the wait allows (their
+    // round trip overlaps the product)
+    constexpr int NX = (32 * RG + NT - 1) / NT;
+    ACC xold[NX];
     for (int c0 = cfirst; c0 < clast; c0 += TW) {
       const int bw = min(TW, clast - c0);
       __syncthreads();  // the previous block's tiles are no longer read
-      for (int e = tid; e < TW * 32; e += NT) {
-        const int r2 = e & 31, k = e >> 5;
-        if (k < bw && r2 < nrow) cp_async(&Lt[e], &L[(int64_t)(c0 + k) * f.ld + t.r0 + r2]);
-        else Lt[e] = T(0);
+      // 16-byte pieces of each column (rows t.r0 + r2, r2 a multiple of E:
+      // 16-byte aligned, t.r0 being a multiple of 32 past a full block)
+      constexpr int E = 16 / (int)sizeof(T), PQ = 32 / E;
+      for (int e = tid; e < TW * PQ; e += NT) {
+        const int r2 = E * (e % PQ), k = e / PQ;
+        T* dst = &Lt[k * 32 + r2];
+        const T* src = tb + (int64_t)(c0 - cfirst + k) * tld + r2;
+        if (k < bw && r2 + E <= nrow) {
+          cp_async16(dst, src);
+        } else {
+#pragma unroll
+          for (int u = 0; u < E; ++u) dst[u] = (k < bw && r2 + u < nrow) ? src[u] : T(0);
+        }
       }
-      if (PDL) pdl_wait();
+      wait();
+      if (c0 == cfirst) {
+#pragma unroll
+        for (int u = 0; u < NX; ++u) {
+          const int e = tid + NT * u, r2 = e % 32, q = e / 32;
+          xold[u] = (e < 32 * RG && r2 < nrow && q < nr)
+                        ? __ldcg(&xs[(int64_t)(rg + q) * f.m + t.r0 + r2]) : ACC(0);
+        }
+      }
       {
         constexpr int NL = TW * RG / NT;
         ACC v[NL];
 #pragma unroll
         for (int u = 0; u < NL; ++u) {
           const int e = tid + NT * u, k = e % TW, r = e / TW;
-          v[u] = (k < bw && r < nr) ? ysl[(int64_t)(rg + r) * f.m + c0 + k] : ACC(0);
+          v[u] = (k < bw && r < nr) ? __ldcg(&yin[(int64_t)(rg + r) * f.m + c0 + k]) : ACC(0);
         }
 #pragma unroll
         for (int u = 0; u < NL; ++u) {
           const int e = tid + NT * u;
-          yb[(e % TW) * RG + e / TW] = v[u];
+          yb[(e % TW) * RS + e / TW] = v[u];
         }
       }
       cp_async_wait_all();
@@ -859,7 +997,7 @@ __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a
       for (int kk = 0; kk < KPG; ++kk) {
         const int k = g * KPG + kk;
         const ACC l = (ACC)Lt[k * 32 + rr];
-        const V* yv = reinterpret_cast<const V*>(yb + k * RG);
+        const V* yv = reinterpret_cast<const V*>(yb + k * RS);
 #pragma unroll
         for (int q = 0; q < RG / VW; ++q) {
           const V y4 = yv[q];
@@ -879,13 +1017,14 @@ __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a
     for (int q = 0; q < RG; ++q) red[(g * 32 + rr) * (RG + 1) + q] = acc[q];
     __syncthreads();
     // 32 rows x RG sums, spread over all threads
-    for (int e = tid; e < 32 * RG; e += NT) {
-      const int r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
-      if (r2 < nrow && q < nr) {
+#pragma unroll
+    for (int u = 0; u < NX; ++u) {
+      const int e = tid + NT * u, r2 = e % 32, q = e / 32, i2 = t.r0 + r2;
+      if (e < 32 * RG && r2 < nrow && q < nr) {
         ACC sum = ACC(0);
 #pragma unroll
         for (int gg = 0; gg < NGU; ++gg) sum += red[(gg * 32 + r2) * (RG + 1) + q];
-        xs[(int64_t)(rg + q) * f.m + i2] -= sum;
+        xs[(int64_t)(rg + q) * f.m + i2] = xold[u] - sum;
       }
     }
     __syncthreads();
@@ -900,12 +1039,13 @@ __device__ __forceinline__ void upd_body(const LTask& t, const LsArgs<T, ACC>& a
 // contribution rows' share was put into tacc by k_rect_bwd and taken out by
 // the gather.
 template <typename T, typename ACC> constexpr size_t red_smem() {
-  return sizeof(T) * 32 * (TW + 1) + sizeof(ACC) * (TW * (RGn<ACC>::v + 1) + 32 * RGn<ACC>::v);
+  return sizeof(T) * 32 * (TW + 1) + sizeof(ACC) * (TW * (RGn<ACC>::v + 1) + 32 * RGP<ACC>::v);
 }
-template <typename T, typename ACC, int NT, bool PDL>
+template <typename T, typename ACC, int NT, int MODE, typename W>
 __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a,
-                                         unsigned char* dsm) {
-  constexpr int RG = RGn<ACC>::v, SR = 32, NH = NT / TW;
+                                         unsigned char* dsm, const W& wait,
+                                         const PSrc<T>& ps = PSrc<T>{}) {
+  constexpr int RG = RGn<ACC>::v, RS = RGP<ACC>::v, SR = 32, NH = NT / TW;
   using V = typename Vec4<ACC>::V;
   constexpr int VW = Vec4<ACC>::W;
   T* Lt = reinterpret_cast<T*>(dsm);  // Lt[ii*(TW+1) + k] = L(s0 + ii, c0 + k)
@@ -914,12 +1054,15 @@ __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a
   const FrontDesc f = a.fr[t.f];
   const T* L = a.arena + f.off;
   const int c0 = t.c0, bw = t.bw, tid = threadIdx.x, k = tid % TW, h = tid / TW;
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
   const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
   // the accumulator of the step block holding columns [c0, c0 + bw)
-  ACC* tf = a.tt + ((int64_t)t.f * 2 + ((c0 / SW) & 1)) * SW * MAXR + (int64_t)(c0 % SW) * MAXR;
-  const int rend = min(t.r0 + BRED_ROWS, f.n);
+  ACC* tf = (MODE == 1 ? a.tt + a.ttoff[t.f] + (int64_t)(c0 / SW) * SW * MAXR
+                       : a.tt + ((int64_t)t.f * 2 + ((c0 / SW) & 1)) * SW * MAXR) +
+            (c0 % SW);
+  const int rend = min(t.r0 + (MODE == 1 ? SR : BRED_ROWS), f.n);
   __syncthreads();  // the previous task's shared data is no longer read
-  if (PDL) pdl_trigger();
+  if (MODE == 0) pdl_trigger();
   for (int rg = 0; rg < a.nrhs; rg += RG) {
     const int nr = min(RG, a.nrhs - rg);
     ACC acc[RG];
@@ -931,13 +1074,26 @@ __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a
       for (int e = tid; e < SR * TW; e += NT) {
         const int ii = e % SR, kk = e / SR;
         T* dst = &Lt[ii * (TW + 1) + kk];
-        if (ii < nrow && kk < bw) cp_async(dst, &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]);
+        if (ii < nrow && kk < bw)
+          cp_async(dst, MODE == 1 ? ps.base + (int64_t)kk * ps.ld + (s0 + ii - c0 - SW)
+                                  : &L[(int64_t)(c0 + kk) * f.ld + s0 + ii]);
         else *dst = T(0);
       }
-      if (PDL) pdl_wait();
+      wait();
       for (int e = tid; e < SR * RG; e += NT) {
         const int ii = e % SR, r = e / SR;
-        xt[ii * RG + r] = (ii < nrow && r < nr) ? ysl[(int64_t)(rg + r) * f.m + s0 + ii] : ACC(0);
+        ACC z = ACC(0);
+        if (ii < nrow && r < nr) {
+          const int64_t xi = (int64_t)(rg + r) * f.m + s0 + ii;
+          z = __ldcg(&ysl[xi]);
+          if (MODE == 1) {
+            // z = u - t of the row's block (complete: the wait covered it)
+            const int row = s0 + ii, jb = row / SW;
+            z -= __ldcg(&a.tt[a.ttoff[t.f] + ((int64_t)jb * MAXR + rg + r) * SW + (row - jb * SW)]);
+            if (ps.writer) xs[xi] = z;
+          }
+        }
+        xt[ii * RS + r] = z;
       }
       cp_async_wait_all();
       __syncthreads();
@@ -945,7 +1101,7 @@ __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a
       for (int i2 = 0; i2 < SR / NH; ++i2) {
         const int ii = h * (SR / NH) + i2;
         const ACC l = (ACC)Lt[ii * (TW + 1) + k];
-        const V* xv = reinterpret_cast<const V*>(&xt[ii * RG]);
+        const V* xv = reinterpret_cast<const V*>(&xt[ii * RS]);
 #pragma unroll
         for (int q = 0; q < RG / VW; ++q) {
           const V x4 = xv[q];
@@ -970,7 +1126,7 @@ __device__ __forceinline__ void red_body(const LTask& t, const LsArgs<T, ACC>& a
     if (h == 0 && k < bw)
 #pragma unroll
       for (int q = 0; q < RG; ++q)
-        if (q < nr) aadd(&tf[k * MAXR + rg + q], acc[q] + (NH == 2 ? half[k * (RG + 1) + q] : ACC(0)));
+        if (q < nr) aadd(&tf[(int64_t)(rg + q) * SW + k], acc[q] + (NH == 2 ? half[k * (RG + 1) + q] : ACC(0)));
     __syncthreads();
   }
 }
@@ -979,29 +1135,116 @@ template <typename T, typename ACC, bool BWD>
 __global__ void __launch_bounds__(256) k_diag_mv(const LTask* __restrict__ tasks,
                                                  LsArgs<T, ACC> a) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  diag_body<T, ACC, BWD, true>(tasks[blockIdx.x], blockIdx.y, a, dsm);
+  diag_body<T, ACC, BWD, DMV_ROWS, 0>(tasks[blockIdx.x], blockIdx.y, a, dsm, PdlWait{});
 }
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(512) k_fwd_upd3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  upd_body<T, ACC, 512, true>(tasks[blockIdx.x], a, dsm);
+  upd_body<T, ACC, 512, 0>(tasks[blockIdx.x], a, dsm, PdlWait{});
 }
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ tasks,
                                                   LsArgs<T, ACC> a) {
   extern __shared__ __align__(16) unsigned char dsm[];
-  red_body<T, ACC, 512, true>(tasks[blockIdx.x], a, dsm);
+  red_body<T, ACC, 512, 0>(tasks[blockIdx.x], a, dsm, PdlWait{});
 }
 
-// 16-byte asynchronous copy global -> shared (both addresses 16-byte aligned)
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+// ---------------------------------------------------------------------------
+// Dataflow sweep: the block steps of all large fronts of a level in one
+// launch.  Persistent CTAs take tasks in list order through an atomic ticket
+// (counter 0); every task's dependencies come earlier in the list, so a CTA
+// only ever waits for tasks that running CTAs have already taken, whatever
+// the number of CTAs resident.  Critical path per block step: the diagonal
+// tasks' counter handoff plus one mat-vec, instead of a kernel launch.
+constexpr int DF_SPIN_LIMIT = 1 << 20;  // polls per wait (under a second with the back-off)
+constexpr int DF_ROWS = 16;  // output rows per diagonal task (LSOLVE_BW2 / 16 tasks per block)
+
+// counters [w0, w0 + nw) >= need0 and counter w1 (>= 0) >= need1, polled by
+// thread 0; gives up (ST_TIMEOUT in *err) after DF_SPIN_LIMIT polls or once
+// another wait gave up
+struct DfWait {
+  const int* cnt;
+  unsigned* err;
+  int w0, nw, need0, w1, need1;
+  __device__ bool poll(const int* c, int need) const {
+    unsigned ns = 32;
+    for (int it = 0; it < DF_SPIN_LIMIT; ++it) {
+      if (*reinterpret_cast<const volatile int*>(c) >= need) return true;
+      if (*reinterpret_cast<volatile unsigned*>(err) & ST_TIMEOUT) return false;
+      __nanosleep(ns);
+      if (ns < 256) ns *= 2;
+    }
+    atomicOr(err, ST_TIMEOUT);
+    return false;
+  }
+  __device__ void operator()() const {
+    if (threadIdx.x == 0) {
+      bool ok = true;
+      for (int q = 0; q < nw && ok; ++q) ok = poll(cnt + w0 + q, need0);
+      if (ok && w1 >= 0) poll(cnt + w1, need1);
+      __threadfence();
+    }
+    __syncthreads();
+  }
+};
+
+// z = u - t for rows [r0, r0 + 32) of a front's first block (MODE 1
+// backward: the blocks below are finished by the reductions that read them)
+template <typename T, typename ACC, typename W>
+__device__ __forceinline__ void fin_body(const LTask& t, const LsArgs<T, ACC>& a, const W& wait) {
+  const FrontDesc f = a.fr[t.f];
+  ACC* xs = a.scratch + a.scr_off[t.f] * a.nrhs;
+  const ACC* ysl = a.ys + a.scr_off[t.f] * a.nrhs;
+  const ACC* tb = a.tt + a.ttoff[t.f];
+  const int nrow = min(32, f.n - t.r0);
+  wait();
+  for (int e = threadIdx.x; e < 32 * a.nrhs; e += blockDim.x) {
+    const int ii = e % 32, r = e / 32, row = t.r0 + ii;
+    if (ii < nrow) {
+      const int64_t xi = (int64_t)r * f.m + row;
+      xs[xi] = __ldcg(&ysl[xi]) - __ldcg(&tb[(int64_t)r * SW + row]);
+    }
+  }
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+
+template <typename T, typename ACC, bool BWD>
+__global__ void __launch_bounds__(256) k_chain(const DfTask* __restrict__ tasks, int ntask,
+                                               LsArgs<T, ACC> a, unsigned* __restrict__ err) {
+  extern __shared__ __align__(16) unsigned char dsm[];
+  __shared__ int s_ti;
+  constexpr int DR = DF_ROWS;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) s_ti = atomicAdd(a.dfc, 1);
+    __syncthreads();
+    const int ti = s_ti;
+    if (ti >= ntask) break;
+    const DfTask d = tasks[ti];
+    const DfWait w{a.dfc, err, d.w0, d.nw, d.need0, d.w1, d.need1};
+    const LTask t{d.f, d.c0, d.bw, d.r0, 0, 0};
+    PSrc<T> ps;
+    ps.base = a.pmat + d.pofs;
+    ps.ld = d.ldp;
+    ps.writer = d.sub != 0;
+    if (!BWD) {
+      if (d.kind == DF_DIAG_FWD) diag_body<T, ACC, false, DR, 1>(t, d.sub, a, dsm, w);
+      else upd_body<T, ACC, 256, 1>(t, a, dsm, w, ps);
+    } else {
+      if (d.kind == DF_RED_BWD) red_body<T, ACC, 256, 1>(t, a, dsm, w, ps);
+      else if (d.kind == DF_DIAG_BWD) diag_body<T, ACC, true, DR, 1>(t, d.sub, a, dsm, w);
+      else fin_body<T, ACC>(t, a, w);
+    }
+    // every thread's results visible device-wide before the count
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(a.dfc + d.sig, 1);
+  }
+}
+template <typename T, typename ACC> constexpr size_t chain_smem() {
+  constexpr size_t d = diag_mv_smem<T, ACC, DF_ROWS>(), u = upd_smem<T, ACC, 256>(),
+                   r = red_smem<T, ACC>();
+  return d > u ? (d > r ? d : r) : (u > r ? u : r);
 }
 
 // The contribution-row kernels read L in 16-byte pieces of a column: every
@@ -1389,6 +1632,18 @@ void launch_lsolve(int kind, const LTask* tasks, int ntask, LsArgs<T, ACC> a, in
   }
 }
 
+// persistent CTAs of a dataflow sweep: resident CTAs per SM x SMs (set once)
+static int g_chain_ctas = 0;
+
+void launch_chain(bool bwd, const DfTask* tasks, int ntask, LsArgs<float, float> a, unsigned* err,
+                  cudaStream_t s) {
+  if (ntask <= 0) return;
+  const int grid = std::max(1, std::min(ntask, g_chain_ctas));
+  if (bwd) k_chain<float, float, true><<<grid, 256, chain_smem<float, float>(), s>>>(tasks, ntask, a, err);
+  else k_chain<float, float, false><<<grid, 256, chain_smem<float, float>(), s>>>(tasks, ntask, a, err);
+  SG_CUDA(cudaGetLastError());
+}
+
 template <typename T>
 void launch_inv_diag(const T* arena, const FrontDesc* fr, const LTask* tasks, int ntask,
                      T* inv, const int64_t* inv_off, bool unit, cudaStream_t s) {
@@ -1422,6 +1677,24 @@ void prepare_solve_kernels() {
                                (int)upd_smem<T, T, 512>()));
   SG_CUDA(cudaFuncSetAttribute(k_bwd_red3<T, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)red_smem<T, T>()));
+  if constexpr (std::is_same<T, float>::value) {
+    const int cs = (int)chain_smem<T, T>();
+    SG_CUDA(cudaFuncSetAttribute(k_chain<T, T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
+    SG_CUDA(cudaFuncSetAttribute(k_chain<T, T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, cs));
+    int dev = 0, nsm = 0, per0 = 0, per1 = 0;
+    SG_CUDA(cudaGetDevice(&dev));
+    SG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    SG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per0, k_chain<T, T, false>, 256, cs));
+    SG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per1, k_chain<T, T, true>, 256, cs));
+    g_chain_ctas = std::max(1, nsm * std::max(1, std::min(per0, per1)));
+  }
+}
+
+void launch_form_p(const float* arena, const FrontDesc* fr, const PTask* tasks, int ntask,
+                   const float* inv2t, const int64_t* inv2_off, float* pmat, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_form_p<<<ntask, 256, 0, s>>>(arena, fr, tasks, inv2t, inv2_off, pmat);
+  SG_CUDA(cudaGetLastError());
 }
 
 template <typename T>

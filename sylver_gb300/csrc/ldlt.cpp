@@ -661,7 +661,8 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   put(L.sfr, L.hsfr, s);
   put(L.sscr, L.hsscr, s);
   put(L.sdoff, L.hsdoff, s);
-  fk.splan.build_tasks(L.hsfr, fk.levels, s);
+  fk.splan.dataflow = Schedule::current().solve_dataflow >= 0;
+  fk.splan.build_tasks(L.hsfr, fk.levels, (int)sizeof(T), s);
   fk.splan.compute_inverses<T>(static_cast<const T*>(fk.factor_base()), L.sfr.as<FrontDesc>(),
                               true, s);
   SG_CUDA(cudaStreamSynchronize(s));

@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <stdexcept>
 #include <type_traits>
 
 namespace sylver_gb300 {
@@ -609,7 +610,8 @@ void FKeep::plan_cholesky() {
   upd.upload(upds, s);
   dfr.upload(hfr, s);
   dscr.upload(hscr, s);
-  splan.build_tasks(hfr, levels, s);
+  splan.dataflow = sched.solve_dataflow >= 0;
+  splan.build_tasks(hfr, levels, precision == 1 ? 4 : 8, s);
   rlist0.upload(rl0, s);
   std::vector<int> p0(st.n);
   for (int i = 0; i < st.n; ++i) p0[i] = st.perm[i];
@@ -639,6 +641,7 @@ void FKeep::upload_static(cudaStream_t s) {
     splan.inv.ensure((size_t)std::max<int64_t>(splan.inv_elems, 1) * es);
     splan.inv2.ensure((size_t)std::max<int64_t>(splan.inv2_elems, 1) * es);
     splan.inv2t.ensure((size_t)std::max<int64_t>(splan.inv2_elems, 1) * es);
+    if (splan.dataflow && splan.p_elems > 0) splan.pmat.ensure((size_t)splan.p_elems * sizeof(float));
   }
   tcerr.ensure(sizeof(unsigned));
   if (blkinv_count > 0) blkinv.ensure((size_t)blkinv_count * BLK_B * BLK_B * sizeof(float));
@@ -836,10 +839,21 @@ std::vector<int> SolvePlan::small_first(const std::vector<FrontDesc>& hfr,
 }
 
 void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector<Level>& levels,
-                            cudaStream_t s) {
+                            int elem, cudaStream_t s) {
   const int LB = LSOLVE_BW;
   lv.clear();
   htasks.clear();
+  hdf.clear();
+  hdfo.assign(hfr.size(), make_int2(0, 0));
+  httoff.assign(hfr.size(), 0);
+  dfc_elems = 0;
+  df_tt_elems = 0;
+  // the dataflow sweeps need the FP32 products P_ib (FP64: per-step launches)
+  if (elem != 4) dataflow = false;
+  hpt.clear();
+  p_elems = 0;
+  // rows per dataflow diagonal task (DfRows in kernels_solve.cu)
+  const int DFR = 16, NSUB = LSOLVE_BW2 / DFR;
   hinv.clear();
   hinv_off.assign(hfr.size(), 0);
   inv_elems = 0;
@@ -933,22 +947,149 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
         }
         push(ops, kind, a);
       };
-      for (int b = 0; b < maxb2; ++b) {
-        step(v.fwd, LS_FWD_DIAG2, b, true);
-        step(v.fwd, LS_FWD_UPD2, b, false);
+      if (dataflow) {
+        // counters of the level: [0] ticket, then per front: row tiles of 32
+        // (forward: updates applied), per block: a sink (the tasks nothing
+        // waits for count there), reductions added and diagonal tasks done
+        // (backward)
+        constexpr int RT = LSOLVE_UPD_ROWS, BR = 32;  // rows per update / reduction task
+        v.dfc_base = dfc_elems;
+        int cnt = 1;
+        int64_t tto = 0;
+        std::vector<int> o(v.nfront, 0), nrt(v.nfront, 0), nbk(v.nfront, 0);
+        for (int f = v.nsmall; f < v.nfront; ++f) {
+          const int n = hfr[L.f0 + f].n;
+          nrt[f] = (n + RT - 1) / RT;
+          nbk[f] = (n + LB2 - 1) / LB2;
+          o[f] = cnt;
+          hdfo[L.f0 + f] = make_int2(cnt, nrt[f] + 3 * nbk[f]);
+          cnt += nrt[f] + 3 * nbk[f];
+          httoff[L.f0 + f] = tto;
+          tto += (int64_t)nbk[f] * LB2 * 32;
+        }
+        dfc_elems += cnt;
+        v.dfc_count = cnt;
+        df_tt_elems = std::max(df_tt_elems, tto);
+        auto bw_of = [&](int f, int b) { return std::min(LB2, hfr[L.f0 + f].n - b * LB2); };
+        auto ready = [&](int f, int b) { return o[f] + nrt[f] + b; };           // forward
+        auto nred_ctr = [&](int f, int b) { return o[f] + nrt[f] + nbk[f] + b; };
+        auto zdone = [&](int f, int b) { return o[f] + nrt[f] + 2 * nbk[f] + b; };
+        auto nred_of = [&](int f, int j) {  // reductions into block j: 32-row pieces below it
+          int c = 0;
+          for (int jj = j + 1; jj < nbk[f]; ++jj) c += (bw_of(f, jj) + BR - 1) / BR;
+          return c;
+        };
+        // P_ib for every block with rows below it (ld: rows rounded up to 4)
+        std::vector<std::vector<std::pair<int64_t, int>>> pb(v.nfront);
+        for (int f = v.nsmall; f < v.nfront; ++f) {
+          const int n = hfr[L.f0 + f].n;
+          for (int b = 0; b + 1 < nbk[f]; ++b) {
+            const int c1 = (b + 1) * LB2, ldp = round_up(n - c1, 4);
+            pb[f].push_back({p_elems, ldp});
+            for (int r0 = c1; r0 < n; r0 += 64)
+              hpt.push_back({L.f0 + f, b * LB2, c1, r0, ldp, 0, p_elems});
+            p_elems += (int64_t)ldp * LB2;
+          }
+        }
+        // forward: x_i -= P_ib x_b once x_b is final (the next block's rows
+        // first: the chain); y_b = X_b x_b off the chain
+        int64_t a = (int64_t)hdf.size();
+        for (int b = 0; b < maxb2; ++b) {
+          for (int pass = 0; pass < 2; ++pass)
+            for (int f = v.nsmall; f < v.nfront; ++f) {
+              if (b + 1 >= nbk[f]) continue;
+              const int t0 = b * LB2 / RT, nt = LB2 / RT, tn = (b + 2) * LB2 / RT;
+              const int lo = pass == 0 ? (b + 1) * LB2 / RT : tn, hi = pass == 0 ? tn : nrt[f];
+              for (int rt = lo; rt < std::min(hi, nrt[f]); ++rt)
+                hdf.push_back({DF_UPD_FWD, f, b * LB2, LB2, rt * RT, 0, o[f] + t0, b > 0 ? nt : 0,
+                               b, o[f] + rt, b, o[f] + rt, pb[f][b].second, 0, pb[f][b].first});
+            }
+          for (int f = v.nsmall; f < v.nfront; ++f) {
+            if (b >= nbk[f]) continue;
+            const int t0 = b * LB2 / RT, nt = (bw_of(f, b) + RT - 1) / RT;
+            for (int q = 0; q < NSUB; ++q)
+              hdf.push_back({DF_DIAG_FWD, f, b * LB2, bw_of(f, b), 0, q, o[f] + t0, b > 0 ? nt : 0,
+                             b, -1, 0, ready(f, 0), 0, 0, 0});
+          }
+        }
+        v.fwd.push_back({LS_CHAIN_FWD, a, (int64_t)hdf.size()});
+        rows(v.fwd, LS_SCATTER_FWD);
+        rows(v.bwd, LS_GATHER_BWD);
+        // backward: u_b = X_b^T x_b for every block; then from the last
+        // block: z_j = u_j - t_j and t_b += P_jb^T z_j (the block before
+        // first: the chain; its tasks store z_j); z_0 = u_0 - t_0
+        a = (int64_t)hdf.size();
+        for (int f = v.nsmall; f < v.nfront; ++f)
+          for (int b = 0; b < nbk[f]; ++b)
+            for (int q = 0; q < NSUB; ++q)
+              hdf.push_back({DF_DIAG_BWD, f, b * LB2, bw_of(f, b), 0, q, 0, 0, 0, -1, 0,
+                             zdone(f, b), 0, 0, 0});
+        for (int j = maxb2 - 1; j >= 1; --j)
+          for (int b = j - 1; b >= 0; --b)
+            for (int f = v.nsmall; f < v.nfront; ++f) {
+              if (j >= nbk[f]) continue;
+              const int r1 = j * LB2 + bw_of(f, j);
+              for (int r0 = j * LB2; r0 < r1; r0 += BR)
+                hdf.push_back({DF_RED_BWD, f, b * LB2, LB2, r0, b == j - 1 ? 1 : 0,
+                               nred_ctr(f, j), 1, nred_of(f, j), zdone(f, j), NSUB,
+                               nred_ctr(f, b), pb[f][b].second, 0, pb[f][b].first});
+            }
+        for (int f = v.nsmall; f < v.nfront; ++f)
+          for (int r0 = 0; r0 < bw_of(f, 0); r0 += BR)
+            hdf.push_back({DF_FIN_BWD, f, 0, bw_of(f, 0), r0, 0, nred_ctr(f, 0), 1,
+                           nred_of(f, 0), zdone(f, 0), NSUB, ready(f, 0), 0, 0, 0});
+        v.bwd.push_back({LS_CHAIN_BWD, a, (int64_t)hdf.size()});
+        rows(v.bwd, LS_SCATTER_BWD);
+      } else {
+        for (int b = 0; b < maxb2; ++b) {
+          step(v.fwd, LS_FWD_DIAG2, b, true);
+          step(v.fwd, LS_FWD_UPD2, b, false);
+        }
+        rows(v.fwd, LS_SCATTER_FWD);
+        rows(v.bwd, LS_GATHER_BWD);
+        for (int b = maxb2 - 1; b >= 0; --b) {
+          step(v.bwd, LS_BWD_RED2, b, false);
+          step(v.bwd, LS_BWD_DIAG2, b, true);
+        }
+        rows(v.bwd, LS_SCATTER_BWD);
       }
-      rows(v.fwd, LS_SCATTER_FWD);
-      rows(v.bwd, LS_GATHER_BWD);
-      for (int b = maxb2 - 1; b >= 0; --b) {
-        step(v.bwd, LS_BWD_RED2, b, false);
-        step(v.bwd, LS_BWD_DIAG2, b, true);
-      }
-      rows(v.bwd, LS_SCATTER_BWD);
     }
     rect(v.fwd, true);
     lv.push_back(std::move(v));
   }
   tasks.upload(htasks, s);
+  if (dataflow) {
+    // Each sweep's list must be a topological order: run it in list order on
+    // the host, every wait already met when its task comes up (then a CTA
+    // only ever waits for tasks running CTAs took before it), every counter
+    // inside the level's range.
+    for (const Lv& v : lv)
+      for (int dir = 0; dir < 2; ++dir)
+        for (const SOp& op : dir ? v.bwd : v.fwd) {
+          if (op.kind != LS_CHAIN_FWD && op.kind != LS_CHAIN_BWD) continue;
+          const int64_t lim = v.dfc_count;
+          std::vector<int> c((size_t)lim, 0);
+          for (int64_t q = op.a; q < op.b; ++q) {
+            const DfTask& t = hdf[q];
+            auto in = [&](int i) { return i > 0 && i < lim; };
+            bool ok = in(t.sig) && (t.nw == 0 || (in(t.w0) && in(t.w0 + t.nw - 1))) &&
+                      (t.w1 < 0 || in(t.w1));
+            for (int i = 0; ok && i < t.nw; ++i) ok = c[t.w0 + i] >= t.need0;
+            if (ok && t.w1 >= 0) ok = c[t.w1] >= t.need1;
+            if (!ok) throw std::runtime_error("dataflow solve: task list out of order");
+            c[t.sig]++;
+          }
+        }
+    dftasks.upload(hdf, s);
+    ptasks.upload(hpt, s);
+    dfo.upload(hdfo, s);
+    ttoff.upload(httoff, s);
+    dfcnt.ensure((size_t)std::max<int64_t>(dfc_elems, 1) * sizeof(int));
+    if (!dferr.p) {
+      dferr.ensure(sizeof(unsigned));
+      SG_CUDA(cudaMemsetAsync(dferr.p, 0, sizeof(unsigned), s));
+    }
+  }
   invt.upload(hinv, s);
   inv_off.upload(hinv_off, s);
   invt2.upload(hinv2, s);
@@ -965,15 +1106,30 @@ void SolvePlan::compute_inverses(const T* arena, const FrontDesc* dfr, bool unit
   launch_inv_block<T>(arena, dfr, invt2.as<LTask>(), (int)hinv2.size(), inv.as<T>(),
                    inv_off.as<int64_t>(), inv2.as<T>(), inv2t.as<T>(), inv2_off.as<int64_t>(),
                    s);
+  if constexpr (std::is_same<T, float>::value) {
+    if (dataflow && !hpt.empty()) {
+      pmat.ensure((size_t)p_elems * sizeof(float));
+      launch_form_p(arena, dfr, ptasks.as<PTask>(), (int)hpt.size(), inv2t.as<float>(),
+                    inv2_off.as<int64_t>(), pmat.as<float>(), s);
+    }
+  }
 }
 template void SolvePlan::compute_inverses<float>(const float*, const FrontDesc*, bool,
                                                  cudaStream_t);
 template void SolvePlan::compute_inverses<double>(const double*, const FrontDesc*, bool,
                                                   cudaStream_t);
 
+void SolvePlan::fetch_error(unsigned* h, cudaStream_t s) {
+  *h = 0;
+  if (!dataflow || !dferr.p) return;
+  SG_CUDA(cudaMemcpyAsync(h, dferr.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  SG_CUDA(cudaMemsetAsync(dferr.p, 0, sizeof(unsigned), s));
+}
+
 void SolvePlan::ensure_tt(size_t elem, int64_t scratch_elems, int n) {
   const void* before = tt.p;
-  tt.ensure((size_t)std::max(max_large, 1) * 2 * LSOLVE_BW2 * 32 * elem);
+  tt.ensure((size_t)std::max<int64_t>((int64_t)std::max(max_large, 1) * 2 * LSOLVE_BW2 * 32,
+                                      df_tt_elems) * elem);
   // the backward steps leave the accumulators zero; a new buffer starts zero
   if (tt.p != before) SG_CUDA(cudaMemset(tt.p, 0, tt.bytes));
   ys.ensure((size_t)std::max<int64_t>(scratch_elems, 1) * elem);
@@ -993,10 +1149,21 @@ void SolvePlan::run(bool fwd, const T* arena, const FrontDesc* dfr, const int* r
     const int64_t* sc = dscr + v.f0;
     LsArgs<T, ACC> a{arena, fr, rlist, x, n, nrhs, scratch, ys.as<ACC>(), sc, inv.as<T>(),
                      inv_off.as<int64_t>() + v.f0, tt.as<ACC>(), inv2.as<T>(),
-                     inv2_off.as<int64_t>() + v.f0, inv2t.as<T>(), tacc.as<ACC>()};
+                     inv2_off.as<int64_t>() + v.f0, inv2t.as<T>(), tacc.as<ACC>(),
+                     dataflow ? dfcnt.as<int>() + v.dfc_base : nullptr,
+                     dataflow ? dfo.as<int2>() + v.f0 : nullptr,
+                     dataflow ? ttoff.as<int64_t>() + v.f0 : nullptr,
+                     dataflow ? static_cast<const T*>(pmat.p) : nullptr, dataflow ? 1 : 0};
     const std::vector<SOp>& ops = fwd ? v.fwd : v.bwd;
     for (size_t k = 0; k < ops.size(); ++k) {
       const SOp& op = ops[k];
+      if (op.kind == LS_CHAIN_FWD || op.kind == LS_CHAIN_BWD) {
+        if constexpr (std::is_same<T, float>::value && std::is_same<ACC, float>::value)
+          launch_chain(op.kind == LS_CHAIN_BWD, dftasks.as<DfTask>() + op.a, (int)(op.b - op.a),
+                       a, dferr.as<unsigned>(), s);
+        if (prof) mark(2 + op.kind, s);
+        continue;
+      }
       if (op.kind == LS_SMALL_TRI) {
         launch_small_tri<T, ACC>(fwd, arena, fr, v.nsmall, rlist, x, tacc.as<ACC>(), n, nrhs,
                                  v.small_maxn, unit, s);
@@ -1107,7 +1274,10 @@ int FKeep::solve_raw(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
   for (int r = 0; r < nrhs; ++r)
     SG_CUDA(cudaMemcpyAsync(x + (size_t)r * ldx, xp.as<double>() + (size_t)r * n,
                             n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  return 0;
+  unsigned dferr_h = 0;
+  splan.fetch_error(&dferr_h, s);
+  SG_CUDA(cudaStreamSynchronize(s));
+  return dferr_h ? SYLVER_ERROR_CUDA_UNKNOWN : 0;
 }
 
 int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
@@ -1139,10 +1309,12 @@ int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
     }
   };
   const bool refine = job == 0 && (f32 || ir_max_iter > 0);
+  unsigned dferr_h = 0;  // a dataflow sweep's bounded wait gave up: the result is wrong
   if (!refine) {
     one_solve(x, ldx, x, ldx, false, job);
+    splan.fetch_error(&dferr_h, s);
     SG_CUDA(cudaStreamSynchronize(s));
-    return 0;
+    return dferr_h ? SYLVER_ERROR_CUDA_UNKNOWN : 0;
   }
   // iterative refinement: x0 = solve(b); repeat r = b - A x (FP64), check
   // the scaled backward error, x += solve(r)
@@ -1163,7 +1335,9 @@ int FKeep::solve(int job, int nrhs, double* x, int ldx, cudaStream_t s) {
                     norms.as<double>(), s);
     SG_CUDA(cudaMemcpyAsync(hn.data(), norms.p, 3 * nrhs * sizeof(double),
                             cudaMemcpyDeviceToHost, s));
+    splan.fetch_error(&dferr_h, s);
     SG_CUDA(cudaStreamSynchronize(s));
+    if (dferr_h) return SYLVER_ERROR_CUDA_UNKNOWN;
     double worst = 0.0;
     for (int r = 0; r < nrhs; ++r) {
       double den = anorm_h * hn[3 * r + 1] + hn[3 * r + 2];

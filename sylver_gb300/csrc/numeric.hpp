@@ -59,6 +59,8 @@ struct Schedule {
                              // path (multiple of 64, <= 256; <0: 64-column SIMT steps)
   int fs_panel_group = 0;    // FP32 Cholesky: outer panels per trailing fully-summed update
   int front_memory = 0;      // front storage economy: 1 always, < 0 never, 0 when needed
+  int solve_dataflow = 0;    // large-front solve sweeps: one dataflow launch per level
+                             // (>= 0) or one launch per block step (< 0)
   static Schedule& current();
   // default 96 rows: measured faster than the FP32 cap of 128 on 40^3, 56^3 and
   // 80^3 log-normal 27-point matrices (schedule sweeps of the learned scheduler)
@@ -138,8 +140,26 @@ struct SolvePlan {
   struct Lv {
     int f0 = 0, nsmall = 0, nfront = 0;
     int small_maxn = 0;  // most pivot rows of the level's small fronts
+    int64_t dfc_base = 0, dfc_count = 0;  // dataflow sweeps: the level's counters in dfcnt
     std::vector<SOp> fwd, bwd;
   };
+  // Dataflow sweeps (LS_CHAIN_FWD / LS_CHAIN_BWD, task ranges in hdf) instead
+  // of one launch per block step; set before build_tasks, which keeps it for
+  // FP32 factors only.
+  bool dataflow = true;
+  std::vector<DfTask> hdf;
+  std::vector<int2> hdfo;         // per level-ordered front: its counters (offset, count)
+  std::vector<int64_t> httoff;    // per level-ordered front: its backward accumulators in tt
+  int64_t dfc_elems = 0, df_tt_elems = 0;
+  DevMem dftasks, dfo, ttoff, dfcnt, dferr;
+  // the dataflow sweeps use P_ib = L_ib X_b, formed after each factorization
+  // with the inverses (hpt: its tasks, p_elems floats)
+  std::vector<PTask> hpt;
+  int64_t p_elems = 0;
+  DevMem ptasks, pmat;
+  // error bits a dataflow sweep raised since the last call (ST_TIMEOUT), read
+  // into *h by an asynchronous copy on s that the caller synchronizes
+  void fetch_error(unsigned* h, cudaStream_t s);
   std::vector<Lv> lv;
   std::vector<LTask> htasks;
   std::vector<LTask> hinv;       // diagonal blocks to invert (f = level-ordered index)
@@ -158,8 +178,9 @@ struct SolvePlan {
   // build_tasks.
   static std::vector<int> small_first(const std::vector<FrontDesc>& hfr,
                                       const std::vector<Level>& levels);
+  // elem: bytes of the factor's entries (the dataflow diagonal tasks' rows)
   void build_tasks(const std::vector<FrontDesc>& hfr, const std::vector<Level>& levels,
-                   cudaStream_t s);
+                   int elem, cudaStream_t s);
   void ensure_tt(size_t elem, int64_t scratch_elems, int n);
   template <typename T, typename ACC>
   void run(bool fwd, const T* arena, const FrontDesc* dfr, const int* rlist, ACC* x, int n,

@@ -112,7 +112,8 @@ def test_schedule_round_trip(sylver):
     """Every field of sylver_gb300_schedule_t reaches the library and comes
     back; no arguments restore the defaults (zeros)."""
     vals = dict(small_front_rows=96, tc_min_cb_rows=128, solve_large_cols=64, ldlt_tpp_cols=8,
-                fs_panel_cols=128, fs_panel_group=3, front_memory=1)
+                fs_panel_cols=128, fs_panel_group=3, front_memory=1,
+                solve_dataflow=-1)
     try:
         sylver.set_schedule(**vals)
         assert sylver.get_schedule() == vals
