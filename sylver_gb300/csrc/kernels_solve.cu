@@ -1251,6 +1251,28 @@ template <typename T, typename ACC> constexpr size_t chain_smem() {
 // front's storage starts on a 64-element boundary with a leading dimension
 // that is a multiple of 4, so a piece that starts on a row divisible by 4 is
 // 16-byte aligned (and lies inside the column's padded length).
+// Two FP32 fused multiply-adds in one instruction (fma.rn.f32x2, sm_100
+// and later): c + a * b lane by lane on values packed two to a 64-bit
+// register (the lower half is the first), each rounded exactly as fmaf.
+// Halves the FMA instructions of the backward contribution-row product,
+// which issues 16 multiply-adds per 4-byte entry of L at 16 right-hand sides
+// (0.94 -> 0.86 ms per sweep at 80^3; the forward kernel, which holds eight
+// columns of L in flight in registers, measured slower with it: 0.69 -> 0.88).
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ unsigned long long f2dup(float v) {
+  const unsigned long long u = __float_as_uint(v);
+  return u | (u << 32);
+}
+__device__ __forceinline__ float f2lo(unsigned long long v) { return __uint_as_float((unsigned)v); }
+__device__ __forceinline__ float f2hi(unsigned long long v) {
+  return __uint_as_float((unsigned)(v >> 32));
+}
+
 constexpr int RF_KU = 8;   // columns of L in flight per thread (forward)
 constexpr int RB_SR = 16;  // rows per pipeline slice (backward)
 template <typename T> constexpr int rb_nst() { return 3; }
@@ -1415,6 +1437,9 @@ __global__ void __launch_bounds__(RECT_BWD_T) k_rect_bwd(const LTask* __restrict
     ACC acc0[RQ], acc1[RQ];
 #pragma unroll
     for (int q = 0; q < RQ; ++q) acc0[q] = acc1[q] = ACC(0);
+    unsigned long long pa0[RQ / 2], pa1[RQ / 2];  // FP32: packed pairs (fma.rn.f32x2)
+#pragma unroll
+    for (int q = 0; q < RQ / 2; ++q) pa0[q] = pa1[q] = 0ull;
     for (int s = 0; s < nst; ++s) {
       cp_async_wait<NST - 2>();
       __syncthreads();  // slice s landed for all; slice s - 1's buffers are free
@@ -1440,19 +1465,20 @@ __global__ void __launch_bounds__(RECT_BWD_T) k_rect_bwd(const LTask* __restrict
 #pragma unroll
         for (int u = 0; u < CH; ++u) {
           const V* xv = reinterpret_cast<const V*>(xb + (i4 + u) * RQ);
+          if constexpr (VW == 4) {
+            const unsigned long long d0 = f2dup(l0[u]), d1 = f2dup(l1[u]);
 #pragma unroll
-          for (int q = 0; q < RQ / VW; ++q) {
-            const V x4 = xv[q];
-            if constexpr (VW == 4) {
-              acc0[4 * q + 0] += l0[u] * x4.x;
-              acc0[4 * q + 1] += l0[u] * x4.y;
-              acc0[4 * q + 2] += l0[u] * x4.z;
-              acc0[4 * q + 3] += l0[u] * x4.w;
-              acc1[4 * q + 0] += l1[u] * x4.x;
-              acc1[4 * q + 1] += l1[u] * x4.y;
-              acc1[4 * q + 2] += l1[u] * x4.z;
-              acc1[4 * q + 3] += l1[u] * x4.w;
-            } else {
+            for (int q = 0; q < RQ / 4; ++q) {
+              const ulonglong2 x2 = reinterpret_cast<const ulonglong2*>(xv)[q];
+              pa0[2 * q] = f2fma(d0, x2.x, pa0[2 * q]);
+              pa0[2 * q + 1] = f2fma(d0, x2.y, pa0[2 * q + 1]);
+              pa1[2 * q] = f2fma(d1, x2.x, pa1[2 * q]);
+              pa1[2 * q + 1] = f2fma(d1, x2.y, pa1[2 * q + 1]);
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < RQ / VW; ++q) {
+              const V x4 = xv[q];
               acc0[2 * q + 0] += l0[u] * x4.x;
               acc0[2 * q + 1] += l0[u] * x4.y;
               acc1[2 * q + 0] += l1[u] * x4.x;
@@ -1460,6 +1486,15 @@ __global__ void __launch_bounds__(RECT_BWD_T) k_rect_bwd(const LTask* __restrict
             }
           }
         }
+      }
+    }
+    if constexpr (VW == 4) {
+#pragma unroll
+      for (int q = 0; q < RQ / 2; ++q) {
+        acc0[2 * q] = f2lo(pa0[q]);
+        acc0[2 * q + 1] = f2hi(pa0[q]);
+        acc1[2 * q] = f2lo(pa1[q]);
+        acc1[2 * q + 1] = f2hi(pa1[q]);
       }
     }
     cp_async_wait<0>();
