@@ -1160,29 +1160,40 @@ __global__ void __launch_bounds__(512) k_bwd_red3(const LTask* __restrict__ task
 constexpr int DF_SPIN_LIMIT = 1 << 20;  // polls per wait (under a second with the back-off)
 constexpr int DF_ROWS = 16;  // output rows per diagonal task (LSOLVE_BW2 / 16 tasks per block)
 
-// counters [w0, w0 + nw) >= need0 and counter w1 (>= 0) >= need1, polled by
-// thread 0; gives up (ST_TIMEOUT in *err) after DF_SPIN_LIMIT polls or once
+// counters [w0, w0 + nw) >= need0 and counter w1 (>= 0) >= need1 (nw < 32),
+// polled by warp 0, one counter per lane so that all of them cost one round
+// trip; gives up (ST_TIMEOUT in *err) after DF_SPIN_LIMIT polls or once
 // another wait gave up
 struct DfWait {
   const int* cnt;
   unsigned* err;
   int w0, nw, need0, w1, need1;
-  __device__ bool poll(const int* c, int need) const {
-    unsigned ns = 32;
-    for (int it = 0; it < DF_SPIN_LIMIT; ++it) {
-      if (*reinterpret_cast<const volatile int*>(c) >= need) return true;
-      if (*reinterpret_cast<volatile unsigned*>(err) & ST_TIMEOUT) return false;
-      __nanosleep(ns);
-      if (ns < 256) ns *= 2;
-    }
-    atomicOr(err, ST_TIMEOUT);
-    return false;
-  }
   __device__ void operator()() const {
-    if (threadIdx.x == 0) {
-      bool ok = true;
-      for (int q = 0; q < nw && ok; ++q) ok = poll(cnt + w0 + q, need0);
-      if (ok && w1 >= 0) poll(cnt + w1, need1);
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      const int* c = nullptr;
+      int need = 0;
+      if (lane < nw) {
+        c = cnt + w0 + lane;
+        need = need0;
+      } else if (lane == nw && w1 >= 0) {
+        c = cnt + w1;
+        need = need1;
+      }
+      bool done = c == nullptr, all = false, gaveup = false;
+      unsigned ns = 32;
+      for (int it = 0; it < DF_SPIN_LIMIT; ++it) {
+        if (!done) done = *reinterpret_cast<const volatile int*>(c) >= need;
+        all = __all_sync(0xffffffffu, done);
+        if (all) break;
+        if ((it & 63) == 63 && (*reinterpret_cast<volatile unsigned*>(err) & ST_TIMEOUT)) {
+          gaveup = true;  // the same value in every lane: one load for the warp
+          break;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns *= 2;
+      }
+      if (!all && !gaveup && lane == 0) atomicOr(err, ST_TIMEOUT);
       __threadfence();
     }
     __syncthreads();

@@ -1072,7 +1072,7 @@ void SolvePlan::build_tasks(const std::vector<FrontDesc>& hfr, const std::vector
           for (int64_t q = op.a; q < op.b; ++q) {
             const DfTask& t = hdf[q];
             auto in = [&](int i) { return i > 0 && i < lim; };
-            bool ok = in(t.sig) && (t.nw == 0 || (in(t.w0) && in(t.w0 + t.nw - 1))) &&
+            bool ok = in(t.sig) && t.nw < 32 && (t.nw == 0 || (in(t.w0) && in(t.w0 + t.nw - 1))) &&
                       (t.w1 < 0 || in(t.w1));
             for (int i = 0; ok && i < t.nw; ++i) ok = c[t.w0 + i] >= t.need0;
             if (ok && t.w1 >= 0) ok = c[t.w1] >= t.need1;
