@@ -12,14 +12,21 @@
 // (src/NumericFront.hxx:299-390 alloc_contrib_blocks / free_contrib_blocks,
 // src/kernels/assemble.hxx:216-223 fini_node).
 //
-// Host-side bookkeeping only: best fit over coalesced free intervals, then
-// the top of the used region.  All sizes and addresses are in elements,
-// multiples of 64 (every front starts on a 64-element boundary).
+// Host-side bookkeeping only: best fit over coalesced free intervals (the
+// shortest that fits, the lowest address among equals), then the top of the
+// used region.  The free intervals are kept by address (for coalescing) and
+// by length (for the fit), so each call costs O(log #intervals): the LDL^T
+// factorization places its fronts level by level at factor time, and a
+// linear scan over thousands of holes cost milliseconds per factorization.
+// All sizes and addresses are in elements, multiples of 64 (every front
+// starts on a 64-element boundary).
 #pragma once
 
 #include <cstdint>
 #include <iterator>
 #include <map>
+#include <set>
+#include <utility>
 
 namespace sylver_gb300 {
 
@@ -28,21 +35,19 @@ class ArenaAlloc {
   static int64_t round64(int64_t v) { return (v + 63) / 64 * 64; }
   void reset() {
     free_.clear();
+    bylen_.clear();
     top_ = 0;
     high_ = 0;
   }
   // start of a block of `size` elements
   int64_t alloc(int64_t size) {
     size = round64(size);
-    auto best = free_.end();
-    for (auto it = free_.begin(); it != free_.end(); ++it) {
-      const int64_t len = it->second - it->first;
-      if (len >= size && (best == free_.end() || len < best->second - best->first)) best = it;
-    }
-    if (best != free_.end()) {
-      const int64_t a = best->first, b = best->second;
-      free_.erase(best);
-      if (b > a + size) free_[a + size] = b;
+    auto best = bylen_.lower_bound({size, INT64_MIN});
+    if (best != bylen_.end()) {
+      const int64_t a = best->second, b = a + best->first;
+      bylen_.erase(best);
+      free_.erase(a);
+      if (b > a + size) add(a + size, b);
       return a;
     }
     const int64_t a = top_;
@@ -57,26 +62,33 @@ class ArenaAlloc {
     auto next = free_.lower_bound(a);
     if (next != free_.end() && next->first == b) {
       b = next->second;
+      bylen_.erase({next->second - next->first, next->first});
       next = free_.erase(next);
     }
     if (next != free_.begin()) {
       auto prev = std::prev(next);
       if (prev->second == a) {
         a = prev->first;
+        bylen_.erase({prev->second - prev->first, prev->first});
         free_.erase(prev);
       }
     }
     if (b == top_) {
       top_ = a;
     } else {
-      free_[a] = b;
+      add(a, b);
     }
   }
   int64_t top() const { return top_; }
   int64_t high_water() const { return high_; }
 
  private:
-  std::map<int64_t, int64_t> free_;  // start -> end
+  void add(int64_t a, int64_t b) {
+    free_[a] = b;
+    bylen_.insert({b - a, a});
+  }
+  std::map<int64_t, int64_t> free_;           // start -> end
+  std::set<std::pair<int64_t, int64_t>> bylen_;  // (length, start)
   int64_t top_ = 0, high_ = 0;
 };
 
