@@ -353,7 +353,8 @@ int sylver_gb300_fkeep_counters(void const* fkeep, long* kernel_launches, int* n
  * array in the library image: a level needing more than 2,097,152 doubles
  * (sum of the level's front rows x min(nrhs, 32)) returns
  * SYLVER_ERROR_X_SIZE.  The first call on a device looks up that array's
- * address; make it before any stream capture.  All calls share the array,
+ * address.  The call waits for its stream before returning, so it is not
+ * for use while that stream is being captured.  All calls share the array,
  * so calls that overlap on the GPU race.  Returns a reference flag. */
 int spldlt_tree_solve_fwd_noalloc_dbl(bool posdef, void const* tree, int nrhs, double* x_dev,
                                       int ldx, void* stream);

@@ -15,8 +15,9 @@
 //    part of the library image: every GPU that loads the library holds it
 //    until the process exits.
 //  * Set-up: the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current and caches it; make that
-//    first call before any stream capture.
+//    (cudaGetSymbolAddress) with that device current and caches it.  Every
+//    call waits for its stream before returning, so the entry point is not
+//    for use while that stream is being captured.
 //  * Device: the factorization lives on the library's device.  The call is
 //    refused (SYLVER_ERROR_CALL_SEQUENCE) when another device is current or
 //    the caller's stream belongs to another device, before anything runs.
