@@ -31,10 +31,12 @@ template <typename ACC> constexpr int RQ_MID = sizeof(ACC) == 8 ? 8 : 16;
 
 template <typename T> __device__ __forceinline__ void aadd(T* p, T v) { atomicAdd(p, v); }
 
-// The large-front solve steps use programmatic dependent launch
-// (pdl_trigger / pdl_wait): a step lets the next one launch at once, and
-// its CTAs stage the factor data they need (which no step writes) before
-// they wait for the previous step's grid.
+// The large fronts' pivot rows are solved in 256-column block steps.  FP32:
+// one dataflow launch per level and direction (k_chain, below) whose tasks
+// hand each step to the next through counters.  FP64: one launch per step
+// with programmatic dependent launch (pdl_trigger / pdl_wait): a step lets
+// the next one launch at once, and its CTAs stage the factor data they need
+// (which no step writes) before they wait for the previous step's grid.
 
 template <typename T, typename ACC>
 __global__ void __launch_bounds__(256) k_solve_fwd(const T* __restrict__ arena,
@@ -777,16 +779,16 @@ template <> struct Vec4<double> {
 };
 
 // Diagonal block of a 256-column step as a product with its explicit
-// inverse, DMV_ROWS = 8 output rows per task (32 tasks per block), 256
-// threads:
+// inverse, DR output rows per task (256 / DR tasks per block), 256 threads:
 //   forward   y_b = X v,    v = xs(block)        -> ys(block)
 //   backward  z_b = X^T v,  v = xs(block) - tt   -> ys(block)
+//             (dataflow sweeps: u_b = X^T xs(block), no accumulator)
 // (X^T read from the transposed copy, so both directions read the matrix
-// coalesced down a column.)  Thread (row i, k-phase g) sums k = g (mod 32);
-// the phases are reduced through shared memory.  The backward step reads
-// accumulator (c0/256)&1 and clears the other one, which the next (lower)
-// block's reduction fills.  With PDL the inverse slice is staged before the
-// wait for the previous launch.
+// coalesced down a column.)  Thread (row i, k-phase g) sums k = g (mod
+// 256 / DR); the phases are reduced through shared memory.  The per-step
+// backward launch reads accumulator (c0/256)&1 and clears the other one,
+// which the next (lower) block's reduction fills.  The inverse slice is
+// staged before the wait for the data earlier steps write.
 template <typename T, typename ACC, int DR = DMV_ROWS> constexpr size_t diag_mv_smem() {
   return sizeof(T) * DR * SW +
          sizeof(ACC) * ((256 / DR) * DR * (RGn<ACC>::v + 1) + SW * RGP<ACC>::v);
