@@ -644,10 +644,15 @@ __global__ void __launch_bounds__(256) k_inv_block(const T* __restrict__ arena,
 #pragma unroll
       for (int q = 0; q < 16; ++q) acc[q] = T(0);
       for (int k = j; k < i; ++k) {
+        // both tiles read along their stored columns (consecutive threads,
+        // consecutive addresses)
         for (int e = tid; e < LB * LB; e += blockDim.x) {
-          int rr = e % LB, kk = e / LB;
-          int grow = LB * i + rr, gcol = LB * k + kk;
+          const int rr = e % LB, kk = e / LB;
+          const int grow = LB * i + rr, gcol = LB * k + kk;
           As[kk * 65 + rr] = (grow < bw && gcol < bw) ? L[(int64_t)(c0 + gcol) * f.ld + c0 + grow] : T(0);
+        }
+        for (int e = tid; e < LB * LB; e += blockDim.x) {
+          const int kk = e % LB, rr = e / LB;
           Bs[rr * 65 + kk] = X[(int64_t)(LB * j + rr) * SW + LB * k + kk];  // B(kk, rr) = X_kj
         }
         __syncthreads();
