@@ -453,7 +453,7 @@ def cpu_baseline(args, gpu_flops):
     oracle.load()
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    k = args.cpu_sample_k or args.k
+    k = args.cpu_sample_k or reference_sample_k(args)
     prob = workload(k, args.nrhs)
     an = sg.Analysis(prob.a.n, prob.a.ptr, prob.a.row, order=prob.order)
     full = prob.a.to_scipy_full()
@@ -506,6 +506,17 @@ def host_cpu():
     return info
 
 
+def reference_sample_k(args):
+    """Grid edge of the reference arm's per-step sample: the largest edge <= args.k
+    (a multiple of 4) whose steps and warm-ups together fit in about three minutes.
+    One full 80^3 step of the FP64 oracle port takes about 23 s on the 16 Neoverse-V2
+    cores of a GB300 host, and the factor work grows like k^6 on these grids."""
+    budget_s, t80 = 180.0, 23.0
+    per_step = budget_s / max(1, args.steps + args.warmup)
+    k = int(80.0 * (per_step / t80) ** (1.0 / 6.0))
+    return max(16, min(args.k, k // 4 * 4))
+
+
 def run_reference(args, rank, ws):
     """CPU reference arm: the oracle port (FP64, all host threads)."""
     import oracle
@@ -515,7 +526,7 @@ def run_reference(args, rank, ws):
     oracle.load()
     cores = os.cpu_count() or 1
     oracle.set_threads(cores)
-    k = args.cpu_sample_k or args.k
+    k = args.cpu_sample_k or reference_sample_k(args)
     prob = workload(k, args.nrhs)
     an = sg.Analysis(prob.a.n, prob.a.ptr, prob.a.row, order=prob.order)
     sy = an.symbolic()
@@ -544,7 +555,10 @@ def run_reference(args, rank, ws):
                        "parallelism": "host threads"},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "GFLOP/s", "cores": cores, "kind": "port",
-                             "sample": f"full factor+solve per step, OpenBLAS {cores} threads"},
+                             "sample": f"one factor+solve+1 IR of lognormal27 {k}^3 (n={prob.a.n}, "
+                                       f"nrhs={args.nrhs}) per step, sized so that {args.steps} "
+                                       f"steps + {args.warmup} warm-ups fit in about 3 minutes; "
+                                       f"FP64, OpenBLAS {cores} threads"},
             "e2e": {"value": v, "unit": "GFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "accuracy": {"bwd_err": be}}
