@@ -43,3 +43,19 @@ def test_two_rank_replica_reduction(tmp_path):
     for p, o in zip(procs, outs):
         assert p.returncode == 0, o
     assert any("rank0 ok 20.0" in o for o in outs)
+
+
+def test_reference_arm_sample_fits_its_budget():
+    """The reference arm times the CPU port on a grid sized so that its steps
+    and warm-ups take about five minutes on the machine's host (one full 80^3
+    step is about 23 s, the work grows like k^6): the full grid for short
+    runs, a smaller one of the same family for the driver's 20 + 5."""
+    import types
+    sys.path.insert(0, ROOT)
+    import bench
+    for steps, warm, want in ((1, 0, 80), (5, 3, 80), (10, 3, 80), (20, 5, 68)):
+        k = bench.reference_sample_k(types.SimpleNamespace(steps=steps, warmup=warm, k=80))
+        assert k == want, (steps, warm, k)
+        assert k % 4 == 0
+        assert (steps + warm) * 23.0 * (k / 80.0) ** 6 <= 300.0 or k == 80
+    assert bench.reference_sample_k(types.SimpleNamespace(steps=20, warmup=5, k=40)) == 40
