@@ -389,9 +389,11 @@ typedef struct {
                             LDL^T: each level's factor columns copied to a compact store and
                             whole blocks given back (LDL^T always gives contribution blocks
                             back) */
-  int solve_dataflow;    /* solves: the block steps of a level's large fronts as one launch of
-                            persistent CTAs that hand each step to the next through counters
-                            (0 or positive, default), or one launch per block step (negative) */
+  int solve_dataflow;    /* solves with FP32 factors: the block steps of a level's large fronts
+                            as one launch of persistent CTAs that hand each step to the next
+                            through counters, or one launch per block step.  0 (default):
+                            dataflow for Cholesky, per-step launches for LDL^T (measured faster
+                            there); positive: dataflow for both; negative: never */
 } sylver_gb300_schedule_t;
 
 /* Set the schedule used by factorizations planned afterwards (a new fkeep);

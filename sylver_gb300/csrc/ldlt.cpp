@@ -661,7 +661,10 @@ static int factorize_ldlt_t(FKeep& fk, cudaStream_t s) {
   put(L.sfr, L.hsfr, s);
   put(L.sscr, L.hsscr, s);
   put(L.sdoff, L.hsdoff, s);
-  fk.splan.dataflow = Schedule::current().solve_dataflow >= 0;
+  // per-step launches unless asked for: on the shifted 7-point 48^3 matrix (4
+  // right-hand sides, five corrections) the dataflow sweeps measured slower
+  // (refined solve 23.0-24.2 ms against 21.0-22.4 ms)
+  fk.splan.dataflow = Schedule::current().solve_dataflow > 0;
   fk.splan.build_tasks(L.hsfr, fk.levels, (int)sizeof(T), s);
   fk.splan.compute_inverses<T>(static_cast<const T*>(fk.factor_base()), L.sfr.as<FrontDesc>(),
                               true, s);

@@ -59,8 +59,8 @@ struct Schedule {
                              // path (multiple of 64, <= 256; <0: 64-column SIMT steps)
   int fs_panel_group = 0;    // FP32 Cholesky: outer panels per trailing fully-summed update
   int front_memory = 0;      // front storage economy: 1 always, < 0 never, 0 when needed
-  int solve_dataflow = 0;    // large-front solve sweeps: one dataflow launch per level
-                             // (>= 0) or one launch per block step (< 0)
+  int solve_dataflow = 0;    // large-front solve sweeps (FP32): one dataflow launch per
+                             // level (Cholesky >= 0, LDL^T > 0) or one launch per block step
   static Schedule& current();
   // default 96 rows: measured faster than the FP32 cap of 128 on 40^3, 56^3 and
   // 80^3 log-normal 27-point matrices (schedule sweeps of the learned scheduler)
