@@ -288,7 +288,8 @@ void* sylver_gb300_stream(void);
 
 /* Re-run the factorization held by fkeep with one CUDA event pair around
  * every launch (no graph) and accumulate per kernel kind:
- * 0 memset, 1 init-A, 2 extend-add, 3 small fronts, 4 panel triangular solve,
+ * 0 memset, 1 init-A, 2 extend-add (or the one-pass assembly that replaces all
+ * three, kinds 0 and 1 then empty), 3 small fronts, 4 panel triangular solve,
  * 5 SIMT tile update, 6 diagonal-block Cholesky, 7 solve inverses, 8 tensor-core
  * panel split, 9 tensor-core update, 10 blocked diagonal block, 11 blocked panel
  * (Cholesky factorizations only).  ms[k] = total milliseconds, launches[k] =

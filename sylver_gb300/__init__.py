@@ -339,6 +339,8 @@ class Factor:
                                            ctypes.byref(ms))
         return dict(kernel_launches=nl.value, nlevels=lv.value, factor_ms=ms.value)
 
+    # "extend_add" also holds the one-pass assembly (zeroing, original entries and
+    # extend-add in one launch per level; "memset" and "init_a" are then empty)
     KINDS = ("memset", "init_a", "extend_add", "small_fronts", "panel_trsm", "update",
              "diag_chol", "diag_inverse", "panel_split", "update_tc", "blk_diag", "blk_panel")
 

@@ -216,6 +216,19 @@ void launch_init_a(T* arena, const double* val, const int64_t* src, const int64_
 template <typename T>
 void launch_extend_add_grouped(T* arena, const ChildDesc* cd, const EaItem* items,
                                const int* grp, const int* maps, int ngroups, cudaStream_t s);
+// Assembly of whole front columns in one pass: columns [j0, j1) of the front
+// at off (m rows, leading dimension ld); column j's original entries are
+// arow/asrc[acp[cbase + j], acp[cbase + j + 1]) (distinct rows >= j) and the
+// children's CB columns that land in it are items[gptr[cbase + j],
+// gptr[cbase + j + 1]) in child order (at most 32, maps that keep row order).
+struct AsmTask {
+  int64_t off;
+  int ld, m, j0, j1, cbase, pad;
+};
+template <typename T>
+void launch_assemble(T* arena, const double* val, const AsmTask* t, int ntask, const int* acp,
+                     const int* arow, const int64_t* asrc, const int* gptr, const EaItem* items,
+                     const ChildDesc* cd, const int* maps, cudaStream_t s);
 // atomic = false: at most one child per parent in this launch (see kernel).
 template <typename T>
 void launch_extend_add(T* arena, const ChildDesc* cd, const EaItem* items, const int* maps,

@@ -174,6 +174,100 @@ __global__ void k_extend_add_grouped(T* __restrict__ arena, const ChildDesc* __r
   }
 }
 
+// Assembly of a level's fronts in one pass (child row maps that keep row
+// order): one warp per front column builds rows [j, m) of column j in chunks
+// of R rows in shared memory — zero, the column's original entries, then each
+// child CB column that lands there, in child order — and stores every chunk
+// once.  The front needs no zeroing beforehand and its entries no read-modify-
+// write, and every entry gets the sum of zeroing + k_init_a + the grouped
+// extend-add: (0 + a) then the children in order, bit for bit.  A child
+// column is read from its first row on in rounds of 32 x U rows; its rows
+// land in increasing parent rows, so the rows of a round that fall inside the
+// chunk are a prefix of it and the next chunk resumes after them.  Each
+// column's metadata is loaded once, spread over the lanes: lane q holds item
+// q's child column (next row, rows, map, source) and the column's first 32
+// original entries sit one per lane.
+template <typename T>
+__global__ void __launch_bounds__(256) k_assemble(T* __restrict__ arena,
+                                                  const double* __restrict__ val,
+                                                  const AsmTask* __restrict__ tasks,
+                                                  const int* __restrict__ acp,
+                                                  const int* __restrict__ arow,
+                                                  const int64_t* __restrict__ asrc,
+                                                  const int* __restrict__ gptr,
+                                                  const EaItem* __restrict__ items,
+                                                  const ChildDesc* __restrict__ cd,
+                                                  const int* __restrict__ maps) {
+  constexpr int R = 4096 / (int)sizeof(T);
+  constexpr int U = 8;
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ T sbuf[8][R];
+  const AsmTask t = tasks[blockIdx.x];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  T* buf = sbuf[warp];
+  for (int j = t.j0 + warp; j < t.j1; j += 8) {
+    T* col = arena + t.off + (int64_t)j * t.ld;
+    const int cj = t.cbase + j;
+    const int a0 = acp[cj], a1 = acp[cj + 1], g0 = gptr[cj], ng = gptr[cj + 1] - g0;
+    int cur = 0, cmc = 0;
+    unsigned long long cmap = 0, csrc = 0;
+    if (lane < ng) {
+      const EaItem it = items[g0 + lane];
+      const ChildDesc c = cd[it.child];
+      cur = it.col;
+      cmc = c.mc;
+      cmap = (unsigned long long)(maps + c.map_off);
+      csrc = (unsigned long long)(arena + c.cb_off + (int64_t)it.col * c.ld_c);
+    }
+    int ar = -1;
+    T av = T(0);
+    if (a0 + lane < a1) {
+      ar = arow[a0 + lane];
+      av = (T)val[asrc[a0 + lane]];
+    }
+    for (int r0 = j; r0 < t.m; r0 += R) {
+      const int nr = min(R, t.m - r0), r1 = r0 + nr;
+      for (int i = lane; i < nr; i += 32) buf[i] = T(0);
+      __syncwarp();
+      if (ar >= r0 && ar < r1) buf[ar - r0] = av;
+      for (int e = a0 + 32 + lane; e < a1; e += 32) {
+        const int r = arow[e];
+        if (r >= r0 && r < r1) buf[r - r0] = (T)val[asrc[e]];
+      }
+      __syncwarp();
+      for (int q = 0; q < ng; ++q) {
+        const int mc = __shfl_sync(FULL, cmc, q);
+        const int* map = reinterpret_cast<const int*>(__shfl_sync(FULL, cmap, q));
+        const T* src = reinterpret_cast<const T*>(__shfl_sync(FULL, csrc, q));
+        int i = __shfl_sync(FULL, cur, q);
+        for (;;) {
+          int pr[U];
+          T v[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int ii = i + u * 32 + lane;
+            pr[u] = ii < mc ? map[ii] : r1;
+            v[u] = ii < mc ? src[ii] : T(0);
+          }
+          int cnt = 0;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const bool ok = pr[u] < r1;
+            if (ok) buf[pr[u] - r0] += v[u];
+            cnt += __popc(__ballot_sync(FULL, ok));
+          }
+          i += cnt;
+          if (cnt < U * 32) break;
+        }
+        if (lane == q) cur = i;
+        __syncwarp();  // this child's additions land before the next one's
+      }
+      for (int i = lane; i < nr; i += 32) col[r0 + i] = buf[i];
+      __syncwarp();
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Whole-front partial Cholesky in shared memory (m <= SMALL_M): eliminate the
 // first n columns and update the contribution block in place.
@@ -329,6 +423,14 @@ void launch_zero_lower(T* arena, const ZeroTask* t, int ntask, cudaStream_t s) {
 }
 
 template <typename T>
+void launch_assemble(T* arena, const double* val, const AsmTask* t, int ntask, const int* acp,
+                     const int* arow, const int64_t* asrc, const int* gptr, const EaItem* items,
+                     const ChildDesc* cd, const int* maps, cudaStream_t s) {
+  if (ntask <= 0) return;
+  k_assemble<T><<<ntask, 256, 0, s>>>(arena, val, t, acp, arow, asrc, gptr, items, cd, maps);
+}
+
+template <typename T>
 void launch_zero_spans(T* arena, const ZeroSpan* t, int ntask, cudaStream_t s) {
   if (ntask <= 0) return;
   k_zero_spans<T><<<ntask, 256, 0, s>>>(arena, t);
@@ -421,6 +523,9 @@ void launch_update(T* arena, const T* abuf, const UpdTask* t, int ntask, cudaStr
                                      cudaStream_t, bool);                                   \
   template void launch_extend_add_grouped<T>(T*, const ChildDesc*, const EaItem*, const int*, \
                                              const int*, int, cudaStream_t);                \
+  template void launch_assemble<T>(T*, const double*, const AsmTask*, int, const int*,       \
+                                   const int*, const int64_t*, const int*, const EaItem*,   \
+                                   const ChildDesc*, const int*, cudaStream_t);             \
   template void launch_small_chol<T>(T*, const SmallTask*, int, int, unsigned*, cudaStream_t); \
   template void launch_diag_chol<T>(T*, const PanelTask*, int, unsigned*, cudaStream_t);     \
   template void launch_panel_trsm<T>(T*, const PanelTask*, int, cudaStream_t);               \

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <climits>
 #include <cstring>
 #include <numeric>
 #include <stdexcept>
@@ -231,10 +232,15 @@ void FKeep::plan_cholesky() {
     }
     arena_elems = std::max<int64_t>(al.high_water(), 1);
   }
-  // zeroing tasks: each front's lower triangle in column ranges of about 64K
-  // entries, level by level (zlv[l] = first task of level l)
+  // zeroing (or one-pass assembly) tasks: each front's lower triangle in
+  // column ranges of about 64K entries, level by level (zlv[l] = first task
+  // of level l); colbase[k] = first column of level-ordered front k in the
+  // per-column tables of the one-pass assembly
   std::vector<ZeroTask> zt;
+  std::vector<AsmTask> at;
   std::vector<int64_t> zlv(levels.size() + 1, 0), ilv(levels.size() + 1, 0);
+  std::vector<int64_t> colbase(ns + 1, 0);
+  for (int k = 0; k < ns; ++k) colbase[k + 1] = colbase[k] + st.nrow[order[k]];
   for (size_t l = 0; l < levels.size(); ++l) {
     zlv[l] = (int64_t)zt.size();
     for (int k = levels[l].f0; k < levels[l].f1; ++k) {
@@ -245,6 +251,7 @@ void FKeep::plan_cholesky() {
         int j1 = j0;
         while (j1 < m && acc < 65536) acc += m - j1++;
         zt.push_back({off[s], ld[s], m, j0, j1});
+        at.push_back({off[s], ld[s], m, j0, j1, (int)colbase[k], 0});
         j0 = j1;
       }
     }
@@ -275,6 +282,60 @@ void FKeep::plan_cholesky() {
   }
   ninit = (int64_t)asrc.size();
   ilv[levels.size()] = ninit;
+
+  // One-pass assembly (k_assemble) when every column's original entries
+  // have distinct rows in the lower triangle, every child's rows land in
+  // increasing parent rows and no front has more than 32 children with a
+  // contribution block; otherwise zeroing + k_init_a + extend-add.
+  std::vector<int> acp, arow, gptr;
+  std::vector<int64_t> asrc_c;
+  one_pass = !init_atomic && colbase[ns] < INT_MAX && ninit < INT_MAX;
+  if (one_pass) {
+    std::vector<int> mark(st.n, -1);
+    for (int s = 0; s < ns && one_pass; ++s) {
+      for (int64_t q = st.rptr[s] - 1; q < st.rptr[s + 1] - 1; ++q)
+        mark[st.rlist[q] - 1] = (int)(q - (st.rptr[s] - 1));
+      int nch = 0;
+      for (int c : st.children[s]) {
+        const int mc = st.nrow[c] - st.ncol[c];
+        if (mc <= 0) continue;
+        ++nch;
+        const int64_t b = st.rptr[c] - 1 + st.ncol[c];
+        for (int i = 1; i < mc && one_pass; ++i)
+          if (mark[st.rlist[b + i] - 1] <= mark[st.rlist[b + i - 1] - 1]) one_pass = false;
+      }
+      if (nch > 32) one_pass = false;
+    }
+  }
+  if (one_pass) {
+    acp.assign(colbase[ns] + 1, 0);
+    arow.resize(ninit);
+    asrc_c.resize(ninit);
+    std::vector<std::pair<int64_t, int64_t>> ent;  // (front entry c * nrow + r, source)
+    for (int k = 0; k < ns && one_pass; ++k) {
+      const int s = order[k], nrow = st.nrow[s];
+      ent.clear();
+      for (int64_t q = st.nptr[s] - 1; q < st.nptr[s + 1] - 1; ++q)
+        ent.push_back({st.nlist[2 * q + 1] - 1, st.nlist[2 * q] - 1});
+      std::stable_sort(ent.begin(), ent.end(),
+                       [](const auto& x, const auto& y) { return x.first < y.first; });
+      int64_t e = acp[colbase[k]];
+      int jn = 0;  // next column whose start is unset
+      for (size_t q = 0; q < ent.size(); ++q) {
+        const int c = (int)(ent[q].first / nrow), r = (int)(ent[q].first % nrow);
+        if (r < c || (q > 0 && ent[q].first == ent[q - 1].first)) {
+          one_pass = false;
+          break;
+        }
+        while (jn <= c) acp[colbase[k] + jn++] = (int)e;
+        arow[e] = r;
+        asrc_c[e] = ent[q].second;
+        ++e;
+      }
+      while (jn <= nrow) acp[colbase[k] + jn++] = (int)e;
+    }
+  }
+  if (one_pass) gptr.assign(colbase[ns] + 1, 0);
 
   // rlist (0-based) and solve descriptors in level order, small fronts first
   std::vector<int> rl0(st.rlist.size());
@@ -326,7 +387,9 @@ void FKeep::plan_cholesky() {
     // level's at once before the first when no block is reused)
     const size_t l = &L - levels.data();
     const size_t l1 = reuse_blocks ? l + 1 : levels.size();
-    if (reuse_blocks || l == 0) {
+    if (one_pass) {
+      if (zlv[l + 1] > zlv[l]) ops.push_back({Op::ASM, zlv[l], zlv[l + 1], 0});
+    } else if (reuse_blocks || l == 0) {
       if (zlv[l1] > zlv[l]) ops.push_back({Op::MEMSET, zlv[l], zlv[l1], 0});
       if (ilv[l1] > ilv[l]) ops.push_back({Op::INIT, ilv[l], ilv[l1], 0});
     }
@@ -369,7 +432,24 @@ void FKeep::plan_cholesky() {
         ++rank;
       }
     }
-    if (ordered && !dests.empty()) {
+    if (one_pass) {
+      // the level's items grouped by parent column in child order, and each
+      // column's item range (the assembly op above reads them)
+      std::stable_sort(dests.begin(), dests.end(), [](const Dest& x, const Dest& y) {
+        return x.p != y.p ? x.p < y.p : (x.pc != y.pc ? x.pc < y.pc : x.rank < y.rank);
+      });
+      size_t q = 0;
+      for (int k = L.f0; k < L.f1; ++k) {
+        const int m = st.nrow[order[k]];
+        for (int j = 0; j < m; ++j) {
+          gptr[colbase[k] + j] = (int)items.size();
+          while (q < dests.size() && dests[q].p == k && dests[q].pc == j)
+            items.push_back(dests[q++].it);
+        }
+      }
+      if (q != dests.size() || !ordered)
+        throw std::runtime_error("one-pass assembly: child rows out of order");
+    } else if (ordered && !dests.empty()) {
       std::stable_sort(dests.begin(), dests.end(), [](const Dest& x, const Dest& y) {
         return x.p != y.p ? x.p < y.p : (x.pc != y.pc ? x.pc < y.pc : x.rank < y.rank);
       });
@@ -592,9 +672,18 @@ void FKeep::plan_cholesky() {
     op_flops[q] = f;
   }
   cudaStream_t s = Runtime::get().stream;
-  zerot.upload(zt, s);
-  amap_src.upload(asrc, s);
-  amap_dst.upload(adst, s);
+  if (one_pass) {
+    gptr[colbase[ns]] = (int)items.size();
+    asmt.upload(at, s);
+    asm_acp.upload(acp, s);
+    asm_arow.upload(arow, s);
+    asm_asrc.upload(asrc_c, s);
+    asm_gptr.upload(gptr, s);
+  } else {
+    zerot.upload(zt, s);
+    amap_src.upload(asrc, s);
+    amap_dst.upload(adst, s);
+  }
   cdesc.upload(cds, s);
   eaitems.upload(items, s);
   eamaps.upload(maps, s);
@@ -677,6 +766,12 @@ void FKeep::run_ops(cudaStream_t s) {
       case Op::INIT:
         launch_init_a<T>(A, val.as<double>(), amap_src.as<int64_t>() + op.a,
                          amap_dst.as<int64_t>() + op.a, cnt, init_atomic, s);
+        break;
+      case Op::ASM:
+        launch_assemble<T>(A, val.as<double>(), asmt.as<AsmTask>() + op.a, (int)cnt,
+                           asm_acp.as<int>(), asm_arow.as<int>(), asm_asrc.as<int64_t>(),
+                           asm_gptr.as<int>(), eaitems.as<EaItem>(), cdesc.as<ChildDesc>(),
+                           eamaps.as<int>(), s);
         break;
       case Op::EA:
         launch_extend_add<T>(A, cdesc.as<ChildDesc>(), eaitems.as<EaItem>() + op.a,
@@ -815,7 +910,8 @@ int FKeep::profile(const double* val_dev, double* ms, long* nl, double* flops, c
   for (size_t q = 0; q < all.size(); ++q) {
     float t = 0.f;
     cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
-    int k = all[q].kind == Op::EAG ? (int)Op::EA : (int)all[q].kind;  // both extend-add
+    // grouped extend-add and one-pass assembly both count as extend-add
+    int k = (all[q].kind == Op::EAG || all[q].kind == Op::ASM) ? (int)Op::EA : (int)all[q].kind;
     ms[k] += t;
     nl[k] += 1;
     flops[k] += op_flops.empty() ? 0.0 : op_flops[q];

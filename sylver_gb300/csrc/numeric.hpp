@@ -117,7 +117,7 @@ struct AKeep {
 
 // One kernel launch of the factor schedule.
 struct Op {
-  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV, SPLIT, TCUPD, BDIAG, BPANEL, EAG } kind;
+  enum Kind { MEMSET, INIT, EA, SMALL, PANEL, UPD, DIAG, INV, SPLIT, TCUPD, BDIAG, BPANEL, EAG, ASM } kind;
   int64_t a = 0, b = 0;  // task range [a, b)
   int aux = 0;           // SMALL: max front rows; SPLIT/TCUPD: tensor-core level
 };
@@ -245,6 +245,9 @@ struct FKeep {
   std::vector<int> op_level;         // level of each op (-1: whole-factor set-up / inverses)
   bool init_atomic = false;
   int64_t ninit = 0;
+  // fronts assembled column by column in one pass per level (k_assemble)
+  // instead of zeroing + original entries + extend-add
+  bool one_pass = false;
   // Cholesky: front blocks placed with contribution blocks given back (when
   // all blocks would take more than half of the device memory)
   bool reuse_blocks = false;
@@ -259,6 +262,7 @@ struct FKeep {
   const void* factor_base() const { return fcopy ? fstore.p : arena.p; }
   size_t factor_bytes() const { return fcopy ? fstore.bytes : arena.bytes; }
   DevMem amap_src, amap_dst, cdesc, eaitems, eamaps, eagroups, small, panel, upd, diagt, zerot;
+  DevMem asmt, asm_acp, asm_arow, asm_asrc, asm_gptr;
   int nzero = 0;
   DevMem dfr, dscr, rlist0, perm0;
   DevMem xp, scratch, bcopy, resid, norms;
