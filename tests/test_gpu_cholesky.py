@@ -246,9 +246,9 @@ def test_solve_rhs_counts_match_oracle(sylver, orc, gpu, nrhs):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_factors_bitwise_reproducible(sylver, gpu, precision):
-    """The extend-add sums each parent entry's children in child order (one
-    launch per child rank, no atomics), so factorizing the same values twice
-    into the same factor storage gives the same bits, FP64 and FP32 (the
+    """The assembly sums each front entry's original value and then its
+    children in child order without atomics, so factorizing the same values
+    twice into the same factor storage gives the same bits, FP64 and FP32 (the
     tensor-core updates included)."""
     import ctypes
     p = w.lognormal27(20, nrhs=1)
@@ -272,9 +272,9 @@ def test_factors_bitwise_reproducible(sylver, gpu, precision):
 def test_front_memory_economy_matches(sylver, orc, gpu):
     """Front storage economy forced on (schedule front_memory = 1: contribution
     blocks given back to later fronts once the parent's level has assembled
-    them, every level zeroed and initialised just before it, the mode large
-    problems take automatically): the same solutions as the default layout,
-    FP64 against the oracle and FP32 with refinement."""
+    them, every level assembled just before it, the mode large problems take
+    automatically): the same solutions as the default layout, FP64 against the
+    oracle and FP32 with refinement."""
     p = w.lognormal27(20, nrhs=2)
     an = sylver.Analysis(p.a.n, p.a.ptr, p.a.row, order=p.order)
     ref = sylver.Factor(an, True, p.a.val).solve(p.rhs)
@@ -291,3 +291,63 @@ def test_front_memory_economy_matches(sylver, orc, gpu):
     assert np.abs(x - ref).max() <= 1e-12 * np.abs(ref).max()
     assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
     assert w.backward_error(p.a.to_scipy_full(), x32, p.rhs).max() <= 1e-14
+
+
+def _comb(nch=40, length=40, nsep=5):
+    """nch independent chains of `length` unknowns, each coupled through its
+    last unknown to a dense separator of nsep: the root front has nch
+    children with contribution blocks."""
+    import scipy.sparse as sp
+    n = nch * length + nsep
+    rows, cols, vals = [], [], []
+    for k in range(nch):
+        b = k * length
+        for i in range(length - 1):
+            rows.append(b + i + 1); cols.append(b + i); vals.append(-1.0)
+        for t in range(nsep):
+            rows.append(nch * length + t); cols.append(b + length - 1); vals.append(-0.5)
+    for t in range(nsep):
+        for u in range(t):
+            rows.append(nch * length + t); cols.append(nch * length + u); vals.append(-0.25)
+    low = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    off = low + low.T
+    d = np.asarray(abs(off).sum(axis=1)).ravel() + 1.0
+    return w.SymMatrix.from_scipy(sp.csr_matrix(off + sp.diags(d)))
+
+
+@pytest.mark.parametrize("case", ["grid", "comb40"])
+def test_assembly_paths(sylver, orc, gpu, case):
+    """Fronts are assembled in one pass per level (zero, original entries and
+    children summed per column, stored once) unless a front has more than 32
+    children with contribution blocks, when zeroing + original entries +
+    extend-add run instead.  The per-kind profile shows which ran; both solve
+    like the FP64 oracle and reach 1e-14 with FP32 factors and refinement."""
+    if case == "grid":
+        p = w.lognormal27(12, nrhs=2)
+        a, order, rhs = p.a, p.order, p.rhs
+    else:
+        a = _comb()
+        order = w.natural_order(a.n)
+        rhs = np.asfortranarray(np.random.default_rng(9).standard_normal((a.n, 2)))
+    an = sylver.Analysis(a.n, a.ptr, a.row, order=order)
+    sy = an.symbolic()
+    par = np.asarray(sy["sparent"]) - 1
+    nrow, ncol = np.diff(sy["rptr"]), np.diff(sy["sptr"])
+    kids = np.bincount(par[(par >= 0) & (par < sy["nnodes"]) & (nrow > ncol)],
+                       minlength=sy["nnodes"])
+    one_pass = kids.max() <= 32
+    assert one_pass == (case == "grid")
+    f = sylver.Factor(an, True, a.val)
+    assert f.flag == 0
+    prof = f.profile()
+    if one_pass:
+        assert prof["memset"]["launches"] == 0 and prof["init_a"]["launches"] == 0
+    else:
+        assert prof["memset"]["launches"] > 0 and prof["init_a"]["launches"] > 0
+    assert prof["extend_add"]["launches"] > 0
+    x = f.solve(rhs)
+    o = orc.OracleFactor(True, sy, a.val)
+    xo = o.solve(rhs)
+    assert np.abs(x - xo).max() <= 1e-10 * np.abs(xo).max()
+    f32 = sylver.Factor(an, True, a.val, precision=sylver.FP32, ir_max_iter=10)
+    assert w.backward_error(a.to_scipy_full(), f32.solve(rhs), rhs).max() <= 1e-14
