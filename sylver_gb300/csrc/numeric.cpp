@@ -197,11 +197,11 @@ void FKeep::plan_cholesky() {
     }
   }
   // front blocks: one after another when they all fit in half of the device
-  // memory (zeroed and initialised by one launch each at the start);
-  // otherwise placed level by level with the contribution blocks a level
-  // assembled given back before the next level is placed (the schedule runs
-  // the levels in order on one stream, so each level's zeroing, just before
-  // it, comes after that assembly)
+  // memory; otherwise placed level by level with the contribution blocks a
+  // level assembled given back before the next level is placed (the schedule
+  // runs the levels in order on one stream, so each level's assembly, which
+  // writes every entry of its fronts' lower triangles, comes after the
+  // previous level read those blocks)
   off.assign(ns, 0);
   ld.assign(ns, 0);
   int64_t blocks = 0;
@@ -383,8 +383,9 @@ void FKeep::plan_cholesky() {
   ops.clear();
   op_level.clear();
   for (auto& L : levels) {
-    // the level's front blocks <- 0, then the original entries (every
-    // level's at once before the first when no block is reused)
+    // one-pass assembly of the level's fronts; otherwise the front blocks
+    // <- 0, then the original entries (every level's at once before the
+    // first when no block is reused), then the extend-add below
     const size_t l = &L - levels.data();
     const size_t l1 = reuse_blocks ? l + 1 : levels.size();
     if (one_pass) {
